@@ -1,0 +1,343 @@
+"""Benchmark: closest-hit traversal throughput (Mrays/s) and build time on the
+incoherent 1M-triangle scene.
+
+Workload (one "step"): closest-hit traversal of 16,777,216 incoherent rays
+through the 4-wide MBVH of 1,000,000 triangles (centroids uniform in the unit
+cube, vertices at centroid + unit direction x log-normal(median 0.005,
+sigma 0.5)), built with locally-ordered clustering and collapsed to an MBVH.
+Rays start uniformly on a radius-2 sphere around the cube centre and point at
+uniform points in the cube. All data is seeded synthetic input.
+
+Default arm: the CUDA library. ``value`` is device-resident throughput
+(CUDA events around each traversal launch, L2 flushed between steps);
+``e2e`` is the same metric through the C ABI's host-buffer entry point
+(rtbvh_intersect_mbvh_batch) with the ray upload and hit download inside the
+timed region. ``--impl reference`` times the CPU restatement of the
+reference's rayon traversal on all host cores over bounded ray samples.
+
+Multi-GPU (torchrun, one rank per GPU): replicas only -- every rank traces its
+own copy of the workload; ``value`` is the sum over ranks of rays divided by
+the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TRIS = 1_000_000
+N_RAYS = 16_777_216
+SCENE_SEED, RAY_SEED = 2, 3
+METRIC = "closest-hit Mrays/s (1M-tri incoherent LOCB+MBVH, 16.7M rays)"
+B_IN, B_OUT, B_NODE, B_TRI = 24, 16, 128, 40  # algorithmic bytes: ray in, hit out, quad node, triangle (36 + index 4)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_scene():
+    from rtbvh_gb300 import scenes
+    tris = scenes.incoherent(N_TRIS, seed=SCENE_SEED)
+    rays, tmax = scenes.incoherent_rays(N_RAYS, seed=RAY_SEED)
+    return tris, rays, tmax
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_gpu(args):
+    import torch
+
+    import rtbvh_gb300 as rb
+    from rtbvh_gb300 import build as libbuild
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    libbuild.build()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    tris, rays, tmax = make_scene()
+    d_tris = torch.from_numpy(tris).cuda()
+    d_rays = torch.from_numpy(rays).cuda()
+    d_tmax = torch.from_numpy(tmax).cuda()
+
+    # ------------------------------------------------------------ build
+    build_ms, mbvh_ms = [], []
+    for i in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bvh = rb.Builder(primitives=rb.Triangles(d_tris)).construct_locally_ordered_clustered(host_mirror=False)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        mbvh = rb.Mbvh.construct(bvh, host_mirror=False)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if i > 0:
+            build_ms.append((t1 - t0) * 1e3)
+            mbvh_ms.append((t2 - t1) * 1e3)
+
+    # ------------------------------------------------------------ roofline inputs
+    _, st = mbvh.intersect(d_rays, stats=True)
+    st = st.to(torch.int64)
+    visits = float(st[:, 0].sum())
+    tests = float(st[:, 1].sum())
+    max_stack = int(st[:, 2].max())
+    alg_bytes = N_RAYS * (B_IN + B_OUT) + B_NODE * visits + B_TRI * tests
+    status = mbvh.status()
+    if status != rb.ResultCode.Ok:
+        raise RuntimeError(f"traversal reported {status!r}")
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        hits, _ = mbvh.intersect(d_rays)
+        return hits
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(float(len(times)))
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+    ms = statistics.mean(times)
+    total_ms = sum(times)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t)
+        dist.barrier()
+    value = ws * N_RAYS * args.steps / (total_ms * 1e-3) / 1e6
+
+    # any-hit on the same structure (tmax = 0.5 x distance)
+    for _ in range(2):
+        mbvh.intersect(d_rays, t_max=d_tmax, any_hit=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    mbvh.intersect(d_rays, t_max=d_tmax, any_hit=True)
+    e1.record(stream)
+    e1.synchronize()
+    any_ms = e0.elapsed_time(e1)
+
+    # ------------------------------------------------------------ e2e through the C ABI with host buffers
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((N_RAYS, 4), dtype=torch.float32).pin_memory()
+    lib = rb.load_library()
+    import ctypes
+    for _ in range(2):
+        lib.rtbvh_intersect_mbvh_batch(mbvh.handle, ctypes.c_void_p(h_rays.data_ptr()), None, N_RAYS,
+                                       ctypes.c_void_p(h_hits.data_ptr()), 0)
+    e2e_times = []
+    for _ in range(max(3, args.steps // 2)):
+        t0 = time.perf_counter()
+        rc = lib.rtbvh_intersect_mbvh_batch(mbvh.handle, ctypes.c_void_p(h_rays.data_ptr()), None, N_RAYS,
+                                            ctypes.c_void_p(h_hits.data_ptr()), 0)
+        e2e_times.append(time.perf_counter() - t0)
+        if rc != 0:
+            raise RuntimeError(f"rtbvh_intersect_mbvh_batch -> {rc}")
+    e2e = ws * N_RAYS / statistics.median(e2e_times) / 1e6
+
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "trace_mbvh_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(tris, rays)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "incoherent-1M-locb-mbvh", "triangles": N_TRIS, "rays": N_RAYS,
+                       "builder": "locally-ordered clustering (radius 14, grid 1024) + 4-wide MBVH",
+                       "query": "closest-hit t/u/v/prim", "l2": "flushed between steps (256 MB write)",
+                       "parallelism": "replicas" if ws > 1 else "single"},
+            "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 24,
+                    "d2h_bytes_per_step": N_RAYS * 16},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 3), "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "bytes_per_ray": round(alg_bytes / N_RAYS, 1),
+                         "mean_node_visits": round(visits / N_RAYS, 3),
+                         "mean_tri_tests": round(tests / N_RAYS, 3)},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "build_ms": {"locb": round(statistics.median(build_ms), 3), "mbvh": round(statistics.median(mbvh_ms), 3)},
+            "any_hit": {"value": round(ws * N_RAYS / (any_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
+                        "t_max": "0.5 x distance"},
+            "max_stack_depth": max_stack,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(tris, rays, threads=None, sample=1_000_000):
+    """CPU restatement of the reference (oracle) on the host cores: LOCB +
+    MBVH build once, then the rayon-style chunked traversal of a ray sample."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    a, c = oracle.triangle_prep(tris)
+    t0 = time.perf_counter()
+    nodes, idx = oracle.build(a, c, "locb", threads=threads)
+    m = oracle.mbvh(nodes)
+    build_s = time.perf_counter() - t0
+    sub = rays[:sample]
+    t0 = time.perf_counter()
+    oracle.trace("mbvh", m, idx, tris.reshape(-1, 9), sub, threads=threads, stats=False)
+    dt = time.perf_counter() - t0
+    return {"value": round(len(sub) / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"first {len(sub)} of the {N_RAYS} rays; LOCB+MBVH build {build_s:.2f} s (not in value)"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's traversal on
+    all host cores, each step a bounded sample of the same workload."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from oracle import buildlib
+    buildlib.build()
+    tris, rays, _ = make_scene()
+    threads = os.cpu_count() or 1
+    a, c = oracle.triangle_prep(tris)
+    nodes, idx = oracle.build(a, c, "locb", threads=threads)
+    m = oracle.mbvh(nodes)
+    flat = tris.reshape(-1, 9)
+    sample = 500_000
+    times = []
+    for s in range(args.warmup + args.steps):
+        lo = (s * sample) % (N_RAYS - sample)
+        sub = rays[lo:lo + sample]
+        t0 = time.perf_counter()
+        oracle.trace("mbvh", m, idx, flat, sub, threads=threads, stats=False)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    ms = statistics.mean(times) * 1e3
+    value = sample * len(times) / sum(times) / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "incoherent-1M-locb-mbvh", "triangles": N_TRIS, "rays": N_RAYS,
+                   "sample_rays_per_step": sample},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} consecutive rays per step of the {N_RAYS}-ray set"},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,250 @@
+/*
+ * rtbvh.h -- C ABI of the GB300 BVH build + ray traversal library
+ * (librtbvh_gb300.so; also installed as librtbvh_rs.so).
+ *
+ * Part 1 is a drop-in for the C ABI of meirbon/rtbvh's `rtbvh_ffi` crate
+ * (rtbvh_ffi/src/lib.rs, header generated by cbindgen in rtbvh_ffi/build.rs):
+ * same symbol names, same enum values, same struct layouts, same ownership
+ * (the library owns every structure; handles are by-value views that stay
+ * valid until free_*). Builds run on the GPU; node arrays are mirrored to
+ * host memory so that the handle pointers and the host-callback traversal
+ * entry points keep working.
+ *
+ * Part 2 adds GPU entry points (prefix rtbvh_gpu_) that take device pointers
+ * and a CUDA stream: builds from device triangles, the fused closest-hit /
+ * any-hit traversal, refit and the differentiable backward pass. They return
+ * ResultCode, extended by the values marked "extension" below.
+ */
+#ifndef RTBVH_H
+#define RTBVH_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* rtbvh_ffi/src/lib.rs:17-25 */
+typedef enum ResultCode {
+  Ok = 0,
+  Error = 1,
+  NoPrimitives = 2,
+  InequalAabbsAndPrimitives = 3,
+  Nan = 4,
+  /* extensions (no counterpart in the reference) */
+  DeviceError = 5,   /* a CUDA call failed */
+  Timeout = 6,       /* a bounded device-side wait gave up */
+  StackOverflow = 7, /* a traversal stack bound was exceeded */
+  OutOfMemory = 8,
+  InvalidArgument = 9
+} ResultCode;
+
+/* rtbvh_ffi/src/lib.rs:129-133 (repr(u32)) */
+#ifdef __cplusplus
+enum BvhType : uint32_t {
+  LocallyOrderedClustered = 0,
+  BinnedSAH = 1,
+};
+#else
+enum BvhType {
+  LocallyOrderedClustered = 0,
+  BinnedSAH = 1,
+};
+typedef uint32_t BvhType;
+#endif
+
+/* rtbvh_ffi/src/lib.rs:144-151 -- 32 bytes */
+typedef struct RTAabb {
+  float min[3];
+  int32_t count;
+  float max[3];
+  int32_t left_first;
+} RTAabb;
+
+/* rtbvh_ffi/src/lib.rs:175-179 -- 32 bytes */
+typedef struct RTBvhNode {
+  RTAabb aabb;
+} RTBvhNode;
+
+/* rtbvh_ffi/src/lib.rs:197-208 -- 128 bytes, quad node in SoA form */
+typedef struct RTMbvhNode {
+  float min_x[4];
+  float max_x[4];
+  float min_y[4];
+  float max_y[4];
+  float min_z[4];
+  float max_z[4];
+  int32_t children[4];
+  int32_t counts[4];
+} RTMbvhNode;
+
+/* rtbvh_ffi/src/lib.rs:210-220 */
+typedef struct RTBvh {
+  uint32_t id;
+  uint32_t node_count;
+  const RTBvhNode *nodes;
+  uint32_t index_count;
+  const uint32_t *indices;
+} RTBvh;
+
+/* rtbvh_ffi/src/lib.rs:234-244 */
+typedef struct RTMbvh {
+  uint32_t id;
+  uint32_t node_count;
+  const RTMbvhNode *nodes;
+  uint32_t index_count;
+  const uint32_t *indices;
+} RTMbvh;
+
+/* Candidate callback of the host traversal entry points:
+ * (primitive id, in/out t, user data) -> true stops the traversal. */
+typedef bool (*RTIntersectFn)(uint32_t, float *, void *);
+
+/* ------------------------------------------------------------------ part 1 */
+
+/* rtbvh_ffi/src/lib.rs:345-389. The spatial-split builder is not part of this
+ * library: always returns Error and leaves *result untouched. */
+ResultCode create_spatial_Bvh(const RTAabb *aabbs, uintptr_t prim_count, const float *centers, uintptr_t stride,
+                              const float *vertices, uintptr_t vertex_stride, uintptr_t triangle_stride,
+                              uint32_t prims_per_leaf, RTBvh *result);
+
+/* rtbvh_ffi/src/lib.rs:428-493. Host inputs; the build runs on the GPU.
+ * centers/result NULL -> Error; center_stride must be 12 or 16 (the reference
+ * aborts on any other value, this library returns Error); aabbs NULL -> the
+ * boxes are the centre points; prims_per_leaf 0 -> 1. */
+ResultCode create_bvh(const RTAabb *aabbs, uintptr_t prim_count, const float *centers, uintptr_t center_stride,
+                      uintptr_t prims_per_leaf, BvhType bvh_type, RTBvh *result);
+
+/* rtbvh_ffi/src/lib.rs:499-513 */
+ResultCode create_mbvh(RTBvh bvh, RTMbvh *mbvh);
+
+/* rtbvh_ffi/src/lib.rs:519-538. Recomputes the node boxes of a stored Bvh from
+ * new primitive boxes, on the GPU. The boxes equal the reference's bit for
+ * bit; the node topology is kept (the reference also zeroes every node's
+ * count/left_first, a defect this library does not reproduce). */
+ResultCode refit(const RTAabb *aabbs, RTBvh bvh);
+
+/* rtbvh_ffi/src/lib.rs:551-581 (host traversal calling back per candidate) */
+ResultCode intersect(RTBvh bvh, const float *origin, const float *direction, float *t, void *user_data,
+                     RTIntersectFn intersect);
+
+/* rtbvh_ffi/src/lib.rs:599-686 */
+ResultCode intersect_packet(RTBvh bvh, const float *origin_x, const float *origin_y, const float *origin_z,
+                            const float *direction_x, const float *direction_y, const float *direction_z, float *t,
+                            void *user_data, RTIntersectFn intersect);
+
+/* rtbvh_ffi/src/lib.rs:700-731 */
+ResultCode intersect_mbvh(RTMbvh bvh, const float *origin, const float *direction, float *t, void *user_data,
+                          RTIntersectFn intersect);
+
+/* rtbvh_ffi/src/lib.rs:749-835 */
+ResultCode intersect_mbvh_packet(RTMbvh bvh, const float *origin_x, const float *origin_y, const float *origin_z,
+                                 const float *direction_x, const float *direction_y, const float *direction_z,
+                                 float *t, void *user_data, RTIntersectFn intersect);
+
+/* rtbvh_ffi/src/lib.rs:837-849 */
+void free_bvh(RTBvh bvh);
+void free_mbvh(RTMbvh bvh);
+
+/* ------------------------------------------------------------------ part 2
+ * GPU entry points. No counterpart in the reference (it has no GPU path);
+ * each is the device-side form of the reference call named beside it.
+ * `stream` is a cudaStream_t (NULL: the legacy default stream).
+ * Device arrays:
+ *   vertices  n x 9 float   v0, v1, v2 of triangle i
+ *   aabbs     n x RTAabb
+ *   rays      R x 6 float   origin, direction
+ *   t_max     R float       per-ray upper bound (NULL: 1e34, Ray::new)
+ *   hits      R x 4         float t, float u, float v, int32 prim (-1: miss)
+ */
+typedef void *rtbvh_stream_t;
+
+/* flags for the build entry points */
+#define RTBVH_FLAG_NO_HOST_MIRROR 1u /* keep nodes on the device only (handle pointers are NULL) */
+
+/* flags for the trace entry points */
+#define RTBVH_TRACE_ANY_HIT 1u /* stop at the first accepted triangle (occlusion) */
+#define RTBVH_TRACE_STATS 2u   /* write per-ray node visits / triangle tests / max stack depth */
+
+/* Builder::construct_binned_sah / construct_locally_ordered_clustered on
+ * device triangles (src/bvh.rs:87-137, with aabbs = Triangle::aabb and
+ * centres = Triangle::center of shared/src/lib.rs:27-39). The triangles are
+ * kept with the structure for traversal. */
+ResultCode rtbvh_gpu_create_bvh_from_triangles(const float *vertices, uintptr_t prim_count,
+                                               uintptr_t prims_per_leaf, BvhType bvh_type, uint32_t flags,
+                                               rtbvh_stream_t stream, RTBvh *result);
+
+/* create_bvh (rtbvh_ffi/src/lib.rs:428-493) with device inputs. centers has
+ * center_stride bytes per primitive (12 or 16). aabbs must not be NULL. */
+ResultCode rtbvh_gpu_create_bvh(const RTAabb *aabbs, uintptr_t prim_count, const float *centers,
+                                uintptr_t center_stride, uintptr_t prims_per_leaf, BvhType bvh_type, uint32_t flags,
+                                rtbvh_stream_t stream, RTBvh *result);
+
+/* Mbvh::construct (src/bvh.rs:381-404) on the GPU. */
+ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t stream, RTMbvh *result);
+
+/* Attaches device triangles (prim-id order) to a Bvh (is_mbvh = 0) or Mbvh
+ * (is_mbvh = 1) for the fused traversal; they are re-laid in leaf order
+ * (v0, v1-v0, v2-v0). Structures built by rtbvh_gpu_create_bvh_from_triangles
+ * (and Mbvhs made from them) already carry them. */
+ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const float *vertices, uintptr_t prim_count,
+                                   rtbvh_stream_t stream);
+
+/* MbvhIndexIterator (src/iter_indices.rs:212-313) driving the triangle test
+ * of src/builders/spatial_sah.rs:132-163, for R rays, one ray per thread.
+ * Asynchronous on `stream`; errors found on the device (stack overflow) are
+ * reported by rtbvh_gpu_status. stats: R x 3 uint32 or NULL. */
+ResultCode rtbvh_gpu_intersect_mbvh(RTMbvh mbvh, const float *rays, const float *t_max, uintptr_t ray_count,
+                                    float *hits, uint32_t flags, uint32_t *stats, rtbvh_stream_t stream);
+
+/* BvhIndexIterator (src/iter_indices.rs:18-107) driving the triangle test. */
+ResultCode rtbvh_gpu_intersect_bvh(RTBvh bvh, const float *rays, const float *t_max, uintptr_t ray_count,
+                                   float *hits, uint32_t flags, uint32_t *stats, rtbvh_stream_t stream);
+
+/* Same as rtbvh_gpu_intersect_mbvh with HOST rays / t_max / hits: copies in,
+ * traces and copies out in chunks on two internal streams, and returns when
+ * the hits are in host memory. Page-locked host buffers give full speed. */
+ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float *rays, const float *t_max, uintptr_t ray_count,
+                                      float *hits, uint32_t flags);
+
+/* Reads (and clears) the device status word of a structure: Ok, or the first
+ * error a traversal on it raised (StackOverflow, Timeout). Synchronises. */
+ResultCode rtbvh_gpu_status(uint32_t structure_id, int is_mbvh);
+
+/* Device views of a structure's arrays (nodes, indices, leaf-ordered
+ * triangles 3 x float4 per index slot). Pointers stay valid until free_*. */
+typedef struct RTGpuView {
+  const void *nodes;
+  uint32_t node_count;
+  const uint32_t *indices;
+  uint32_t index_count;
+  const float *leaf_triangles;
+} RTGpuView;
+ResultCode rtbvh_gpu_view(uint32_t structure_id, int is_mbvh, RTGpuView *view);
+
+/* Bvh::refit (src/bvh.rs:176-205) on the GPU from device triangles or device
+ * aabbs (exactly one non-NULL); updates the Bvh and, if mbvh_id != UINT32_MAX,
+ * re-collapses that Mbvh from it and re-lays its triangles. */
+ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float *vertices, const RTAabb *aabbs, uint32_t mbvh_id,
+                           rtbvh_stream_t stream);
+
+/* Backward pass of the closest-hit triangle test for rays traced with
+ * rtbvh_gpu_intersect_mbvh (hits as written there). Maps upstream
+ * (dL/dt, dL/du, dL/dv) per ray (R x 3 float) to dL/dvertices (n x 9 float,
+ * overwritten, summed in a fixed order per triangle so that the result is
+ * deterministic) and dL/dray (R x 6 float: origin, direction; NULL to skip).
+ * vertices are the triangles the hits were traced against (prim-id order). */
+ResultCode rtbvh_gpu_intersect_backward(const float *vertices, uintptr_t prim_count, const float *rays,
+                                        const float *hits, const float *grad_tuv, uintptr_t ray_count,
+                                        float *grad_vertices, float *grad_rays, rtbvh_stream_t stream);
+
+/* Library version string. */
+const char *rtbvh_gpu_version(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* RTBVH_H */

@@ -1,0 +1,1108 @@
+// rtbvh oracle -- TEST INFRASTRUCTURE ONLY.
+//
+// A plain C++ restatement of the CPU algorithms of meirbon/rtbvh (Rust crate
+// `rtbvh` 0.6.2 plus its `rtbvh_ffi` wrapper) for the BVH construction and
+// single-ray traversal path. It exists to check the CUDA implementation in
+// `rtbvh_gb300/` and to serve as the timed CPU baseline. Only `tests/`,
+// `__graft_entry__.smoke()` and the CPU-baseline leg of `bench.py` may load it;
+// the product library never links or calls it.
+//
+// Each function names the reference file:line it follows (paths relative to
+// the reference project root).
+//
+// Parity status of this restatement:
+//  * pinned by the reference's own known-answer tests: morton_split
+//    (src/morton.rs:109-115), prefix_sum (src/utils.rs:295-345), build input
+//    errors (src/lib.rs:28-64), builder structural checks on the teapot
+//    (src/builders/binned_sah.rs:407-458, src/builders/locb.rs:336-388), the
+//    five-triangle case (src/lib.rs:246-311) and the FFI quad hit at t == 1
+//    (rtbvh_ffi/src/lib.rs:945-1060);
+//  * unpinned: exact node layouts, split choices, hit ids and t values on real
+//    scenes. No reference test pins them and the Rust crate cannot be compiled
+//    here (no cargo/rustc), so they follow the reference source line by line.
+//
+// Floating-point conventions (the reference leans on `glam`, whose version is
+// not pinned by the reference):
+//  * Vec3 is scalar: dot is ((x*x') + (y*y')) + (z*z'), cross is the standard
+//    component formula, no FMA contraction (this file must be compiled with
+//    -ffp-contract=off).
+//  * Vec3::min/max follow Rust f32::min/max: a NaN operand is ignored. For the
+//    unspecified -0.0/+0.0 tie this restatement returns -0.0 for min and +0.0
+//    for max, which keeps unions order-independent.
+//  * Vec4 (SSE) min/max follow _mm_min_ps/_mm_max_ps: min(a,b) = a<b ? a : b,
+//    max(a,b) = a>b ? a : b (NaN selects the second operand).
+//  * `f32 as i32` / `as usize` saturate and map NaN to 0 (Rust semantics).
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------- scalars
+inline float rs_min(float a, float b) {
+  if (a != a) return b;
+  if (b != b) return a;
+  if (a < b) return a;
+  if (b < a) return b;
+  return std::signbit(a) ? a : b;
+}
+inline float rs_max(float a, float b) {
+  if (a != a) return b;
+  if (b != b) return a;
+  if (a > b) return a;
+  if (b > a) return b;
+  return std::signbit(a) ? b : a;
+}
+inline float sse_min(float a, float b) { return a < b ? a : b; }
+inline float sse_max(float a, float b) { return a > b ? a : b; }
+
+// Rust `f32 as i32`.
+inline int32_t rs_f32_to_i32(float f) {
+  if (f != f) return 0;
+  if (f >= 2147483648.0f) return INT32_MAX;
+  if (f <= -2147483648.0f) return INT32_MIN;
+  return (int32_t)f;
+}
+// Rust `f32 as usize` (64-bit).
+inline uint64_t rs_f32_to_usize(float f) {
+  if (f != f) return 0;
+  if (f <= 0.0f) return 0;
+  if (f >= 18446744073709551616.0f) return UINT64_MAX;
+  return (uint64_t)f;
+}
+
+struct V3 {
+  float x, y, z;
+  float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+inline V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+inline V3 sub(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline float dot(V3 a, V3 b) { return ((a.x * b.x) + (a.y * b.y)) + (a.z * b.z); }
+inline V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+
+// ---------------------------------------------------------------- Aabb
+// src/aabb.rs:13-20 -- {min, extra1, max, extra2}, 32 bytes.
+struct Aabb {
+  float min[3];
+  int32_t extra1;
+  float max[3];
+  int32_t extra2;
+};
+static_assert(sizeof(Aabb) == 32, "Aabb must be 32 bytes");
+
+// src/aabb.rs:49-57
+inline Aabb aabb_new() {
+  Aabb a;
+  for (int i = 0; i < 3; ++i) { a.min[i] = 1e34f; a.max[i] = -1e34f; }
+  a.extra1 = 0;
+  a.extra2 = 0;
+  return a;
+}
+// src/aabb.rs:251-261
+inline void aabb_grow(Aabb& a, V3 p) {
+  for (int i = 0; i < 3; ++i) { a.min[i] = rs_min(a.min[i], p[i]); a.max[i] = rs_max(a.max[i], p[i]); }
+}
+// src/aabb.rs:263-273
+inline void aabb_grow_bb(Aabb& a, const Aabb& b) {
+  for (int i = 0; i < 3; ++i) { a.min[i] = rs_min(a.min[i], b.min[i]); a.max[i] = rs_max(a.max[i], b.max[i]); }
+}
+// src/aabb.rs:73-86 (extras take Default, i.e. 0)
+inline Aabb aabb_union_of(const Aabb& a, const Aabb& b) {
+  Aabb r;
+  for (int i = 0; i < 3; ++i) { r.min[i] = rs_min(a.min[i], b.min[i]); r.max[i] = rs_max(a.max[i], b.max[i]); }
+  r.extra1 = 0;
+  r.extra2 = 0;
+  return r;
+}
+// src/aabb.rs:312-321 (with_offset at :300-310 is the same arithmetic)
+inline void aabb_offset_by(Aabb& a, float d) {
+  for (int i = 0; i < 3; ++i) { a.min[i] = a.min[i] - d; a.max[i] = a.max[i] + d; }
+}
+// src/aabb.rs:342-346
+inline float aabb_half_area(const Aabb& a) {
+  float d0 = a.max[0] - a.min[0], d1 = a.max[1] - a.min[1], d2 = a.max[2] - a.min[2];
+  float t = (d0 + d1) * d2;
+  float u = d0 * d1;
+  return t + u;
+}
+// src/aabb.rs:353-363, extend at :387-390
+inline int aabb_longest_axis(const Aabb& a) {
+  int ax = 0;
+  if ((a.max[1] - a.min[1]) > (a.max[0] - a.min[0])) ax = 1;
+  if ((a.max[2] - a.min[2]) > (a.max[ax] - a.min[ax])) ax = 2;
+  return ax;
+}
+// src/aabb.rs:124-131
+inline Aabb aabb_union_of_list(const Aabb* boxes, size_t n) {
+  Aabb a = aabb_new();
+  for (size_t i = 0; i < n; ++i) aabb_grow_bb(a, boxes[i]);
+  aabb_offset_by(a, 0.0001f);
+  return a;
+}
+// src/aabb.rs:141-143 (Vec3A cmple: NaN compares false)
+inline bool aabb_is_valid(const Aabb& a) {
+  return a.min[0] <= a.max[0] && a.min[1] <= a.max[1] && a.min[2] <= a.max[2];
+}
+// src/aabb.rs:246-249
+inline bool aabb_contains(const Aabb& a, V3 p) {
+  return p.x > a.min[0] && p.x < a.max[0] && p.y > a.min[1] && p.y < a.max[1] && p.z > a.min[2] &&
+         p.z < a.max[2];
+}
+
+// ---------------------------------------------------------------- BvhNode
+// src/bvh_node.rs:12-14 -- a node is an Aabb: extra1 = count (-1: interior),
+// extra2 = left_first (-1: invalid). Accessors at src/bvh_node.rs:79-147.
+typedef Aabb BvhNode;
+inline bool node_is_leaf(const BvhNode& n) { return n.extra1 >= 0; }
+inline BvhNode node_new() { return aabb_new(); }  // src/bvh_node.rs:62-66
+
+// ---------------------------------------------------------------- Ray
+// src/ray.rs:9-16, Ray::new at src/ray.rs:166-182.
+struct Ray {
+  V3 origin;
+  float t_min;
+  V3 direction;
+  float t;
+  V3 inv_direction;
+  uint8_t signs[4];
+};
+inline Ray ray_new(V3 o, V3 d) {
+  Ray r;
+  r.origin = o;
+  r.direction = d;
+  r.t_min = 1e-4f;
+  r.t = 1e34f;
+  r.inv_direction = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  r.signs[0] = d.x < 0.0f;
+  r.signs[1] = d.y < 0.0f;
+  r.signs[2] = d.z < 0.0f;
+  r.signs[3] = 0;
+  return r;
+}
+inline bool v3_is_nan(V3 v) { return v.x != v.x || v.y != v.y || v.z != v.z; }
+
+// src/aabb.rs:145-181 -- sign-indexed slab test; returns the FAR t.
+inline bool aabb_intersect(const Aabb& a, const Ray& r, float* out) {
+  auto sel = [&](int s, int axis) { return s == 0 ? a.min[axis] : a.max[axis]; };
+  float ray_min = (sel(r.signs[0], 0) - r.origin.x) * r.inv_direction.x;
+  float ray_max = (sel(1 - r.signs[0], 0) - r.origin.x) * r.inv_direction.x;
+  float y_min = (sel(r.signs[1], 1) - r.origin.y) * r.inv_direction.y;
+  float y_max = (sel(1 - r.signs[1], 1) - r.origin.y) * r.inv_direction.y;
+  if ((ray_min > y_max) || (y_min > ray_max)) return false;
+  if (y_min > ray_min) ray_min = y_min;
+  if (y_max < ray_max) ray_max = y_max;
+  float z_min = (sel(r.signs[2], 2) - r.origin.z) * r.inv_direction.z;
+  float z_max = (sel(1 - r.signs[2], 2) - r.origin.z) * r.inv_direction.z;
+  if ((ray_min > z_max) || (z_min > ray_max)) return false;
+  if (z_max < ray_max) ray_max = z_max;
+  if (ray_max > r.t_min) { *out = ray_max; return true; }
+  return false;
+}
+
+// ---------------------------------------------------------------- MbvhNode
+// src/mbvh_node.rs:29-38, 128 bytes.
+struct MbvhNode {
+  float min_x[4], max_x[4], min_y[4], max_y[4], min_z[4], max_z[4];
+  int32_t children[4];
+  int32_t counts[4];
+};
+static_assert(sizeof(MbvhNode) == 128, "MbvhNode must be 128 bytes");
+
+// src/mbvh_node.rs:56-78
+inline MbvhNode mnode_new() {
+  MbvhNode m;
+  for (int i = 0; i < 4; ++i) {
+    m.min_x[i] = m.min_y[i] = m.min_z[i] = 1e34f;
+    m.max_x[i] = m.max_y[i] = m.max_z[i] = -1e34f;
+    m.children[i] = -1;
+    m.counts[i] = -1;
+  }
+  return m;
+}
+// src/mbvh_node.rs:40-53 (Default, used by the final resize)
+inline MbvhNode mnode_default() {
+  MbvhNode m;
+  std::memset(&m, 0, sizeof(m));
+  for (int i = 0; i < 4; ++i) { m.children[i] = -1; m.counts[i] = -1; }
+  return m;
+}
+// src/mbvh_node.rs:161-174
+inline void mnode_set_bounds_bb(MbvhNode& m, int i, const Aabb& b) {
+  m.min_x[i] = b.min[0]; m.min_y[i] = b.min[1]; m.min_z[i] = b.min[2];
+  m.max_x[i] = b.max[0]; m.max_y[i] = b.max[1]; m.max_z[i] = b.max[2];
+}
+
+struct MbvhHit {
+  uint8_t ids[4];
+  bool result[4];
+};
+
+// src/mbvh_node.rs:176-240 -- 4-wide slab test with SSE min/max, then a
+// 5-compare sorting network on t_min (the last compare swaps ids only).
+inline MbvhHit mnode_intersect(const MbvhNode& m, const Ray& r) {
+  float t_min[4];
+  MbvhHit h;
+  for (int i = 0; i < 4; ++i) {
+    float tx0 = (m.min_x[i] - r.origin.x) * r.inv_direction.x;
+    float tx1 = (m.max_x[i] - r.origin.x) * r.inv_direction.x;
+    float ty0 = (m.min_y[i] - r.origin.y) * r.inv_direction.y;
+    float ty1 = (m.max_y[i] - r.origin.y) * r.inv_direction.y;
+    float tz0 = (m.min_z[i] - r.origin.z) * r.inv_direction.z;
+    float tz1 = (m.max_z[i] - r.origin.z) * r.inv_direction.z;
+    float tx_min = sse_min(tx0, tx1), tx_max = sse_max(tx0, tx1);
+    float ty_min = sse_min(ty0, ty1), ty_max = sse_max(ty0, ty1);
+    float tz_min = sse_min(tz0, tz1), tz_max = sse_max(tz0, tz1);
+    float tmin = sse_max(tx_min, sse_max(ty_min, tz_min));
+    float tmax = sse_min(tx_max, sse_min(ty_max, tz_max));
+    t_min[i] = tmin;
+    h.result[i] = (tmax >= tmin) && (tmin < r.t);
+  }
+  uint8_t ids[4] = {0, 1, 2, 3};
+  if (t_min[0] > t_min[1]) { std::swap(t_min[0], t_min[1]); std::swap(ids[0], ids[1]); }
+  if (t_min[2] > t_min[3]) { std::swap(t_min[2], t_min[3]); std::swap(ids[2], ids[3]); }
+  if (t_min[0] > t_min[2]) { std::swap(t_min[0], t_min[2]); std::swap(ids[0], ids[2]); }
+  if (t_min[1] > t_min[3]) { std::swap(t_min[1], t_min[3]); std::swap(ids[1], ids[3]); }
+  if (t_min[2] > t_min[3]) { std::swap(ids[2], ids[3]); }
+  for (int i = 0; i < 4; ++i) h.ids[i] = ids[i];
+  return h;
+}
+
+// src/mbvh_node.rs:297-411
+void merge_nodes(size_t m_index, size_t cur_node, const BvhNode* pool, size_t pool_len,
+                 std::vector<MbvhNode>& mpool, size_t& pool_ptr) {
+  for (int i = 0; i < 4; ++i) mnode_set_bounds_bb(mpool[m_index], i, pool[cur_node]);
+  int32_t nodes[4] = {-1, -1, -1, -1};
+  int32_t leafs[4] = {-1, -1, -1, -1};
+  if (pool[cur_node].extra2 >= 0) {
+    uint32_t left_first = (uint32_t)pool[cur_node].extra2;
+    size_t child[2] = {left_first, (size_t)left_first + 1};
+    for (int side = 0; side < 2; ++side) {
+      const int s0 = side * 2;
+      if (child[side] < pool_len) {
+        const BvhNode& cn = pool[child[side]];
+        if (cn.extra2 >= 0) {
+          uint32_t lf = (uint32_t)cn.extra2;
+          if (node_is_leaf(cn)) {
+            nodes[s0] = (int32_t)lf;
+            leafs[s0] = cn.extra1;
+          } else {
+            for (int k = 0; k < 2; ++k) {
+              const BvhNode& g = pool[lf + k];
+              if (node_is_leaf(g)) {
+                nodes[s0 + k] = g.extra2;
+                leafs[s0 + k] = g.extra1;
+              } else {
+                nodes[s0 + k] = (int32_t)(lf + k);
+              }
+              mnode_set_bounds_bb(mpool[m_index], s0 + k, g);
+            }
+          }
+        }
+      }
+    }
+  }
+  for (int i = 0; i < 4; ++i) {
+    int32_t node = nodes[i];
+    int32_t count = leafs[i];
+    if (node >= 0 && count >= 0) {
+      mpool[m_index].children[i] = node;
+      mpool[m_index].counts[i] = count;
+      continue;
+    } else if (node == -1) {
+      continue;
+    }
+    const BvhNode& bn = pool[(size_t)node];
+    if (node_is_leaf(bn)) {
+      mpool[m_index].children[i] = bn.extra2;
+      mpool[m_index].counts[i] = bn.extra1;
+      mnode_set_bounds_bb(mpool[m_index], i, bn);
+    } else {
+      size_t new_m = pool_ptr++;
+      mpool[m_index].children[i] = (int32_t)new_m;
+      mnode_set_bounds_bb(mpool[m_index], i, bn);
+      merge_nodes(new_m, (size_t)node, pool, pool_len, mpool, pool_ptr);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- Morton
+// src/utils.rs:12-22
+uint32_t round_up_log2(uint32_t bits, uint32_t offset) {
+  if (bits == 0) return offset;
+  while ((1u << offset) < bits) offset += 1;
+  return offset;
+}
+// src/morton.rs:10-25 (usize is 64 bits)
+uint32_t morton_split(uint32_t v) {
+  uint32_t log_bits = round_up_log2(32, 0);
+  uint64_t x = v;
+  uint64_t mask = ~(uint64_t)0;
+  uint64_t i = log_bits;
+  uint64_t n = (uint64_t)1 << log_bits;
+  while (i > 0) {
+    mask = (mask | (mask << n)) & ~(mask << (n / 2));
+    x = (x | (x << n)) & mask;
+    n >>= 1;
+    i -= 1;
+  }
+  return (uint32_t)x;
+}
+
+struct MortonEncoder {
+  V3 world_to_grid, grid_offset;
+  uint32_t grid_dim;
+};
+// src/morton.rs:36-46
+MortonEncoder morton_encoder_new(const Aabb& a, uint32_t grid_dim) {
+  MortonEncoder e;
+  float g = (float)grid_dim;
+  V3 inv = v3(1.0f / (a.max[0] - a.min[0]), 1.0f / (a.max[1] - a.min[1]), 1.0f / (a.max[2] - a.min[2]));
+  e.world_to_grid = v3(g * inv.x, g * inv.y, g * inv.z);
+  e.grid_offset = v3(-a.min[0] * e.world_to_grid.x, -a.min[1] * e.world_to_grid.y, -a.min[2] * e.world_to_grid.z);
+  e.grid_dim = grid_dim;
+  return e;
+}
+// src/morton.rs:48-61
+uint32_t morton_encode_point(const MortonEncoder& e, V3 p) {
+  float gp[3] = {p.x * e.world_to_grid.x + e.grid_offset.x, p.y * e.world_to_grid.y + e.grid_offset.y,
+                 p.z * e.world_to_grid.z + e.grid_offset.z};
+  int32_t lim = (int32_t)(e.grid_dim - 1);
+  uint32_t c[3];
+  for (int i = 0; i < 3; ++i) c[i] = (uint32_t)std::min(lim, std::max(rs_f32_to_i32(gp[i]), 0));
+  return morton_split(c[0]) | (morton_split(c[1]) << 1) | (morton_split(c[2]) << 2);
+}
+
+// ---------------------------------------------------------------- Bvh
+struct Bvh {
+  std::vector<BvhNode> nodes;
+  std::vector<uint32_t> prim_indices;
+};
+
+// src/utils.rs:74-96 (Lomuto partition over a sub-slice)
+template <class F>
+size_t partition(uint32_t* slice, size_t len, F check) {
+  size_t count = 0;
+  for (size_t i = 0; i < len; ++i) {
+    if (check(slice[i])) {
+      std::swap(slice[i], slice[count]);
+      count += 1;
+    }
+  }
+  return count;
+}
+
+struct SahBin {
+  Aabb aabb;
+  uint64_t prim_count;
+  float right_cost;
+};
+struct SahSplit {
+  float cost;
+  uint32_t count;
+};
+
+struct BinnedCfg {
+  const Aabb* aabbs;
+  const V3* centers;
+  size_t max_depth, bin_count, max_leaf_size;
+  float traversal_cost;
+};
+
+// src/builders/binned_sah.rs:119-128
+inline size_t compute_bin_index(V3 center, size_t bin_count, V3 bin_offset, V3 center_to_bin, int axis) {
+  float bin_index = center[axis] * center_to_bin[axis] + bin_offset[axis];
+  uint64_t b = rs_f32_to_usize(rs_max(bin_index, 0.0f));
+  return (size_t)std::min<uint64_t>((uint64_t)(bin_count - 1), b);
+}
+
+// src/builders/mod.rs:59-76 -- pair allocation; one shared counter.
+struct NodeAlloc {
+  std::atomic<size_t>* counter;
+  size_t len;
+};
+
+struct SahTask {
+  size_t node, begin, end, depth;
+};
+
+
+constexpr float F32_MAX = 3.40282347e+38f;  // f32::MAX
+
+// src/builders/binned_sah.rs:80-114
+SahSplit find_split(SahBin* bins, size_t bin_count) {
+  Aabb cur = aabb_new();
+  uint64_t cnt = 0;
+  for (size_t i = bin_count - 1; i > 0; --i) {
+    aabb_grow_bb(cur, bins[i].aabb);
+    cnt += bins[i].prim_count;
+    bins[i].right_cost = aabb_half_area(cur) * (float)cnt;
+  }
+  cur = aabb_new();
+  cnt = 0;
+  SahSplit best{F32_MAX, (uint32_t)bin_count};
+  for (size_t i = 0; i + 1 < bin_count; ++i) {
+    aabb_grow_bb(cur, bins[i].aabb);
+    cnt += bins[i].prim_count;
+    float cost = aabb_half_area(cur) * (float)cnt + bins[i + 1].right_cost;
+    if (cost < best.cost) best = SahSplit{cost, (uint32_t)(i + 1)};
+  }
+  return best;
+}
+
+// src/builders/binned_sah.rs:132-282 -- one build task. Returns true and fills
+// (ta, tb) when the node was split.
+bool sah_task_run(const BinnedCfg& cfg, BvhNode* nodes, size_t nodes_len, uint32_t* prim_indices,
+                  std::atomic<size_t>& counter, const SahTask& t, SahTask& ta, SahTask& tb,
+                  std::vector<SahBin>& bin_store) {
+  BvhNode& node = nodes[t.node];
+  aabb_offset_by(node, 0.0001f);
+  auto make_leaf = [&]() {
+    aabb_offset_by(node, 0.0001f);
+    node.extra2 = (int32_t)t.begin;
+    node.extra1 = (int32_t)(t.end - t.begin);
+  };
+  const size_t ws = t.end - t.begin;
+  if (ws <= 1 || t.depth >= cfg.max_depth) {
+    make_leaf();
+    return false;
+  }
+  const size_t bc = cfg.bin_count;
+  V3 c2b, off;
+  {
+    float inv[3];
+    for (int a = 0; a < 3; ++a) inv[a] = 1.0f / (node.max[a] - node.min[a]);
+    c2b = v3(inv[0] * (float)bc, inv[1] * (float)bc, inv[2] * (float)bc);
+    off = v3(-node.min[0] * c2b.x, -node.min[1] * c2b.y, -node.min[2] * c2b.z);
+  }
+  bin_store.resize(3 * bc);
+  SahBin* bins[3] = {&bin_store[0], &bin_store[bc], &bin_store[2 * bc]};
+  for (int a = 0; a < 3; ++a)
+    for (size_t i = 0; i < bc; ++i) { bins[a][i].aabb = aabb_new(); bins[a][i].prim_count = 0; bins[a][i].right_cost = F32_MAX; }
+
+  uint32_t* slice = prim_indices + t.begin;
+  for (size_t i = 0; i < ws; ++i) {
+    size_t p = slice[i];
+    for (int a = 0; a < 3; ++a) {
+      size_t bi = compute_bin_index(cfg.centers[p], bc, off, c2b, a);
+      bins[a][bi].prim_count += 1;
+      aabb_grow_bb(bins[a][bi].aabb, cfg.aabbs[p]);
+    }
+  }
+  SahSplit best_splits[3];
+  for (int a = 0; a < 3; ++a) best_splits[a] = find_split(bins[a], bc);
+  int best_axis = 0;
+  if (best_splits[0].cost > best_splits[1].cost) best_axis = 1;
+  if (best_splits[best_axis].cost > best_splits[2].cost) best_axis = 2;
+
+  size_t split_index = best_splits[best_axis].count;
+  float max_split_cost = aabb_half_area(node) * ((float)ws - cfg.traversal_cost);
+  if ((size_t)best_splits[best_axis].count == bc || best_splits[best_axis].cost >= max_split_cost) {
+    if (ws > cfg.max_leaf_size) {
+      best_axis = aabb_longest_axis(node);
+      uint64_t count = 0;
+      for (size_t i = 0; i + 1 < bc; ++i) {
+        count += bins[best_axis][i].prim_count;
+        if (count >= (uint64_t)(ws * 2 / 5 + 1)) {
+          split_index = i + 1;
+          break;
+        }
+      }
+    } else {
+      make_leaf();
+      return false;
+    }
+  }
+  const int ax = best_axis;
+  size_t left_n = partition(slice, ws, [&](uint32_t id) {
+    return compute_bin_index(cfg.centers[id], bc, off, c2b, ax) < split_index;
+  });
+  size_t begin_right = t.begin + left_n;
+  if (begin_right > t.begin && begin_right < t.end) {
+    size_t left = counter.fetch_add(2);
+    if (left + 1 >= nodes_len + 1 || left >= nodes_len) return false;  // reference: unwrap() panics
+    node.extra2 = (int32_t)left;
+    node.extra1 = -1;
+    Aabb left_box = aabb_new(), right_box = aabb_new();
+    for (size_t i = 0; i < (size_t)best_splits[best_axis].count; ++i) aabb_grow_bb(left_box, bins[best_axis][i].aabb);
+    for (size_t i = split_index; i < bc; ++i) aabb_grow_bb(right_box, bins[best_axis][i].aabb);
+    nodes[left] = left_box;
+    nodes[left + 1] = right_box;
+    ta = SahTask{left, t.begin, begin_right, t.depth + 1};
+    tb = SahTask{left + 1, begin_right, t.end, t.depth + 1};
+    return true;
+  }
+  make_leaf();
+  return false;
+}
+
+// src/utils.rs:243-288 -- TaskSpawner::run_task. With spawn_threshold = SIZE_MAX
+// nothing is spawned and the visit order (hence node numbering) is the one a
+// single worker produces.
+void run_task(const BinnedCfg& cfg, BvhNode* nodes, size_t nodes_len, uint32_t* prim_indices,
+              std::atomic<size_t>& counter, SahTask first, size_t spawn_threshold) {
+  std::vector<std::thread> sub;
+  std::vector<SahTask> stack{first};
+  std::vector<SahBin> bins;
+  while (!stack.empty()) {
+    SahTask w = stack.back();
+    stack.pop_back();
+    SahTask a, b;
+    if (sah_task_run(cfg, nodes, nodes_len, prim_indices, counter, w, a, b, bins)) {
+      if ((a.end - a.begin) < (b.end - b.begin)) std::swap(a, b);
+      stack.push_back(b);
+      if ((a.end - a.begin) <= spawn_threshold) {
+        stack.push_back(a);
+        continue;
+      }
+      sub.emplace_back([&cfg, nodes, nodes_len, prim_indices, &counter, a, spawn_threshold]() {
+        run_task(cfg, nodes, nodes_len, prim_indices, counter, a, spawn_threshold);
+      });
+    }
+  }
+  while (!sub.empty()) {
+    sub.back().join();
+    sub.pop_back();
+  }
+}
+
+// src/builders/binned_sah.rs:305-318 (defaults) and :346-400 (build)
+Bvh build_binned_sah(const Aabb* aabbs, const V3* centers, size_t n, size_t prims_per_leaf,
+                     size_t spawn_threshold) {
+  Bvh b;
+  if (n == 0) return b;
+  BinnedCfg cfg{aabbs, centers, 64, 16, prims_per_leaf == 0 ? 1 : prims_per_leaf, 1.0f};
+  b.nodes.assign(2 * n - 1, node_new());
+  b.prim_indices.resize(n);
+  for (size_t i = 0; i < n; ++i) b.prim_indices[i] = (uint32_t)i;
+  std::atomic<size_t> counter{1};
+  b.nodes[0] = aabb_union_of_list(aabbs, n);
+  run_task(cfg, b.nodes.data(), b.nodes.size(), b.prim_indices.data(), counter, SahTask{0, 0, n, 0},
+           spawn_threshold);
+  b.nodes.resize(counter.load());
+  return b;
+}
+
+// ---------------------------------------------------------------- LOCB
+// src/builders/locb.rs:36-45
+inline void locb_search_range(size_t i, size_t begin, size_t end, size_t radius, size_t& sb, size_t& se) {
+  sb = (i > begin + radius) ? i - radius : begin;
+  se = std::min(i + radius + 1, end);
+}
+
+// src/builders/locb.rs:48-245. The reference caches the pair distances in a
+// rolling matrix; every cached entry equals half_area(union(in[lo], in[hi]))
+// for the pair, which is what is computed here directly. Returns false when
+// a node has no neighbour (all distances NaN or >= f32::MAX).
+bool locb_cluster(const BvhNode* in, BvhNode* out, uint32_t* nb, uint32_t* merged, size_t begin, size_t end,
+                  size_t previous_end, size_t radius, size_t& next_begin, size_t& next_end) {
+  for (size_t i = begin; i < end; ++i) {
+    size_t sb, se;
+    locb_search_range(i, begin, end, radius, sb, se);
+    float best_d = F32_MAX;
+    int64_t best_j = -1;
+    for (size_t j = sb; j < i; ++j) {
+      float d = aabb_half_area(aabb_union_of(in[j], in[i]));
+      if (d < best_d) { best_d = d; best_j = (int64_t)j; }
+    }
+    for (size_t j = i + 1; j < se; ++j) {
+      float d = aabb_half_area(aabb_union_of(in[i], in[j]));
+      if (d < best_d) { best_d = d; best_j = (int64_t)j; }
+    }
+    if (best_j < 0) return false;
+    nb[i] = (uint32_t)best_j;
+  }
+  for (size_t i = begin; i < end; ++i) {
+    size_t j = nb[i];
+    merged[i] = (i < j && (size_t)nb[j] == i) ? 1u : 0u;
+  }
+  // src/utils.rs:42-57 inclusive prefix sum
+  uint32_t sum = 0;
+  for (size_t i = begin; i < end; ++i) { sum += merged[i]; merged[i] = sum; }
+  size_t merged_count = merged[end - 1];
+  size_t unmerged_count = end - begin - merged_count;
+  size_t children_count = merged_count * 2;
+  size_t children_begin = end - children_count;
+  size_t unmerged_begin = end - (children_count + unmerged_count);
+  for (size_t i = begin; i < end; ++i) {
+    size_t j = nb[i];
+    if ((size_t)nb[j] == i) {
+      if (i < j) {
+        BvhNode& u = out[unmerged_begin + j - begin - merged[j]];
+        size_t first_child = children_begin + ((size_t)merged[i] - 1) * 2;
+        u = aabb_union_of(in[j], in[i]);
+        u.extra1 = -1;
+        u.extra2 = (int32_t)first_child;
+        out[first_child] = in[i];
+        out[first_child + 1] = in[j];
+      }
+    } else {
+      out[unmerged_begin + i - begin - merged[i]] = in[i];
+    }
+  }
+  for (size_t k = end; k < previous_end; ++k) out[k] = in[k];
+  next_begin = unmerged_begin;
+  next_end = children_begin;
+  return merged_count > 0;
+}
+
+// src/morton.rs:63-102 -- codes, then a stable sort of the indices by code.
+void morton_sorted(const MortonEncoder& enc, const V3* centers, size_t n, std::vector<uint32_t>& idx,
+                   std::vector<uint32_t>& codes, unsigned threads) {
+  codes.resize(n);
+  idx.resize(n);
+  if (threads <= 1 || n < 65536) {
+    for (size_t i = 0; i < n; ++i) codes[i] = morton_encode_point(enc, centers[i]);
+  } else {
+    std::vector<std::thread> ts;
+    for (unsigned t = 0; t < threads; ++t)
+      ts.emplace_back([&, t]() {
+        for (size_t i = t; i < n; i += threads) codes[i] = morton_encode_point(enc, centers[i]);
+      });
+    for (auto& th : ts) th.join();
+  }
+  for (size_t i = 0; i < n; ++i) idx[i] = (uint32_t)i;
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return codes[a] < codes[b]; });
+}
+
+// src/builders/locb.rs:18-29 (new) and :249-328 (build). Returns an empty
+// Bvh and sets *err on a level without neighbours or merges.
+Bvh build_locb(const Aabb* aabbs, const V3* centers, size_t n, int* err, unsigned threads) {
+  Bvh b;
+  *err = 0;
+  if (n == 0) return b;
+  Aabb world = aabb_union_of_list(aabbs, n);
+  MortonEncoder enc = morton_encoder_new(world, 1u << 10);
+  if (n <= 2) {
+    BvhNode root = world;
+    root.extra2 = 0;
+    root.extra1 = (int32_t)n;
+    b.nodes.push_back(root);
+    for (size_t i = 0; i < n; ++i) b.prim_indices.push_back((uint32_t)i);
+    return b;
+  }
+  std::vector<uint32_t> codes;
+  morton_sorted(enc, centers, n, b.prim_indices, codes, threads);
+  const size_t node_count = 2 * n - 1;
+  BvhNode init;
+  for (int i = 0; i < 3; ++i) { init.min[i] = 0.0f; init.max[i] = 0.0f; }
+  init.extra1 = -1;
+  init.extra2 = 0;
+  std::vector<BvhNode> nodes(node_count, init), nodes_copy(node_count, init);
+  std::vector<uint32_t> aux(node_count * 3, (uint32_t)node_count);
+  uint32_t* nb = aux.data();
+  uint32_t* merged = aux.data() + node_count;
+  size_t begin = node_count - n, end = node_count, previous_end = end;
+  for (size_t i = 0; i < n; ++i) {
+    BvhNode& nd = nodes[begin + i];
+    nd = aabbs[b.prim_indices[i]];
+    aabb_offset_by(nd, 0.0001f);
+    nd.extra1 = 1;
+    nd.extra2 = (int32_t)i;
+  }
+  while (end - begin > 1) {
+    size_t nbg, nen;
+    if (!locb_cluster(nodes.data(), nodes_copy.data(), nb, merged, begin, end, previous_end, 14, nbg, nen)) {
+      *err = 1;
+      return Bvh();
+    }
+    std::swap(nodes, nodes_copy);
+    previous_end = end;
+    begin = nbg;
+    end = nen;
+  }
+  b.nodes = std::move(nodes);
+  return b;
+}
+
+// ---------------------------------------------------------------- Mbvh
+// src/bvh.rs:381-404
+std::vector<MbvhNode> mbvh_construct(const BvhNode* nodes, size_t node_count) {
+  std::vector<MbvhNode> m;
+  if (node_count == 0) return m;
+  m.assign(node_count, mnode_new());
+  size_t pool_ptr = 1;
+  merge_nodes(0, 0, nodes, node_count, m, pool_ptr);
+  m.resize(pool_ptr, mnode_default());
+  return m;
+}
+
+// ---------------------------------------------------------------- refit / validate
+// src/bvh.rs:176-205. Faithful: the fresh Aabb::new() carries extras of 0, so
+// the reference overwrites every node's count/left_first with 0.
+void refit(BvhNode* nodes, size_t node_count, const uint32_t* prim_indices, const Aabb* new_aabbs) {
+  for (size_t ii = node_count; ii-- > 0;) {
+    Aabb aabb = aabb_new();
+    if (nodes[ii].extra2 >= 0) {
+      uint32_t left_first = (uint32_t)nodes[ii].extra2;
+      int32_t count = nodes[ii].extra1;
+      if (node_is_leaf(nodes[ii])) {
+        for (int32_t i = 0; i < count; ++i) aabb_grow_bb(aabb, new_aabbs[prim_indices[left_first + (uint32_t)i]]);
+      } else {
+        aabb_grow_bb(aabb, nodes[left_first]);
+        aabb_grow_bb(aabb, nodes[left_first + 1]);
+      }
+      aabb_offset_by(aabb, 0.0001f);
+    }
+    nodes[ii] = aabb;
+  }
+}
+
+// src/bvh.rs:207-244
+void traverse_check(const BvhNode* nodes, const uint32_t* idx, const BvhNode& cur, uint8_t* checks, size_t n,
+                    bool& ok) {
+  if (cur.extra2 >= 0) {
+    uint32_t lf = (uint32_t)cur.extra2;
+    if (node_is_leaf(cur)) {
+      for (int32_t i = 0; i < cur.extra1; ++i) {
+        uint32_t p = idx[(int32_t)lf + i];
+        if (p >= n) { ok = false; continue; }
+        checks[p] = 1;
+      }
+    } else {
+      traverse_check(nodes, idx, nodes[lf], checks, n, ok);
+      traverse_check(nodes, idx, nodes[lf + 1], checks, n, ok);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- traversal
+struct Hit {
+  float t, u, v;
+  int32_t prim;
+};
+struct Stats {
+  uint64_t node_visits = 0, tri_tests = 0, deep_pushes = 0;
+  uint32_t max_stack = 0;
+};
+
+// src/builders/spatial_sah.rs:132-163 (Moller-Trumbore, closest-hit update)
+inline bool mt_intersect(const float* tri, Ray& ray, float t_min, float* pu, float* pv) {
+  V3 v0 = v3(tri[0], tri[1], tri[2]), v1 = v3(tri[3], tri[4], tri[5]), v2 = v3(tri[6], tri[7], tri[8]);
+  V3 edge1 = sub(v1, v0), edge2 = sub(v2, v0);
+  V3 h = cross(ray.direction, edge2);
+  float a = dot(edge1, h);
+  if (a > -1e-5f && a < 1e-5f) return false;
+  float f = 1.0f / a;
+  V3 s = sub(ray.origin, v0);
+  float u = f * dot(s, h);
+  if (!(u >= 0.0f && u <= 1.0f)) return false;
+  V3 q = cross(s, edge1);
+  float v = f * dot(ray.direction, q);
+  if (v < 0.0f || (u + v) > 1.0f) return false;
+  float t = f * dot(edge2, q);
+  if (t > t_min && t < ray.t) {
+    ray.t = t;
+    *pu = u;
+    *pv = v;
+    return true;
+  }
+  return false;
+}
+
+constexpr int ORACLE_STACK = 4096;
+
+// src/iter_indices.rs:212-313 (MbvhIndexIterator) driving the triangle test,
+// as examples/benchmark.rs:15-41 and rtbvh_ffi/src/lib.rs:700-731 do.
+void trace_mbvh_one(const MbvhNode* m, size_t mcount, const uint32_t* idx, const float* tris, Ray& ray,
+                    float t_min_tri, bool any_hit, Hit& out, Stats& st) {
+  out.t = ray.t; out.u = 0.0f; out.v = 0.0f; out.prim = -1;
+  if (mcount == 0) return;
+  int32_t stack[ORACLE_STACK];
+  MbvhHit hit = mnode_intersect(m[0], ray);
+  st.node_visits++;
+  int32_t current = 0, i = 0, j = 0, sp = -1;
+  for (;;) {
+    const MbvhNode& node = m[current];
+    if (i >= 4) {
+      if (sp < 0) break;
+      current = stack[sp--];
+      hit = mnode_intersect(m[current], ray);
+      st.node_visits++;
+      i = 0;
+    } else {
+      int id = hit.ids[3 - i];
+      if (hit.result[id]) {
+        int32_t count = node.counts[id];
+        int32_t lf = node.children[id];
+        if (count > -1) {
+          if (j < count) {
+            uint32_t prim = idx[lf + j];
+            j++;
+            st.tri_tests++;
+            float u, v;
+            if (mt_intersect(tris + 9 * (size_t)prim, ray, t_min_tri, &u, &v)) {
+              out.t = ray.t; out.u = u; out.v = v; out.prim = (int32_t)prim;
+              if (any_hit) return;
+            }
+            continue;
+          }
+          j = 0;
+        } else if (lf > -1) {
+          if (sp + 1 >= ORACLE_STACK) { out.prim = -2; return; }
+          stack[++sp] = lf;
+          if ((uint32_t)(sp + 1) > st.max_stack) st.max_stack = (uint32_t)(sp + 1);
+          if (sp >= 32) st.deep_pushes++;
+        }
+      }
+      i++;
+    }
+  }
+}
+
+// src/bvh_node.rs:150-177
+inline int32_t sort_nodes(bool lh, float lt, bool rh, float rt, int32_t* stack, int32_t sp, int32_t lf) {
+  if (lh && rh) {
+    sp += 1;
+    if (lt < rt) { stack[sp] = lf; sp += 1; stack[sp] = lf + 1; }
+    else { stack[sp] = lf + 1; sp += 1; stack[sp] = lf; }
+  } else if (lh) {
+    sp += 1; stack[sp] = lf;
+  } else if (rh) {
+    sp += 1; stack[sp] = lf + 1;
+  }
+  return sp;
+}
+
+// src/iter_indices.rs:18-107 (BvhIndexIterator) driving the triangle test.
+void trace_bvh_one(const BvhNode* nodes, size_t ncount, const uint32_t* idx, const float* tris, Ray& ray,
+                   float t_min_tri, bool any_hit, Hit& out, Stats& st) {
+  out.t = ray.t; out.u = 0.0f; out.v = 0.0f; out.prim = -1;
+  if (ncount == 0 || v3_is_nan(ray.origin) || v3_is_nan(ray.direction)) return;
+  int32_t stack[ORACLE_STACK];
+  stack[0] = 0;
+  int32_t sp = 0, i = 0;
+  for (;;) {
+    if (sp < 0) break;
+    const BvhNode& node = nodes[stack[sp]];
+    sp -= 1;
+    int32_t count = node.extra1, lf = node.extra2;
+    if (count > -1) {
+      if (i < count) {
+        uint32_t prim = idx[lf + i];
+        i += 1;
+        sp += 1;
+        st.tri_tests++;
+        float u, v;
+        if (mt_intersect(tris + 9 * (size_t)prim, ray, t_min_tri, &u, &v)) {
+          out.t = ray.t; out.u = u; out.v = v; out.prim = (int32_t)prim;
+          if (any_hit) return;
+        }
+        continue;
+      }
+      i = 0;
+    } else if (lf > -1) {
+      st.node_visits++;
+      float lt = 0.0f, rt = 0.0f;
+      bool lh = aabb_intersect(nodes[lf], ray, &lt);
+      bool rh = aabb_intersect(nodes[lf + 1], ray, &rt);
+      if (sp + 2 >= ORACLE_STACK) { out.prim = -2; return; }
+      sp = sort_nodes(lh, lt, rh, rt, stack, sp, lf);
+      if ((uint32_t)(sp + 1) > st.max_stack) st.max_stack = (uint32_t)(sp + 1);
+    }
+  }
+}
+
+void load_aabbs(const float* raw, size_t n, std::vector<Aabb>& out) {
+  out.resize(n);
+  if (n) std::memcpy(out.data(), raw, n * sizeof(Aabb));
+}
+void load_centers(const float* raw, size_t n, std::vector<V3>& out) {
+  out.resize(n);
+  for (size_t i = 0; i < n; ++i) out[i] = v3(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2]);
+}
+
+}  // namespace
+
+// ================================================================= C API
+// Array layouts (all little-endian, float32 unless stated):
+//   aabbs   n x 8  : RTAabb {min[3], i32 count, max[3], i32 left_first}
+//   centers n x 3
+//   nodes   m x 8  : RTBvhNode (same layout as RTAabb)
+//   mnodes  k x 32 : RTMbvhNode {min_x[4],max_x[4],min_y[4],max_y[4],min_z[4],max_z[4], i32 children[4], i32 counts[4]}
+//   tris    n x 9  : v0, v1, v2 of primitive i (primitive-id order)
+//   rays    R x 6  : origin, direction
+//   hits    R x 4  : t, u, v, i32 prim (-1: none)
+//   stats   R x 3  : u32 node visits, u32 triangle tests, u32 max stack depth
+extern "C" {
+
+int32_t ror_abi_sizes(int32_t which) {
+  switch (which) {
+    case 0: return (int32_t)sizeof(Aabb);
+    case 1: return (int32_t)sizeof(BvhNode);
+    case 2: return (int32_t)sizeof(MbvhNode);
+    default: return -1;
+  }
+}
+
+uint32_t ror_morton_split(uint32_t v) { return morton_split(v); }
+
+// Triangle::aabb and Triangle::center of the shared crate
+// (shared/src/lib.rs:27-39; also src/lib.rs:166-178): the empty box grown by
+// the three vertices, and ((v0 + v1) + v2) * (1/3).
+void ror_triangle_prep(const float* tris, size_t n, float* aabbs_out, float* centers_out) {
+  const float third = 1.0f / 3.0f;
+  for (size_t i = 0; i < n; ++i) {
+    const float* t = tris + 9 * i;
+    Aabb a = aabb_new();
+    aabb_grow(a, v3(t[0], t[1], t[2]));
+    aabb_grow(a, v3(t[3], t[4], t[5]));
+    aabb_grow(a, v3(t[6], t[7], t[8]));
+    std::memcpy(aabbs_out + 8 * i, &a, sizeof(Aabb));
+    for (int k = 0; k < 3; ++k) centers_out[3 * i + k] = ((t[k] + t[3 + k]) + t[6 + k]) * third;
+  }
+}
+
+// src/utils.rs:42-57
+uint32_t ror_prefix_sum_u32(const uint32_t* first, size_t count, uint32_t* output) {
+  if (count == 0) return first[0];
+  uint32_t sum = 0;
+  for (size_t i = 0; i < count; ++i) { sum += first[i]; output[i] = sum; }
+  return sum;
+}
+
+// src/aabb.rs:124-131
+void ror_union_of_list(const float* aabbs, size_t n, float* out8) {
+  std::vector<Aabb> a;
+  load_aabbs(aabbs, n, a);
+  Aabb r = aabb_union_of_list(a.data(), n);
+  std::memcpy(out8, &r, sizeof(Aabb));
+}
+
+// Morton codes of the centres against the world box of the aabbs
+// (src/builders/locb.rs:19-20 + src/morton.rs:63-102).
+void ror_morton_codes(const float* aabbs, const float* centers, size_t n, uint32_t* codes_out,
+                      uint32_t* sorted_idx_out) {
+  std::vector<Aabb> a;
+  std::vector<V3> c;
+  load_aabbs(aabbs, n, a);
+  load_centers(centers, n, c);
+  Aabb world = aabb_union_of_list(a.data(), n);
+  MortonEncoder enc = morton_encoder_new(world, 1u << 10);
+  std::vector<uint32_t> idx, codes;
+  morton_sorted(enc, c.data(), n, idx, codes, 1);
+  if (n) {
+    std::memcpy(codes_out, codes.data(), n * 4);
+    std::memcpy(sorted_idx_out, idx.data(), n * 4);
+  }
+}
+
+// Builds. nodes_out must hold 2n-1 nodes, idx_out n entries. Return value:
+// node count (>= 0), -2 no primitives, -5 a LOCB level without a merge.
+// build_type: 0 = locally ordered clustering, 1 = binned SAH.
+// spawn_threshold: 0 = single worker (canonical numbering), else the
+// TaskSpawner threshold (1024 in the reference).
+int64_t ror_build(const float* aabbs, const float* centers, size_t n, size_t prims_per_leaf, int32_t build_type,
+                  size_t spawn_threshold, uint32_t threads, float* nodes_out, uint32_t* idx_out) {
+  if (n == 0) return -2;
+  std::vector<Aabb> a;
+  std::vector<V3> c;
+  load_aabbs(aabbs, n, a);
+  load_centers(centers, n, c);
+  Bvh b;
+  if (build_type == 0) {
+    int err = 0;
+    b = build_locb(a.data(), c.data(), n, &err, threads);
+    if (err) return -5;
+  } else {
+    b = build_binned_sah(a.data(), c.data(), n, prims_per_leaf, spawn_threshold == 0 ? SIZE_MAX : spawn_threshold);
+  }
+  std::memcpy(nodes_out, b.nodes.data(), b.nodes.size() * sizeof(BvhNode));
+  std::memcpy(idx_out, b.prim_indices.data(), b.prim_indices.size() * 4);
+  return (int64_t)b.nodes.size();
+}
+
+// src/bvh.rs:381-404. mnodes_out must hold node_count entries; returns the
+// number of quad nodes.
+int64_t ror_mbvh(const float* nodes, size_t node_count, float* mnodes_out) {
+  std::vector<Aabb> nd;
+  load_aabbs(nodes, node_count, nd);
+  std::vector<MbvhNode> m = mbvh_construct(nd.data(), node_count);
+  if (!m.empty()) std::memcpy(mnodes_out, m.data(), m.size() * sizeof(MbvhNode));
+  return (int64_t)m.size();
+}
+
+// src/bvh.rs:176-205, in place.
+void ror_refit(float* nodes, size_t node_count, const uint32_t* prim_indices, const float* new_aabbs,
+               size_t prim_count) {
+  std::vector<Aabb> nd, na;
+  load_aabbs(nodes, node_count, nd);
+  load_aabbs(new_aabbs, prim_count, na);
+  refit(nd.data(), node_count, prim_indices, na.data());
+  std::memcpy(nodes, nd.data(), node_count * sizeof(Aabb));
+}
+
+// src/bvh.rs:232-244
+int32_t ror_validate(const float* nodes, size_t node_count, const uint32_t* idx, size_t prim_count) {
+  if (node_count == 0) return 0;
+  std::vector<Aabb> nd;
+  load_aabbs(nodes, node_count, nd);
+  std::vector<uint8_t> checks(prim_count, 0);
+  bool ok = true;
+  traverse_check(nd.data(), idx, nd[0], checks.data(), prim_count, ok);
+  for (size_t i = 0; i < prim_count; ++i)
+    if (!checks[i]) ok = false;
+  return ok ? 1 : 0;
+}
+
+// Traversal of R rays (closest hit, or any hit when any_hit != 0). t_max is
+// either one value per ray (t_max != NULL) or the Ray::new default of 1e34.
+// t_min_tri is the triangle test's lower bound (Ray::t_min = 1e-4 in the
+// crate; the FFI test callback uses 1e-5). structure: 0 = Mbvh, 1 = Bvh.
+// threads > 1 splits the rays into chunks of 1000, as examples/benchmark.rs:25.
+// Returns the number of rays whose traversal stack exceeded the oracle's
+// bound (0 expected).
+int64_t ror_trace(int32_t structure, const float* nodes, size_t node_count, const uint32_t* idx, const float* tris,
+                  const float* rays, size_t nrays, const float* t_max, float t_min_tri, int32_t any_hit,
+                  float* hits_out, uint32_t* stats_out, uint32_t threads) {
+  std::atomic<int64_t> bad{0};
+  std::atomic<size_t> next{0};
+  const size_t chunk = 1000;
+  auto worker = [&]() {
+    for (;;) {
+      size_t c0 = next.fetch_add(chunk);
+      if (c0 >= nrays) break;
+      size_t c1 = std::min(nrays, c0 + chunk);
+      for (size_t r = c0; r < c1; ++r) {
+        const float* rr = rays + 6 * r;
+        Ray ray = ray_new(v3(rr[0], rr[1], rr[2]), v3(rr[3], rr[4], rr[5]));
+        if (t_max) ray.t = t_max[r];
+        Hit h;
+        Stats st;
+        if (structure == 0)
+          trace_mbvh_one(reinterpret_cast<const MbvhNode*>(nodes), node_count, idx, tris, ray, t_min_tri,
+                         any_hit != 0, h, st);
+        else
+          trace_bvh_one(reinterpret_cast<const BvhNode*>(nodes), node_count, idx, tris, ray, t_min_tri,
+                        any_hit != 0, h, st);
+        if (h.prim == -2) { bad.fetch_add(1); h.prim = -1; }
+        if (hits_out) {
+          float* ho = hits_out + 4 * r;
+          ho[0] = h.t; ho[1] = h.u; ho[2] = h.v;
+          std::memcpy(ho + 3, &h.prim, 4);
+        }
+        if (stats_out) {
+          stats_out[3 * r + 0] = (uint32_t)st.node_visits;
+          stats_out[3 * r + 1] = (uint32_t)st.tri_tests;
+          stats_out[3 * r + 2] = st.max_stack;
+        }
+      }
+    }
+  };
+  if (threads <= 1) {
+    worker();
+  } else {
+    std::vector<std::thread> ts;
+    for (uint32_t t = 0; t < threads; ++t) ts.emplace_back(worker);
+    for (auto& th : ts) th.join();
+  }
+  return bad.load();
+}
+
+}  // extern "C"

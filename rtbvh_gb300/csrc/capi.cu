@@ -1,0 +1,815 @@
+// C ABI of the library: the rtbvh_ffi-compatible entry points and the GPU
+// entry points declared in include/rtbvh.h.
+//
+// Storage mirrors rtbvh_ffi's StructureManager (rtbvh_ffi/src/lib.rs:8-127):
+// the library owns every structure in two id-indexed tables (Bvh, Mbvh);
+// ids are never reused; free_* empties a slot. Each entry holds the device
+// arrays (nodes, indices, leaf-ordered triangles) and, unless asked not to,
+// a host mirror of nodes and indices that the handle pointers refer to.
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "lib_internal.h"
+
+using namespace rtbvh;
+
+namespace {
+
+struct Entry {
+  bool alive = false;
+  bool mirrored = false;
+  uint32_t node_count = 0;
+  uint32_t prim_count = 0;
+  DAabb* d_nodes = nullptr;       // Bvh
+  DMNode* d_mnodes = nullptr;     // Mbvh
+  uint32_t* d_indices = nullptr;
+  float4* d_tris = nullptr;       // 3 per index slot
+  float* d_vertices = nullptr;    // prim-id order, 9 floats each
+  uint32_t* d_status = nullptr;
+  uint32_t source_bvh = UINT32_MAX;
+  std::vector<DAabb> h_nodes;
+  std::vector<DMNode> h_mnodes;
+  std::vector<uint32_t> h_indices;
+
+  void release() {
+    cudaFree(d_nodes);
+    cudaFree(d_mnodes);
+    cudaFree(d_indices);
+    cudaFree(d_tris);
+    cudaFree(d_vertices);
+    cudaFree(d_status);
+    d_nodes = nullptr;
+    d_mnodes = nullptr;
+    d_indices = nullptr;
+    d_tris = nullptr;
+    d_vertices = nullptr;
+    d_status = nullptr;
+    std::vector<DAabb>().swap(h_nodes);
+    std::vector<DMNode>().swap(h_mnodes);
+    std::vector<uint32_t>().swap(h_indices);
+    node_count = prim_count = 0;
+    alive = false;
+    mirrored = false;
+  }
+};
+
+std::mutex g_mu;
+std::vector<std::unique_ptr<Entry>> g_bvh, g_mbvh;
+
+Entry* lookup(uint32_t id, bool mbvh) {
+  auto& t = mbvh ? g_mbvh : g_bvh;
+  if (id >= t.size()) return nullptr;
+  Entry* e = t[id].get();
+  return (e && e->alive) ? e : nullptr;
+}
+
+uint32_t store(std::unique_ptr<Entry> e, bool mbvh) {
+  auto& t = mbvh ? g_mbvh : g_bvh;
+  t.push_back(std::move(e));
+  return (uint32_t)(t.size() - 1);
+}
+
+cudaStream_t legacy_stream() {
+  static cudaStream_t s = nullptr;
+  static std::once_flag once;
+  std::call_once(once, []() { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); });
+  return s;
+}
+
+template <class T>
+cudaError_t dmalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return cudaSuccess;
+  return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+}
+
+RTBvh bvh_handle(uint32_t id, const Entry& e) {
+  RTBvh h;
+  h.id = id;
+  h.node_count = e.node_count;
+  h.nodes = e.mirrored ? reinterpret_cast<const RTBvhNode*>(e.h_nodes.data()) : nullptr;
+  h.index_count = e.prim_count;
+  h.indices = e.mirrored ? e.h_indices.data() : nullptr;
+  return h;
+}
+
+RTMbvh mbvh_handle(uint32_t id, const Entry& e) {
+  RTMbvh h;
+  h.id = id;
+  h.node_count = e.node_count;
+  h.nodes = e.mirrored ? reinterpret_cast<const RTMbvhNode*>(e.h_mnodes.data()) : nullptr;
+  h.index_count = e.prim_count;
+  h.indices = e.mirrored ? e.h_indices.data() : nullptr;
+  return h;
+}
+
+ResultCode mirror_bvh(Entry& e, cudaStream_t s) {
+  e.h_nodes.resize(e.node_count);
+  e.h_indices.resize(e.prim_count);
+  cudaError_t err;
+  if (e.node_count &&
+      (err = cudaMemcpyAsync(e.h_nodes.data(), e.d_nodes, (size_t)e.node_count * sizeof(DAabb),
+                             cudaMemcpyDeviceToHost, s)))
+    return cuda_rc(err);
+  if (e.prim_count && (err = cudaMemcpyAsync(e.h_indices.data(), e.d_indices, (size_t)e.prim_count * 4,
+                                             cudaMemcpyDeviceToHost, s)))
+    return cuda_rc(err);
+  if ((err = cudaStreamSynchronize(s))) return cuda_rc(err);
+  e.mirrored = true;
+  return Ok;
+}
+
+ResultCode mirror_mbvh(Entry& e, cudaStream_t s) {
+  e.h_mnodes.resize(e.node_count);
+  e.h_indices.resize(e.prim_count);
+  cudaError_t err;
+  if (e.node_count && (err = cudaMemcpyAsync(e.h_mnodes.data(), e.d_mnodes, (size_t)e.node_count * sizeof(DMNode),
+                                             cudaMemcpyDeviceToHost, s)))
+    return cuda_rc(err);
+  if (e.prim_count && (err = cudaMemcpyAsync(e.h_indices.data(), e.d_indices, (size_t)e.prim_count * 4,
+                                             cudaMemcpyDeviceToHost, s)))
+    return cuda_rc(err);
+  if ((err = cudaStreamSynchronize(s))) return cuda_rc(err);
+  e.mirrored = true;
+  return Ok;
+}
+
+// Builds a Bvh entry from device boxes + float4 centres (+ optional device
+// triangles, prim-id order) and stores it.
+ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t n, size_t ppl, BvhType type,
+                           const float* d_vertices, uint32_t flags, cudaStream_t s, RTBvh* result) {
+  BuildOutput out;
+  ResultCode rc = (type == LocallyOrderedClustered) ? build_locb(d_aabbs, d_centers, n, s, &out)
+                                                     : build_binned_sah(d_aabbs, d_centers, n, ppl, s, &out);
+  if (rc != Ok) return rc;
+  auto e = std::make_unique<Entry>();
+  e->alive = true;
+  e->node_count = out.node_count;
+  e->prim_count = (uint32_t)n;
+  e->d_nodes = out.nodes;
+  e->d_indices = out.indices;
+  cudaError_t err;
+  if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
+    e->release();
+    return cuda_rc(err);
+  }
+  if (d_vertices) {
+    if ((err = dmalloc(&e->d_vertices, 9 * n)) ||
+        (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
+        (err = dmalloc(&e->d_tris, 3 * n)) ||
+        (err = launch_gather_triangles(e->d_vertices, e->d_indices, n, e->d_tris, s))) {
+      e->release();
+      return cuda_rc(err);
+    }
+  }
+  if (!(flags & RTBVH_FLAG_NO_HOST_MIRROR)) {
+    if ((rc = mirror_bvh(*e, s)) != Ok) {
+      e->release();
+      return rc;
+    }
+  } else if ((err = cudaStreamSynchronize(s))) {
+    e->release();
+    return cuda_rc(err);
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* raw = e.get();
+  uint32_t id = store(std::move(e), false);
+  *result = bvh_handle(id, *raw);
+  return Ok;
+}
+
+// ------------------------------------------------------------- host iterators
+// Used by the legacy callback entry points only (a host function pointer
+// cannot run on the GPU).
+struct HRay {
+  float o[3], d[3], inv[3];
+  float t_min, t;
+  int s[3];
+};
+HRay make_hray(const float* o, const float* d, float t) {
+  HRay r;
+  for (int i = 0; i < 3; ++i) {
+    r.o[i] = o[i];
+    r.d[i] = d[i];
+    r.inv[i] = 1.0f / d[i];
+    r.s[i] = d[i] < 0.0f;
+  }
+  r.t_min = 1e-4f;
+  r.t = t;
+  return r;
+}
+
+// src/aabb.rs:145-181
+bool h_slab_far(const RTAabb& b, const HRay& r, float* out) {
+  auto sel = [&](int s, int a) { return s == 0 ? b.min[a] : b.max[a]; };
+  float ray_min = (sel(r.s[0], 0) - r.o[0]) * r.inv[0];
+  float ray_max = (sel(1 - r.s[0], 0) - r.o[0]) * r.inv[0];
+  float y_min = (sel(r.s[1], 1) - r.o[1]) * r.inv[1];
+  float y_max = (sel(1 - r.s[1], 1) - r.o[1]) * r.inv[1];
+  if ((ray_min > y_max) || (y_min > ray_max)) return false;
+  if (y_min > ray_min) ray_min = y_min;
+  if (y_max < ray_max) ray_max = y_max;
+  float z_min = (sel(r.s[2], 2) - r.o[2]) * r.inv[2];
+  float z_max = (sel(1 - r.s[2], 2) - r.o[2]) * r.inv[2];
+  if ((ray_min > z_max) || (z_min > ray_max)) return false;
+  if (z_max < ray_max) ray_max = z_max;
+  if (ray_max > r.t_min) {
+    *out = ray_max;
+    return true;
+  }
+  return false;
+}
+
+inline float h_sse_min(float a, float b) { return a < b ? a : b; }
+inline float h_sse_max(float a, float b) { return a > b ? a : b; }
+
+// src/mbvh_node.rs:176-240
+void h_quad(const RTMbvhNode& m, const HRay& r, uint8_t ids[4], bool res[4]) {
+  float tmin[4];
+  for (int i = 0; i < 4; ++i) {
+    float tx0 = (m.min_x[i] - r.o[0]) * r.inv[0], tx1 = (m.max_x[i] - r.o[0]) * r.inv[0];
+    float ty0 = (m.min_y[i] - r.o[1]) * r.inv[1], ty1 = (m.max_y[i] - r.o[1]) * r.inv[1];
+    float tz0 = (m.min_z[i] - r.o[2]) * r.inv[2], tz1 = (m.max_z[i] - r.o[2]) * r.inv[2];
+    float tn = h_sse_max(h_sse_min(tx0, tx1), h_sse_max(h_sse_min(ty0, ty1), h_sse_min(tz0, tz1)));
+    float tx = h_sse_min(h_sse_max(tx0, tx1), h_sse_min(h_sse_max(ty0, ty1), h_sse_max(tz0, tz1)));
+    tmin[i] = tn;
+    res[i] = (tx >= tn) && (tn < r.t);
+  }
+  uint8_t id[4] = {0, 1, 2, 3};
+  auto sw = [&](int a, int b, bool swap_t) {
+    if (swap_t) std::swap(tmin[a], tmin[b]);
+    std::swap(id[a], id[b]);
+  };
+  if (tmin[0] > tmin[1]) sw(0, 1, true);
+  if (tmin[2] > tmin[3]) sw(2, 3, true);
+  if (tmin[0] > tmin[2]) sw(0, 2, true);
+  if (tmin[1] > tmin[3]) sw(1, 3, true);
+  if (tmin[2] > tmin[3]) sw(2, 3, false);
+  for (int i = 0; i < 4; ++i) ids[i] = id[i];
+}
+
+// Packet form (4 rays, SoA) of the quad test, src/mbvh_node.rs:242-295.
+struct HPacket {
+  float o[3][4], inv[3][4];
+  float t[4];
+};
+void h_quad4(const RTMbvhNode& m, const HPacket& p, bool res[4]) {
+  const float* mins[3] = {m.min_x, m.min_y, m.min_z};
+  const float* maxs[3] = {m.max_x, m.max_y, m.max_z};
+  for (int s = 0; s < 4; ++s) res[s] = false;
+  for (int i = 0; i < 4; ++i) {  // ray i of the packet
+    float tmin[4], tmax[4];
+    for (int s = 0; s < 4; ++s) {
+      float t1 = (mins[0][s] - p.o[0][i]) * p.inv[0][i], t2 = (maxs[0][s] - p.o[0][i]) * p.inv[0][i];
+      tmin[s] = h_sse_min(t1, t2);
+      tmax[s] = h_sse_max(t1, t2);
+      for (int a = 1; a < 3; ++a) {
+        t1 = (mins[a][s] - p.o[a][i]) * p.inv[a][i];
+        t2 = (maxs[a][s] - p.o[a][i]) * p.inv[a][i];
+        tmin[s] = h_sse_max(tmin[s], h_sse_min(t1, t2));
+        tmax[s] = h_sse_min(tmax[s], h_sse_max(t1, t2));
+      }
+      if ((tmax[s] > tmin[s]) && (tmin[s] < p.t[i])) res[s] = true;
+    }
+  }
+}
+
+// Aabb::intersect4 (src/aabb.rs:217-244): returns the per-ray t_min.
+bool h_box4(const RTAabb& b, const HPacket& p, float out[4]) {
+  bool any = false;
+  for (int i = 0; i < 4; ++i) {
+    float t1x = (b.min[0] - p.o[0][i]) * p.inv[0][i], t2x = (b.max[0] - p.o[0][i]) * p.inv[0][i];
+    float t1y = (b.min[1] - p.o[1][i]) * p.inv[1][i], t2y = (b.max[1] - p.o[1][i]) * p.inv[1][i];
+    float t1z = (b.min[2] - p.o[2][i]) * p.inv[2][i], t2z = (b.max[2] - p.o[2][i]) * p.inv[2][i];
+    float tmin = h_sse_max(h_sse_min(t1x, t2x), h_sse_max(h_sse_min(t1y, t2y), h_sse_min(t1z, t2z)));
+    float tmax = h_sse_min(h_sse_max(t1x, t2x), h_sse_min(h_sse_max(t1y, t2y), h_sse_max(t1z, t2z)));
+    out[i] = tmin;
+    if (tmax > 0.0f && tmax > tmin && tmin < p.t[i]) any = true;
+  }
+  return any;
+}
+
+constexpr int kHostStack = 64;
+
+bool finite3(const float* v) { return !(v[0] != v[0] || v[1] != v[1] || v[2] != v[2]); }
+
+}  // namespace
+
+// =================================================================== part 1
+extern "C" {
+
+ResultCode create_spatial_Bvh(const RTAabb*, uintptr_t, const float*, uintptr_t, const float*, uintptr_t,
+                              uintptr_t, uint32_t, RTBvh*) {
+  return Error;
+}
+
+ResultCode create_bvh(const RTAabb* aabbs, uintptr_t prim_count, const float* centers, uintptr_t center_stride,
+                      uintptr_t prims_per_leaf, BvhType bvh_type, RTBvh* result) {
+  if (centers == nullptr || result == nullptr) return Error;
+  if (center_stride % 4 != 0 || center_stride < 12 || center_stride > 16) return Error;
+  if (prim_count == 0) return NoPrimitives;
+  if (bvh_type != LocallyOrderedClustered && bvh_type != BinnedSAH) bvh_type = BinnedSAH;  // BvhType::from
+  cudaStream_t s = legacy_stream();
+  const size_t n = prim_count, stride = center_stride / 4;
+  Scratch<float> d_c;
+  Scratch<DAabb> d_a;
+  Scratch<float4> d_c4;
+  cudaError_t e;
+  if ((e = d_c.alloc(n * stride, s)) || (e = d_a.alloc(n, s)) || (e = d_c4.alloc(n, s))) return cuda_rc(e);
+  if ((e = cudaMemcpyAsync(d_c.ptr, centers, n * center_stride, cudaMemcpyHostToDevice, s))) return cuda_rc(e);
+  if (aabbs) {
+    if ((e = cudaMemcpyAsync(d_a.ptr, aabbs, n * sizeof(RTAabb), cudaMemcpyHostToDevice, s))) return cuda_rc(e);
+    if ((e = launch_pack_centers(d_c.ptr, stride, n, d_c4.ptr, s))) return cuda_rc(e);
+  } else {
+    if ((e = launch_point_prep(d_c.ptr, stride, n, d_a.ptr, d_c4.ptr, s))) return cuda_rc(e);
+  }
+  return build_and_store(d_a.ptr, d_c4.ptr, n, prims_per_leaf, bvh_type, nullptr, 0, s, result);
+}
+
+ResultCode create_mbvh(RTBvh bvh, RTMbvh* mbvh) {
+  if (mbvh == nullptr || bvh.nodes == nullptr || bvh.indices == nullptr) return Error;
+  return rtbvh_gpu_create_mbvh(bvh, 0, legacy_stream(), mbvh);
+}
+
+ResultCode refit(const RTAabb* aabbs, RTBvh bvh) {
+  if (aabbs == nullptr || bvh.nodes == nullptr || bvh.indices == nullptr) return Error;
+  cudaStream_t s = legacy_stream();
+  uint32_t n;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(bvh.id, false);
+    if (!e) return Error;
+    n = e->prim_count;
+  }
+  Scratch<DAabb> d_a;
+  cudaError_t err;
+  if ((err = d_a.alloc(n, s)) ||
+      (err = cudaMemcpyAsync(d_a.ptr, aabbs, (size_t)n * sizeof(RTAabb), cudaMemcpyHostToDevice, s)))
+    return cuda_rc(err);
+  return rtbvh_gpu_refit(bvh.id, nullptr, reinterpret_cast<const RTAabb*>(d_a.ptr), UINT32_MAX, s);
+}
+
+// rtbvh_ffi/src/lib.rs:551-581 over src/iter_indices.rs:66-107.
+ResultCode intersect(RTBvh bvh, const float* origin, const float* direction, float* t, void* user_data,
+                     RTIntersectFn cb) {
+  if (!finite3(origin) || !finite3(direction)) return Nan;
+  HRay r = make_hray(origin, direction, *t);
+  const RTBvhNode* nodes = bvh.nodes;
+  const uint32_t* idx = bvh.indices;
+  if (bvh.node_count == 0 || nodes == nullptr) {
+    *t = r.t;
+    return Ok;
+  }
+  int32_t stack[kHostStack];
+  stack[0] = 0;
+  int32_t sp = 0;
+  while (sp >= 0) {
+    const RTAabb& nd = nodes[stack[sp--]].aabb;
+    if (nd.count > -1) {
+      bool stop = false;
+      for (int32_t i = 0; i < nd.count && !stop; ++i) stop = cb(idx[nd.left_first + i], &r.t, user_data);
+      if (stop) break;
+    } else if (nd.left_first > -1) {
+      const int32_t lf = nd.left_first;
+      float lt = 0, rt = 0;
+      bool lh = h_slab_far(nodes[lf].aabb, r, &lt), rh = h_slab_far(nodes[lf + 1].aabb, r, &rt);
+      if (sp + 2 >= kHostStack) return StackOverflow;
+      if (lh && rh) {
+        if (lt < rt) { stack[++sp] = lf; stack[++sp] = lf + 1; }
+        else { stack[++sp] = lf + 1; stack[++sp] = lf; }
+      } else if (lh) {
+        stack[++sp] = lf;
+      } else if (rh) {
+        stack[++sp] = lf + 1;
+      }
+    }
+  }
+  *t = r.t;
+  return Ok;
+}
+
+// rtbvh_ffi/src/lib.rs:700-731 over src/iter_indices.rs:264-313.
+ResultCode intersect_mbvh(RTMbvh bvh, const float* origin, const float* direction, float* t, void* user_data,
+                          RTIntersectFn cb) {
+  if (!finite3(origin) || !finite3(direction)) return Nan;
+  HRay r = make_hray(origin, direction, *t);
+  const RTMbvhNode* nodes = bvh.nodes;
+  const uint32_t* idx = bvh.indices;
+  if (bvh.node_count == 0 || nodes == nullptr) {
+    *t = r.t;
+    return Ok;
+  }
+  int32_t stack[kHostStack];
+  int32_t sp = -1, current = 0;
+  uint8_t ids[4];
+  bool res[4];
+  h_quad(nodes[0], r, ids, res);
+  for (;;) {
+    const RTMbvhNode& node = nodes[current];
+    bool stop = false;
+    for (int i = 0; i < 4 && !stop; ++i) {
+      int id = ids[3 - i];
+      if (!res[id]) continue;
+      int32_t count = node.counts[id], lf = node.children[id];
+      if (count > -1) {
+        for (int32_t j = 0; j < count && !stop; ++j) stop = cb(idx[lf + j], &r.t, user_data);
+      } else if (lf > -1) {
+        if (sp + 1 >= kHostStack) return StackOverflow;
+        stack[++sp] = lf;
+      }
+    }
+    if (stop || sp < 0) break;
+    current = stack[sp--];
+    h_quad(nodes[current], r, ids, res);
+  }
+  *t = r.t;
+  return Ok;
+}
+
+static bool load_packet(const float* ox, const float* oy, const float* oz, const float* dx, const float* dy,
+                        const float* dz, const float* t, HPacket& p) {
+  const float* o[3] = {ox, oy, oz};
+  const float* d[3] = {dx, dy, dz};
+  for (int a = 0; a < 3; ++a)
+    for (int i = 0; i < 4; ++i) {
+      if (o[a][i] != o[a][i] || d[a][i] != d[a][i]) return false;
+      p.o[a][i] = o[a][i];
+      p.inv[a][i] = 1.0f / d[a][i];
+    }
+  for (int i = 0; i < 4; ++i) p.t[i] = t[i];
+  return true;
+}
+
+// rtbvh_ffi/src/lib.rs:599-686 over src/iter_indices.rs:169-210 (packet
+// traversal is not part of the GPU path; this is the host compatibility form).
+ResultCode intersect_packet(RTBvh bvh, const float* origin_x, const float* origin_y, const float* origin_z,
+                            const float* direction_x, const float* direction_y, const float* direction_z, float* t,
+                            void* user_data, RTIntersectFn cb) {
+  HPacket p;
+  if (!load_packet(origin_x, origin_y, origin_z, direction_x, direction_y, direction_z, t, p)) return Nan;
+  const RTBvhNode* nodes = bvh.nodes;
+  const uint32_t* idx = bvh.indices;
+  if (bvh.node_count > 0 && nodes) {
+    int32_t stack[kHostStack];
+    stack[0] = 0;
+    int32_t sp = 0;
+    while (sp >= 0) {
+      const RTAabb& nd = nodes[stack[sp--]].aabb;
+      if (nd.count > -1) {
+        bool stop = false;
+        for (int32_t i = 0; i < nd.count && !stop; ++i) stop = cb(idx[nd.left_first + i], p.t, user_data);
+        if (stop) break;
+      } else if (nd.left_first > -1) {
+        const int32_t lf = nd.left_first;
+        float lt[4], rt[4];
+        bool lh = h_box4(nodes[lf].aabb, p, lt), rh = h_box4(nodes[lf + 1].aabb, p, rt);
+        if (sp + 2 >= kHostStack) return StackOverflow;
+        if (lh && rh) {
+          bool any_less = false;
+          for (int i = 0; i < 4; ++i) any_less = any_less || (lt[i] < rt[i]);
+          if (any_less) { stack[++sp] = lf; stack[++sp] = lf + 1; }
+          else { stack[++sp] = lf + 1; stack[++sp] = lf; }
+        } else if (lh) {
+          stack[++sp] = lf;
+        } else if (rh) {
+          stack[++sp] = lf + 1;
+        }
+      }
+    }
+  }
+  for (int i = 0; i < 4; ++i) t[i] = p.t[i];
+  return Ok;
+}
+
+// rtbvh_ffi/src/lib.rs:749-835 over src/iter_indices.rs:367-414.
+ResultCode intersect_mbvh_packet(RTMbvh bvh, const float* origin_x, const float* origin_y, const float* origin_z,
+                                 const float* direction_x, const float* direction_y, const float* direction_z,
+                                 float* t, void* user_data, RTIntersectFn cb) {
+  HPacket p;
+  if (!load_packet(origin_x, origin_y, origin_z, direction_x, direction_y, direction_z, t, p)) return Nan;
+  const RTMbvhNode* nodes = bvh.nodes;
+  const uint32_t* idx = bvh.indices;
+  if (bvh.node_count > 0 && nodes) {
+    int32_t stack[kHostStack];
+    int32_t sp = -1, current = 0;
+    bool res[4];
+    h_quad4(nodes[0], p, res);
+    for (;;) {
+      const RTMbvhNode& node = nodes[current];
+      bool stop = false;
+      for (int i = 0; i < 4 && !stop; ++i) {
+        int id = 3 - i;
+        if (!res[id]) continue;
+        int32_t count = node.counts[id], lf = node.children[id];
+        if (count > -1) {
+          for (int32_t j = 0; j < count && !stop; ++j) stop = cb(idx[lf + j], p.t, user_data);
+        } else if (lf > -1) {
+          if (sp + 1 >= kHostStack) return StackOverflow;
+          stack[++sp] = lf;
+        }
+      }
+      if (stop || sp < 0) break;
+      current = stack[sp--];
+      h_quad4(nodes[current], p, res);
+    }
+  }
+  for (int i = 0; i < 4; ++i) t[i] = p.t[i];
+  return Ok;
+}
+
+void free_bvh(RTBvh bvh) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (bvh.id < g_bvh.size() && g_bvh[bvh.id]) {
+    g_bvh[bvh.id]->release();
+  } else {
+    fprintf(stderr, "Could not free bvh with id: %u\n", bvh.id);
+  }
+}
+
+void free_mbvh(RTMbvh bvh) {
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (bvh.id < g_mbvh.size() && g_mbvh[bvh.id]) {
+    g_mbvh[bvh.id]->release();
+  } else {
+    fprintf(stderr, "Could not free bvh with id: %u\n", bvh.id);
+  }
+}
+
+// =================================================================== part 2
+
+ResultCode rtbvh_gpu_create_bvh_from_triangles(const float* vertices, uintptr_t prim_count, uintptr_t prims_per_leaf,
+                                               BvhType bvh_type, uint32_t flags, rtbvh_stream_t stream,
+                                               RTBvh* result) {
+  if (result == nullptr || (vertices == nullptr && prim_count > 0)) return Error;
+  if (prim_count == 0) return NoPrimitives;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch<DAabb> d_a;
+  Scratch<float4> d_c4;
+  cudaError_t e;
+  if ((e = d_a.alloc(prim_count, s)) || (e = d_c4.alloc(prim_count, s))) return cuda_rc(e);
+  if ((e = launch_triangle_prep(vertices, prim_count, d_a.ptr, d_c4.ptr, s))) return cuda_rc(e);
+  return build_and_store(d_a.ptr, d_c4.ptr, prim_count, prims_per_leaf, bvh_type, vertices, flags, s, result);
+}
+
+ResultCode rtbvh_gpu_create_bvh(const RTAabb* aabbs, uintptr_t prim_count, const float* centers,
+                                uintptr_t center_stride, uintptr_t prims_per_leaf, BvhType bvh_type, uint32_t flags,
+                                rtbvh_stream_t stream, RTBvh* result) {
+  if (result == nullptr || centers == nullptr || aabbs == nullptr) return Error;
+  if (center_stride % 4 != 0 || center_stride < 12 || center_stride > 16) return Error;
+  if (prim_count == 0) return NoPrimitives;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch<float4> d_c4;
+  cudaError_t e;
+  if ((e = d_c4.alloc(prim_count, s))) return cuda_rc(e);
+  if ((e = launch_pack_centers(centers, center_stride / 4, prim_count, d_c4.ptr, s))) return cuda_rc(e);
+  return build_and_store(reinterpret_cast<const DAabb*>(aabbs), d_c4.ptr, prim_count, prims_per_leaf, bvh_type,
+                         nullptr, flags, s, result);
+}
+
+ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t stream, RTMbvh* result) {
+  if (result == nullptr) return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  DAabb* d_nodes;
+  uint32_t node_count, prim_count;
+  const uint32_t* d_indices;
+  const float4* d_tris;
+  const float* d_vertices;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* src = lookup(bvh.id, false);
+    if (!src) return Error;
+    d_nodes = src->d_nodes;
+    node_count = src->node_count;
+    prim_count = src->prim_count;
+    d_indices = src->d_indices;
+    d_tris = src->d_tris;
+    d_vertices = src->d_vertices;
+  }
+  auto e = std::make_unique<Entry>();
+  e->alive = true;
+  e->prim_count = prim_count;
+  e->source_bvh = bvh.id;
+  ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
+  if (rc != Ok) return rc;
+  cudaError_t err;
+  if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
+      (err = dmalloc(&e->d_indices, prim_count)) ||
+      (err = cudaMemcpyAsync(e->d_indices, d_indices, (size_t)prim_count * 4, cudaMemcpyDeviceToDevice, s))) {
+    e->release();
+    return cuda_rc(err);
+  }
+  if (d_tris) {
+    if ((err = dmalloc(&e->d_tris, 3 * (size_t)prim_count)) ||
+        (err = cudaMemcpyAsync(e->d_tris, d_tris, 48 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
+        (err = dmalloc(&e->d_vertices, 9 * (size_t)prim_count)) ||
+        (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s))) {
+      e->release();
+      return cuda_rc(err);
+    }
+  }
+  if (!(flags & RTBVH_FLAG_NO_HOST_MIRROR)) {
+    if ((rc = mirror_mbvh(*e, s)) != Ok) {
+      e->release();
+      return rc;
+    }
+  } else if ((err = cudaStreamSynchronize(s))) {
+    e->release();
+    return cuda_rc(err);
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* raw = e.get();
+  uint32_t id = store(std::move(e), true);
+  *result = mbvh_handle(id, *raw);
+  return Ok;
+}
+
+ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const float* vertices, uintptr_t prim_count,
+                                   rtbvh_stream_t stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* e = lookup(structure_id, is_mbvh != 0);
+  if (!e || vertices == nullptr) return Error;
+  if (prim_count != e->prim_count) return InequalAabbsAndPrimitives;
+  cudaError_t err;
+  if (!e->d_vertices && (err = dmalloc(&e->d_vertices, 9 * (size_t)prim_count))) return cuda_rc(err);
+  if (!e->d_tris && (err = dmalloc(&e->d_tris, 3 * (size_t)prim_count))) return cuda_rc(err);
+  if ((err = cudaMemcpyAsync(e->d_vertices, vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
+      (err = launch_gather_triangles(e->d_vertices, e->d_indices, prim_count, e->d_tris, s)))
+    return cuda_rc(err);
+  return Ok;
+}
+
+static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
+                               float* hits, uint32_t flags, uint32_t* stats, cudaStream_t s) {
+  TraceArgs a;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(id, mbvh);
+    if (!e) return Error;
+    if (!e->d_tris && e->node_count > 0) return InvalidArgument;
+    a.mnodes = e->d_mnodes;
+    a.nodes = e->d_nodes;
+    a.node_count = e->node_count;
+    a.tris = e->d_tris;
+    a.prim_count = e->prim_count;
+    a.status = e->d_status;
+  }
+  if (ray_count == 0) return Ok;
+  if (rays == nullptr || hits == nullptr) return Error;
+  a.rays = rays;
+  a.t_max = t_max;
+  a.ray_count = ray_count;
+  a.hits = reinterpret_cast<float4*>(hits);
+  a.stats = (flags & RTBVH_TRACE_STATS) ? stats : nullptr;
+  a.any_hit = (flags & RTBVH_TRACE_ANY_HIT) != 0;
+  cudaError_t err = mbvh ? launch_trace_mbvh(a, s) : launch_trace_bvh(a, s);
+  return cuda_rc(err);
+}
+
+ResultCode rtbvh_gpu_intersect_mbvh(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
+                                    float* hits, uint32_t flags, uint32_t* stats, rtbvh_stream_t stream) {
+  return trace_common(mbvh.id, true, rays, t_max, ray_count, hits, flags, stats, static_cast<cudaStream_t>(stream));
+}
+
+ResultCode rtbvh_gpu_intersect_bvh(RTBvh bvh, const float* rays, const float* t_max, uintptr_t ray_count,
+                                   float* hits, uint32_t flags, uint32_t* stats, rtbvh_stream_t stream) {
+  return trace_common(bvh.id, false, rays, t_max, ray_count, hits, flags, stats, static_cast<cudaStream_t>(stream));
+}
+
+ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
+                                      float* hits, uint32_t flags) {
+  if (ray_count == 0) return Ok;
+  if (rays == nullptr || hits == nullptr) return Error;
+  static cudaStream_t streams[2] = {nullptr, nullptr};
+  static std::once_flag once;
+  std::call_once(once, []() {
+    cudaStreamCreateWithFlags(&streams[0], cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&streams[1], cudaStreamNonBlocking);
+  });
+  const size_t chunk = (size_t)1 << 21;
+  const size_t per = ray_count < chunk ? ray_count : chunk;
+  Scratch<float> d_rays[2], d_tmax[2];
+  Scratch<float4> d_hits[2];
+  cudaError_t e;
+  for (int k = 0; k < 2; ++k) {
+    if ((e = d_rays[k].alloc(6 * per, streams[k])) || (e = d_hits[k].alloc(per, streams[k]))) return cuda_rc(e);
+    if (t_max && (e = d_tmax[k].alloc(per, streams[k]))) return cuda_rc(e);
+  }
+  ResultCode rc = Ok;
+  for (size_t c0 = 0, k = 0; c0 < ray_count; c0 += per, k ^= 1) {
+    const size_t cnt = (ray_count - c0) < per ? (ray_count - c0) : per;
+    cudaStream_t s = streams[k];
+    if ((e = cudaMemcpyAsync(d_rays[k].ptr, rays + 6 * c0, 24 * cnt, cudaMemcpyHostToDevice, s))) return cuda_rc(e);
+    if (t_max && (e = cudaMemcpyAsync(d_tmax[k].ptr, t_max + c0, 4 * cnt, cudaMemcpyHostToDevice, s)))
+      return cuda_rc(e);
+    rc = trace_common(mbvh.id, true, d_rays[k].ptr, t_max ? d_tmax[k].ptr : nullptr, cnt,
+                      reinterpret_cast<float*>(d_hits[k].ptr), flags & ~RTBVH_TRACE_STATS, nullptr, s);
+    if (rc != Ok) break;
+    if ((e = cudaMemcpyAsync(hits + 4 * c0, d_hits[k].ptr, 16 * cnt, cudaMemcpyDeviceToHost, s))) return cuda_rc(e);
+  }
+  if ((e = cudaStreamSynchronize(streams[0])) || (e = cudaStreamSynchronize(streams[1]))) return cuda_rc(e);
+  return rc;
+}
+
+ResultCode rtbvh_gpu_status(uint32_t structure_id, int is_mbvh) {
+  uint32_t* d_status;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(structure_id, is_mbvh != 0);
+    if (!e) return Error;
+    d_status = e->d_status;
+  }
+  uint32_t st = 0;
+  cudaError_t err;
+  if ((err = cudaDeviceSynchronize()) || (err = cudaMemcpy(&st, d_status, 4, cudaMemcpyDeviceToHost)) ||
+      (err = cudaMemset(d_status, 0, 4)))
+    return cuda_rc(err);
+  if (st & kStatusStackOverflow) return StackOverflow;
+  if (st & kStatusTimeout) return Timeout;
+  if (st) return Error;
+  return Ok;
+}
+
+ResultCode rtbvh_gpu_view(uint32_t structure_id, int is_mbvh, RTGpuView* view) {
+  if (view == nullptr) return Error;
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* e = lookup(structure_id, is_mbvh != 0);
+  if (!e) return Error;
+  view->nodes = is_mbvh ? static_cast<const void*>(e->d_mnodes) : static_cast<const void*>(e->d_nodes);
+  view->node_count = e->node_count;
+  view->indices = e->d_indices;
+  view->index_count = e->prim_count;
+  view->leaf_triangles = reinterpret_cast<const float*>(e->d_tris);
+  return Ok;
+}
+
+ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb* aabbs, uint32_t mbvh_id,
+                           rtbvh_stream_t stream) {
+  if ((vertices == nullptr) == (aabbs == nullptr)) return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* b = lookup(bvh_id, false);
+  if (!b) return Error;
+  Entry* m = nullptr;
+  if (mbvh_id != UINT32_MAX) {
+    m = lookup(mbvh_id, true);
+    if (!m || m->source_bvh != bvh_id) return Error;
+  }
+  const size_t n = b->prim_count;
+  Scratch<DAabb> d_a;
+  Scratch<float4> d_c4;
+  const DAabb* boxes = reinterpret_cast<const DAabb*>(aabbs);
+  cudaError_t err;
+  if (vertices) {
+    if ((err = d_a.alloc(n, s)) || (err = d_c4.alloc(n, s))) return cuda_rc(err);
+    if ((err = launch_triangle_prep(vertices, n, d_a.ptr, d_c4.ptr, s))) return cuda_rc(err);
+    boxes = d_a.ptr;
+    if (b->d_vertices) {
+      if ((err = cudaMemcpyAsync(b->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
+          (err = launch_gather_triangles(b->d_vertices, b->d_indices, n, b->d_tris, s)))
+        return cuda_rc(err);
+    }
+  }
+  ResultCode rc = refit_bvh(b->d_nodes, b->node_count, b->d_indices, b->prim_count, boxes, s);
+  if (rc != Ok) return rc;
+  if (m) {
+    DMNode* fresh = nullptr;
+    uint32_t count = 0;
+    if ((rc = build_mbvh(b->d_nodes, b->node_count, s, &fresh, &count)) != Ok) return rc;
+    if (count != m->node_count) {
+      cudaFree(fresh);
+      return Error;
+    }
+    cudaFree(m->d_mnodes);
+    m->d_mnodes = fresh;
+    if (vertices) {
+      if (!m->d_vertices && (err = dmalloc(&m->d_vertices, 9 * n))) return cuda_rc(err);
+      if (!m->d_tris && (err = dmalloc(&m->d_tris, 3 * n))) return cuda_rc(err);
+      if ((err = cudaMemcpyAsync(m->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
+          (err = launch_gather_triangles(m->d_vertices, m->d_indices, n, m->d_tris, s)))
+        return cuda_rc(err);
+    }
+    if (m->mirrored && (rc = mirror_mbvh(*m, s)) != Ok) return rc;
+  }
+  if (b->mirrored && (rc = mirror_bvh(*b, s)) != Ok) return rc;
+  return Ok;
+}
+
+ResultCode rtbvh_gpu_intersect_backward(const float* vertices, uintptr_t prim_count, const float* rays,
+                                        const float* hits, const float* grad_tuv, uintptr_t ray_count,
+                                        float* grad_vertices, float* grad_rays, rtbvh_stream_t stream) {
+  if (vertices == nullptr || rays == nullptr || hits == nullptr || grad_tuv == nullptr || grad_vertices == nullptr)
+    return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return cuda_rc(launch_intersect_backward(vertices, prim_count, rays, reinterpret_cast<const float4*>(hits),
+                                           grad_tuv, ray_count, grad_vertices, grad_rays, s));
+}
+
+const char* rtbvh_gpu_version(void) { return "rtbvh-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,174 @@
+// Device-side building blocks shared by the build and traversal kernels.
+//
+// Every translation unit that includes this file is compiled with
+// --fmad=false and IEEE division/sqrt, so plain float expressions round
+// exactly like the reference's scalar Rust code (no contraction into FMA).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rtbvh {
+
+// ------------------------------------------------------------- status words
+// Bits a kernel ORs into its status word instead of trapping.
+enum DeviceStatus : uint32_t {
+  kStatusOk = 0,
+  kStatusTimeout = 1u << 0,        // a bounded spin gave up
+  kStatusStackOverflow = 1u << 1,  // a traversal stack bound was hit
+  kStatusNoMerge = 1u << 2,        // a clustering level merged nothing
+  kStatusBadIndex = 1u << 3,       // an index failed its bounds check
+  kStatusNoNeighbour = 1u << 4,    // a cluster found no neighbour
+};
+
+// Spin budget of every device-side wait: ~2^22 polls with a 256 ns back-off,
+// i.e. about a second, after which the waiter sets kStatusTimeout and leaves.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// ------------------------------------------------------------- node layouts
+// RTAabb / BvhNode (src/aabb.rs:13-20): min, count(extra1), max, left_first(extra2).
+struct alignas(16) DAabb {
+  float min[3];
+  int32_t count;
+  float max[3];
+  int32_t left_first;
+};
+static_assert(sizeof(DAabb) == 32, "DAabb must be 32 bytes");
+
+// RTMbvhNode (src/mbvh_node.rs:29-38).
+struct alignas(128) DMNode {
+  float min_x[4], max_x[4], min_y[4], max_y[4], min_z[4], max_z[4];
+  int32_t children[4];
+  int32_t counts[4];
+};
+static_assert(sizeof(DMNode) == 128, "DMNode must be 128 bytes");
+
+// ------------------------------------------------------------- float helpers
+// Vec3::min / Vec3::max of the reference (Rust f32::min/max): NaN operands are
+// ignored; on a -0/+0 tie min gives -0 and max gives +0 (order-independent).
+__device__ __forceinline__ float rs_min(float a, float b) {
+  float r = fminf(a, b);
+  if (a == b) r = __int_as_float(__float_as_int(a) | __float_as_int(b));
+  return r;
+}
+__device__ __forceinline__ float rs_max(float a, float b) {
+  float r = fmaxf(a, b);
+  if (a == b) r = __int_as_float(__float_as_int(a) & __float_as_int(b));
+  return r;
+}
+// _mm_min_ps / _mm_max_ps: the second operand wins on NaN or equality.
+__device__ __forceinline__ float sse_min(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float sse_max(float a, float b) { return a > b ? a : b; }
+
+// Order-preserving map of floats to uint32 (-0 sorts below +0) for atomic
+// min/max reductions.
+__device__ __forceinline__ uint32_t float_to_ordered(float f) {
+  uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Aabb::half_area (src/aabb.rs:342-346), no FMA.
+__device__ __forceinline__ float half_area(float mnx, float mny, float mnz, float mxx, float mxy, float mxz) {
+  float d0 = mxx - mnx, d1 = mxy - mny, d2 = mxz - mnz;
+  float t = (d0 + d1) * d2;
+  float u = d0 * d1;
+  return t + u;
+}
+
+__device__ __forceinline__ DAabb load_aabb(const DAabb* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  float4 a = __ldg(q), b = __ldg(q + 1);
+  DAabb r;
+  r.min[0] = a.x; r.min[1] = a.y; r.min[2] = a.z; r.count = __float_as_int(a.w);
+  r.max[0] = b.x; r.max[1] = b.y; r.max[2] = b.z; r.left_first = __float_as_int(b.w);
+  return r;
+}
+// Load that bypasses L1 (data written by other blocks of the same launch).
+__device__ __forceinline__ DAabb load_aabb_cg(const DAabb* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  float4 a = __ldcg(q), b = __ldcg(q + 1);
+  DAabb r;
+  r.min[0] = a.x; r.min[1] = a.y; r.min[2] = a.z; r.count = __float_as_int(a.w);
+  r.max[0] = b.x; r.max[1] = b.y; r.max[2] = b.z; r.left_first = __float_as_int(b.w);
+  return r;
+}
+__device__ __forceinline__ void store_aabb(DAabb* p, const DAabb& r) {
+  float4* q = reinterpret_cast<float4*>(p);
+  q[0] = make_float4(r.min[0], r.min[1], r.min[2], __int_as_float(r.count));
+  q[1] = make_float4(r.max[0], r.max[1], r.max[2], __int_as_float(r.left_first));
+}
+
+// ------------------------------------------------------------- grid barrier
+// Sense-counting barrier for cooperative launches. Waits are bounded: on
+// timeout the status word gets kStatusTimeout and the caller must return.
+struct GridBarrier {
+  unsigned int count;
+  unsigned int generation;
+};
+
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int nblocks, uint32_t* status) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned int* vgen = &bar->generation;
+    unsigned int gen = *vgen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(&bar->count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(&bar->count, 0u);
+      __threadfence();
+      atomicAdd(&bar->generation, 1u);
+    } else {
+      uint32_t it = 0;
+      while (*vgen == gen) {
+        if (++it > kSpinLimit) {
+          atomicOr(status, kStatusTimeout);
+          ok = 0;
+          break;
+        }
+        __nanosleep(256);
+      }
+    }
+    __threadfence();
+    if (ok && (*(volatile uint32_t*)status & kStatusTimeout)) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ------------------------------------------------------------- block scan
+// Inclusive scan of one value per thread over a block of BLOCK threads.
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t v, uint32_t* s_warp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = BLOCK / 32;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t n = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += n;
+  }
+  if (lane == 31) s_warp[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < NW ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t n = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += n;
+    }
+    if (lane < NW) s_warp[lane] = w;
+  }
+  __syncthreads();
+  uint32_t prefix = warp > 0 ? s_warp[warp - 1] : 0u;
+  uint32_t t = s_warp[NW - 1];
+  __syncthreads();
+  if (total) *total = t;
+  return v + prefix;
+}
+
+}  // namespace rtbvh

@@ -1,0 +1,116 @@
+// Host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/rtbvh.h"
+#include "device_common.cuh"
+
+namespace rtbvh {
+
+// Stream-ordered scratch buffer (cudaMallocAsync / cudaFreeAsync).
+template <class T>
+struct Scratch {
+  T* ptr = nullptr;
+  size_t count = 0;
+  cudaStream_t stream = nullptr;
+  cudaError_t alloc(size_t n, cudaStream_t s) {
+    stream = s;
+    count = n;
+    if (n == 0) return cudaSuccess;
+    return cudaMallocAsync(reinterpret_cast<void**>(&ptr), n * sizeof(T), s);
+  }
+  ~Scratch() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+  }
+  Scratch() = default;
+  Scratch(const Scratch&) = delete;
+  Scratch& operator=(const Scratch&) = delete;
+};
+
+// ------------------------------------------------------------------ prep
+// Triangle::aabb / Triangle::center (shared/src/lib.rs:27-39) of n triangles
+// (9 floats each). centers are written as float4 (w = 0).
+cudaError_t launch_triangle_prep(const float* vertices, size_t n, DAabb* aabbs, float4* centers, cudaStream_t s);
+// Primitive::aabb of point primitives (rtbvh_ffi/src/lib.rs:396-422): the
+// empty box grown by the point. Also repacks the centres into float4.
+cudaError_t launch_point_prep(const float* centers, size_t stride_floats, size_t n, DAabb* aabbs, float4* centers4,
+                              cudaStream_t s);
+// Repacks strided centres into float4.
+cudaError_t launch_pack_centers(const float* centers, size_t stride_floats, size_t n, float4* centers4,
+                                cudaStream_t s);
+// Aabb::union_of_list (src/aabb.rs:124-131) into *world (one DAabb).
+cudaError_t launch_world_bounds(const DAabb* aabbs, size_t n, DAabb* world, uint32_t* acc6, cudaStream_t s);
+// MortonEncoder::encode of every centre against `world` (src/morton.rs:36-61);
+// vals[i] = i.
+cudaError_t launch_morton(const float4* centers, size_t n, const DAabb* world, uint32_t* keys, uint32_t* vals,
+                          cudaStream_t s);
+// Leaf-ordered triangles: out[3k..3k+2] = {v0, prim}, {v1 - v0, 0}, {v2 - v0, 0}
+// for p = indices[k].
+cudaError_t launch_gather_triangles(const float* vertices, const uint32_t* indices, size_t n, float4* out,
+                                    cudaStream_t s);
+
+// ------------------------------------------------------------------ sort
+// Stable LSD radix sort (onesweep) of (key, value) pairs on the low `bits`
+// key bits. Buffers are ping-ponged; the sorted data ends in keys/vals.
+// `status` receives kStatusTimeout if a look-back wait gave up.
+size_t radix_sort_temp_bytes(size_t n);
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, size_t n, int bits, void* temp, size_t temp_bytes,
+                             uint32_t* status, cudaStream_t s);
+
+// ------------------------------------------------------------------ builds
+struct BuildOutput {
+  DAabb* nodes = nullptr;        // device, node_count entries (cudaMalloc'd, owned by caller)
+  uint32_t* indices = nullptr;   // device, prim_count entries
+  uint32_t node_count = 0;
+};
+// Builder::construct_locally_ordered_clustered (src/bvh.rs:113-137,
+// src/builders/locb.rs). aabbs/centers are device arrays of n entries.
+ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n, cudaStream_t s, BuildOutput* out);
+// Builder::construct_binned_sah (src/bvh.rs:87-111, src/builders/binned_sah.rs).
+ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n, size_t prims_per_leaf,
+                            cudaStream_t s, BuildOutput* out);
+
+// Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here.
+ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes,
+                      uint32_t* mnode_count);
+
+// Bvh::refit (src/bvh.rs:176-205) bounds, topology kept.
+ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
+                     const DAabb* aabbs, cudaStream_t s);
+
+// ------------------------------------------------------------------ traversal
+struct TraceArgs {
+  const DMNode* mnodes = nullptr;
+  const DAabb* nodes = nullptr;
+  uint32_t node_count = 0;
+  const float4* tris = nullptr;  // leaf-ordered, 3 float4 per index slot
+  uint32_t prim_count = 0;       // index slots (bounds of leaf ranges)
+  const float* rays = nullptr;
+  const float* t_max = nullptr;
+  size_t ray_count = 0;
+  float4* hits = nullptr;
+  uint32_t* stats = nullptr;
+  uint32_t* status = nullptr;
+  bool any_hit = false;
+};
+cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
+cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
+
+// ------------------------------------------------------------------ backward
+cudaError_t launch_intersect_backward(const float* vertices, size_t prim_count, const float* rays,
+                                      const float4* hits, const float* grad_tuv, size_t ray_count,
+                                      float* grad_vertices, float* grad_rays, cudaStream_t s);
+
+// Number of SMs of the current device (cached).
+int sm_count();
+
+inline ResultCode cuda_rc(cudaError_t e) {
+  if (e == cudaSuccess) return Ok;
+  if (e == cudaErrorMemoryAllocation) return OutOfMemory;
+  return DeviceError;
+}
+
+}  // namespace rtbvh

@@ -1,0 +1,357 @@
+// Locally-ordered clustering build (src/builders/locb.rs) on the GPU.
+//
+// Pipeline: primitive boxes -> world box (Aabb::union_of_list) -> 30-bit
+// Morton codes of the centres -> stable radix sort -> leaves (sorted boxes
+// + 1e-4) -> clustering levels until one node is left.
+//
+// All clustering levels run in ONE cooperative launch. A level of m nodes
+// [begin, end) does, with a grid barrier after each phase:
+//   1. nearest neighbour of every node inside the window
+//      [max(begin, i-14), min(end, i+15)) by the half area of the union,
+//      first (lowest index) minimum wins -- boxes staged in shared memory;
+//   2. per-block counts of the merge flags (i < j, nb[j] == i);
+//   3. the inclusive prefix of the flags and the scatter of parents,
+//      unmerged nodes (next level) and children (final node array).
+// Node positions follow the reference exactly (locb.rs:178-215), so the
+// output is bit-identical to the reference's node array. Levels of at most
+// kTailNodes nodes are finished by block 0 alone with block barriers.
+#include <cstdio>
+
+#include "lib_internal.h"
+
+namespace rtbvh {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kRadius = 14;       // LocallyOrderedClusteringBuilder::search_radius
+constexpr uint32_t kTailNodes = 2048;
+
+struct LocbParams {
+  DAabb* lvl[2];
+  DAabb* final_nodes;
+  uint32_t* nb;
+  uint32_t* blocksum;
+  GridBarrier* bar;
+  uint32_t* status;
+  uint32_t* info;  // [0] levels run
+  uint32_t n;
+};
+
+struct SBox {
+  float mn[3], mx[3];
+};
+
+__device__ __forceinline__ SBox to_sbox(const DAabb& a) {
+  SBox b;
+  b.mn[0] = a.min[0]; b.mn[1] = a.min[1]; b.mn[2] = a.min[2];
+  b.mx[0] = a.max[0]; b.mx[1] = a.max[1]; b.mx[2] = a.max[2];
+  return b;
+}
+
+// half_area(union(a, b)); only the comparison of these values matters, so
+// native min/max are fine here (a -0/+0 difference cannot change an order).
+__device__ __forceinline__ float union_half_area(const SBox& a, const SBox& b) {
+  return half_area(fminf(a.mn[0], b.mn[0]), fminf(a.mn[1], b.mn[1]), fminf(a.mn[2], b.mn[2]),
+                   fmaxf(a.mx[0], b.mx[0]), fmaxf(a.mx[1], b.mx[1]), fmaxf(a.mx[2], b.mx[2]));
+}
+
+// Merge flag of node i (locb.rs:159-167).
+__device__ __forceinline__ uint32_t merge_flag(const uint32_t* nb, uint32_t i) {
+  uint32_t j = __ldcg(nb + i);
+  return (i < j && __ldcg(nb + j) == i) ? 1u : 0u;
+}
+
+// Phase 1 for the tile [t0, t0 + kBlock) of the level [begin, end).
+__device__ void nn_tile(const DAabb* in, uint32_t* nb, uint32_t begin, uint32_t end, uint32_t t0, SBox* s_box,
+                        uint32_t* status) {
+  const int span = kBlock + 2 * kRadius;
+  for (int k = threadIdx.x; k < span; k += kBlock) {
+    int64_t idx = (int64_t)t0 - kRadius + k;
+    if (idx >= (int64_t)begin && idx < (int64_t)end) s_box[k] = to_sbox(load_aabb_cg(in + idx));
+  }
+  __syncthreads();
+  const uint32_t i = t0 + threadIdx.x;
+  if (i < end) {
+    const uint32_t sb = (i > begin + kRadius) ? i - kRadius : begin;
+    const uint32_t se = min(i + kRadius + 1, end);
+    const SBox bi = s_box[i - t0 + kRadius];
+    float best = 3.40282347e+38f;
+    int64_t best_j = -1;
+    for (uint32_t j = sb; j < i; ++j) {
+      float d = union_half_area(s_box[j - t0 + kRadius], bi);
+      if (d < best) { best = d; best_j = j; }
+    }
+    for (uint32_t j = i + 1; j < se; ++j) {
+      float d = union_half_area(bi, s_box[j - t0 + kRadius]);
+      if (d < best) { best = d; best_j = j; }
+    }
+    if (best_j < 0) {
+      atomicOr(status, kStatusNoNeighbour);
+      best_j = i;
+    }
+    nb[i] = (uint32_t)best_j;
+  }
+  __syncthreads();
+}
+
+// Phase 3 for the sub-tile [s0, min(s0 + kBlock, c1)); `carry` is the number
+// of merge flags before s0 in the level. Returns the carry for the next sub-tile.
+__device__ uint32_t scatter_tile(const DAabb* in, DAabb* out, DAabb* final_nodes, const uint32_t* nb, uint32_t begin,
+                                 uint32_t end, uint32_t s0, uint32_t c1, uint32_t carry, uint32_t mc,
+                                 uint32_t* s_flag, uint32_t* s_warp, uint32_t* status) {
+  const uint32_t node_total = 2u * 0u;  // unused marker (kept for symmetry)
+  (void)node_total;
+  for (int k = threadIdx.x; k < kBlock + kRadius; k += kBlock) {
+    uint32_t idx = s0 + k;
+    s_flag[k] = idx < end ? merge_flag(nb, idx) : 0u;
+  }
+  __syncthreads();
+  const uint32_t i = s0 + threadIdx.x;
+  uint32_t f = (i < c1) ? s_flag[threadIdx.x] : 0u;
+  uint32_t tile_total;
+  uint32_t incl = block_inclusive_scan<kBlock>(f, s_warp, &tile_total) + carry;
+  const uint32_t unmerged_begin = begin - mc;
+  const uint32_t children_begin = end - 2u * mc;
+  if (i < c1) {
+    const uint32_t j = __ldcg(nb + i);
+    const uint32_t merged_i = incl;
+    if (__ldcg(nb + j) == i) {
+      if (i < j) {
+        uint32_t merged_j = merged_i;
+        for (uint32_t k = i + 1; k <= j; ++k) merged_j += s_flag[k - s0];
+        const uint32_t pos = unmerged_begin + j - begin - merged_j;
+        const uint32_t fc = children_begin + (merged_i - 1u) * 2u;
+        DAabb a = load_aabb_cg(in + i), b = load_aabb_cg(in + j);
+        DAabb p;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          p.min[ax] = rs_min(b.min[ax], a.min[ax]);
+          p.max[ax] = rs_max(b.max[ax], a.max[ax]);
+        }
+        p.count = -1;
+        p.left_first = (int32_t)fc;
+        if (pos < end && fc + 1 < end) {
+          store_aabb(out + pos, p);
+          store_aabb(final_nodes + fc, a);
+          store_aabb(final_nodes + fc + 1, b);
+        } else {
+          atomicOr(status, kStatusBadIndex);
+        }
+      }
+    } else {
+      const uint32_t pos = unmerged_begin + i - begin - merged_i;
+      if (pos < end) store_aabb(out + pos, load_aabb_cg(in + i));
+      else atomicOr(status, kStatusBadIndex);
+    }
+  }
+  __syncthreads();
+  return carry + tile_total;
+}
+
+__global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
+  __shared__ SBox s_box[kBlock + 2 * kRadius];
+  __shared__ uint32_t s_flag[kBlock + kRadius];
+  __shared__ uint32_t s_warp[kBlock / 32];
+  __shared__ uint32_t s_red[2];
+
+  const uint32_t node_count = 2u * p.n - 1u;
+  uint32_t begin = p.n - 1u, end = node_count;
+  int cur = 0;
+  const uint32_t G = gridDim.x;
+  uint32_t levels = 0;
+
+  // ---------------------------------------------------------------- wide levels
+  while (end - begin > kTailNodes) {
+    const uint32_t m = end - begin;
+    const DAabb* in = p.lvl[cur];
+    DAabb* out = p.lvl[cur ^ 1];
+    for (uint32_t tile = blockIdx.x; (size_t)tile * kBlock < m; tile += G)
+      nn_tile(in, p.nb, begin, end, begin + tile * kBlock, s_box, p.status);
+    if (!grid_sync(p.bar, G, p.status)) return;
+
+    const uint32_t chunk = (m + G - 1) / G;
+    const uint32_t c0 = min(begin + blockIdx.x * chunk, end);
+    const uint32_t c1 = min(c0 + chunk, end);
+    uint32_t local = 0;
+    for (uint32_t i = c0 + threadIdx.x; i < c1; i += kBlock) local += merge_flag(p.nb, i);
+    uint32_t tot;
+    block_inclusive_scan<kBlock>(local, s_warp, &tot);
+    if (threadIdx.x == 0) p.blocksum[blockIdx.x] = tot;
+    if (!grid_sync(p.bar, G, p.status)) return;
+
+    uint32_t pre = 0, all = 0;
+    for (uint32_t b = threadIdx.x; b < G; b += kBlock) {
+      uint32_t v = __ldcg(p.blocksum + b);
+      all += v;
+      if (b < blockIdx.x) pre += v;
+    }
+    uint32_t pre_tot, all_tot;
+    block_inclusive_scan<kBlock>(pre, s_warp, &pre_tot);
+    block_inclusive_scan<kBlock>(all, s_warp, &all_tot);
+    const uint32_t mc = all_tot;
+    if (mc == 0) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(p.status, kStatusNoMerge);
+      return;
+    }
+    uint32_t carry = pre_tot;
+    for (uint32_t s0 = c0; s0 < c1; s0 += kBlock)
+      carry = scatter_tile(in, out, p.final_nodes, p.nb, begin, end, s0, c1, carry, mc, s_flag, s_warp, p.status);
+    if (!grid_sync(p.bar, G, p.status)) return;
+    begin -= mc;
+    end -= 2u * mc;
+    cur ^= 1;
+    ++levels;
+  }
+
+  // ---------------------------------------------------------------- tail (block 0)
+  if (blockIdx.x != 0) return;
+  while (end - begin > 1) {
+    const uint32_t m = end - begin;
+    const DAabb* in = p.lvl[cur];
+    DAabb* out = p.lvl[cur ^ 1];
+    for (uint32_t t0 = begin; t0 < end; t0 += kBlock) nn_tile(in, p.nb, begin, end, t0, s_box, p.status);
+    __threadfence_block();
+    __syncthreads();
+    uint32_t local = 0;
+    for (uint32_t i = begin + threadIdx.x; i < end; i += kBlock) local += merge_flag(p.nb, i);
+    uint32_t mc;
+    block_inclusive_scan<kBlock>(local, s_warp, &mc);
+    if (mc == 0) {
+      if (threadIdx.x == 0) atomicOr(p.status, kStatusNoMerge);
+      return;
+    }
+    uint32_t carry = 0;
+    for (uint32_t s0 = begin; s0 < end; s0 += kBlock)
+      carry = scatter_tile(in, out, p.final_nodes, p.nb, begin, end, s0, end, carry, mc, s_flag, s_warp, p.status);
+    __threadfence_block();
+    __syncthreads();
+    (void)m;
+    begin -= mc;
+    end -= 2u * mc;
+    cur ^= 1;
+    ++levels;
+  }
+  if (threadIdx.x == 0) {
+    store_aabb(p.final_nodes + begin, load_aabb_cg(p.lvl[cur] + begin));
+    p.info[0] = levels;
+    p.info[1] = begin;
+  }
+  (void)s_red;
+}
+
+// Leaves: sorted boxes + 1e-4, count 1, left_first = i (locb.rs:289-294).
+__global__ void __launch_bounds__(kBlock)
+    k_locb_leaves(const DAabb* __restrict__ aabbs, const uint32_t* __restrict__ sorted, uint32_t n,
+                  DAabb* __restrict__ lvl) {
+  uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= n) return;
+  DAabb b = load_aabb(aabbs + __ldg(sorted + i));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    b.min[a] = b.min[a] - 0.0001f;
+    b.max[a] = b.max[a] + 0.0001f;
+  }
+  b.count = 1;
+  b.left_first = (int32_t)i;
+  store_aabb(lvl + (n - 1u) + i, b);
+}
+
+// n <= 2: one root leaf holding the world box (locb.rs:258-269).
+__global__ void k_locb_single(const DAabb* world, uint32_t n, DAabb* nodes, uint32_t* indices) {
+  if (threadIdx.x == 0) {
+    DAabb w = *world;
+    w.count = (int32_t)n;
+    w.left_first = 0;
+    store_aabb(nodes, w);
+  }
+  if (threadIdx.x < n) indices[threadIdx.x] = threadIdx.x;
+}
+
+}  // namespace
+
+ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n_, cudaStream_t s, BuildOutput* out) {
+  if (n_ == 0) return NoPrimitives;
+  if (n_ >= (1u << 30)) return InvalidArgument;
+  const uint32_t n = (uint32_t)n_;
+  const uint32_t node_count = n <= 2 ? 1u : 2u * n - 1u;
+  cudaError_t e;
+  DAabb* nodes = nullptr;
+  uint32_t* indices = nullptr;
+  if ((e = cudaMalloc(&nodes, (size_t)node_count * sizeof(DAabb))) != cudaSuccess) return cuda_rc(e);
+  if ((e = cudaMalloc(&indices, (size_t)n * 4)) != cudaSuccess) {
+    cudaFree(nodes);
+    return cuda_rc(e);
+  }
+  auto fail = [&](ResultCode rc) {
+    cudaFree(nodes);
+    cudaFree(indices);
+    return rc;
+  };
+  Scratch<DAabb> world;
+  Scratch<uint32_t> acc, status;
+  if ((e = world.alloc(1, s)) || (e = acc.alloc(8, s)) || (e = status.alloc(4, s))) return fail(cuda_rc(e));
+  if ((e = cudaMemsetAsync(status.ptr, 0, 16, s))) return fail(cuda_rc(e));
+  if ((e = launch_world_bounds(aabbs, n, world.ptr, acc.ptr, s))) return fail(cuda_rc(e));
+  if (n <= 2) {
+    k_locb_single<<<1, 32, 0, s>>>(world.ptr, n, nodes, indices);
+    if ((e = cudaGetLastError()) || (e = cudaStreamSynchronize(s))) return fail(cuda_rc(e));
+    out->nodes = nodes;
+    out->indices = indices;
+    out->node_count = 1;
+    return Ok;
+  }
+  Scratch<uint32_t> keys;
+  Scratch<char> sort_temp;
+  const size_t sort_bytes = radix_sort_temp_bytes(n);
+  if ((e = keys.alloc(n, s)) || (e = sort_temp.alloc(sort_bytes, s))) return fail(cuda_rc(e));
+  if ((e = launch_morton(centers, n, world.ptr, keys.ptr, indices, s))) return fail(cuda_rc(e));
+  if ((e = radix_sort_pairs(keys.ptr, indices, n, 30, sort_temp.ptr, sort_bytes, status.ptr, s)))
+    return fail(cuda_rc(e));
+
+  Scratch<DAabb> lvl0, lvl1;
+  Scratch<uint32_t> nb, blocksum, info;
+  Scratch<GridBarrier> bar;
+  if ((e = lvl0.alloc(node_count, s)) || (e = lvl1.alloc(node_count, s)) || (e = nb.alloc(node_count, s)) ||
+      (e = info.alloc(4, s)) || (e = bar.alloc(1, s)))
+    return fail(cuda_rc(e));
+  k_locb_leaves<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(aabbs, indices, n, lvl0.ptr);
+  if ((e = cudaGetLastError())) return fail(cuda_rc(e));
+
+  int dev = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_locb_levels, kBlock, 0);
+  if (per_sm < 1) return fail(DeviceError);
+  unsigned grid = (unsigned)(sm_count() * per_sm);
+  const unsigned useful = (unsigned)((n + kBlock - 1) / kBlock);
+  if (grid > useful) grid = useful;
+  if (grid < 1) grid = 1;
+  if ((e = blocksum.alloc(grid, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
+    return fail(cuda_rc(e));
+
+  LocbParams p;
+  p.lvl[0] = lvl0.ptr;
+  p.lvl[1] = lvl1.ptr;
+  p.final_nodes = nodes;
+  p.nb = nb.ptr;
+  p.blocksum = blocksum.ptr;
+  p.bar = bar.ptr;
+  p.status = status.ptr;
+  p.info = info.ptr;
+  p.n = n;
+  void* args[] = {&p};
+  if ((e = cudaLaunchCooperativeKernel((void*)k_locb_levels, dim3(grid), dim3(kBlock), args, 0, s)))
+    return fail(cuda_rc(e));
+  uint32_t h_status = 0;
+  if ((e = cudaMemcpyAsync(&h_status, status.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return fail(cuda_rc(e));
+  if (h_status & kStatusTimeout) return fail(Timeout);
+  if (h_status) return fail(Error);
+  out->nodes = nodes;
+  out->indices = indices;
+  out->node_count = node_count;
+  return Ok;
+}
+
+}  // namespace rtbvh

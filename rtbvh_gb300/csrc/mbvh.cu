@@ -1,0 +1,348 @@
+// BVH2 -> 4-wide MBVH collapse (Mbvh::construct, src/bvh.rs:381-404, and
+// MbvhNode::merge_nodes, src/mbvh_node.rs:297-411) on the GPU.
+//
+// The reference numbers quad nodes by a recursive walk that hands out
+// `pool_ptr++` in slot order (a pre-order over quad nodes). Quad nodes are
+// exactly the interior BVH2 nodes at even depth, and the quad subtree rooted
+// at such a node g holds cntE(g) quad nodes, where
+//   cntE(c) = 1 + cntO(left) + cntO(right),  cntO(c) = cntE(left) + cntE(right)
+// for interior c and 0 for leaves. So:
+//   1. parent pointers;
+//   2. cntE/cntO bottom-up (the second child to arrive at a parent computes it);
+//   3. top-down, one quad level per step of a cooperative launch: a quad node
+//      with index mi gives its k-th interior slot the index
+//      mi + 1 + sum of cntE over the interior slots before it.
+// The slot contents reproduce merge_nodes line by line, including its quirks
+// (a leaf child keeps the parent's box in its slot; the second slot of that
+// side stays empty with the parent's box).
+#include "lib_internal.h"
+
+namespace rtbvh {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kNone = 0xffffffffu;
+
+__global__ void __launch_bounds__(kBlock)
+    k_parents(const DAabb* __restrict__ nodes, uint32_t node_count, uint32_t* __restrict__ parent,
+              uint32_t* __restrict__ arrive, uint32_t* __restrict__ status) {
+  uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  arrive[c] = 0;
+  DAabb nd = load_aabb(nodes + c);
+  if (nd.count < 0 && nd.left_first >= 0) {
+    uint32_t lf = (uint32_t)nd.left_first;
+    if (lf + 1 < node_count) {
+      parent[lf] = c;
+      parent[lf + 1] = c;
+    } else {
+      atomicOr(status, kStatusBadIndex);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock)
+    k_counts_bottom_up(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ parent,
+                       uint32_t* __restrict__ arrive, uint32_t* __restrict__ cnt_e, uint32_t* __restrict__ cnt_o) {
+  uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  DAabb nd = load_aabb(nodes + c);
+  if (nd.count < 0) return;  // walks start at leaves
+  cnt_e[c] = 0;
+  cnt_o[c] = 0;
+  __threadfence();
+  uint32_t x = c;
+  for (uint32_t steps = 0; steps < node_count; ++steps) {
+    uint32_t p = __ldcg(parent + x);
+    if (p == kNone) break;
+    if (atomicAdd(arrive + p, 1u) == 0u) break;  // first arrival: the sibling finishes p
+    __threadfence();
+    uint32_t lf = (uint32_t)load_aabb(nodes + p).left_first;
+    uint32_t e = 1u + __ldcg(cnt_o + lf) + __ldcg(cnt_o + lf + 1);
+    uint32_t o = __ldcg(cnt_e + lf) + __ldcg(cnt_e + lf + 1);
+    cnt_e[p] = e;
+    cnt_o[p] = o;
+    __threadfence();
+    x = p;
+  }
+}
+
+struct CollapseParams {
+  const DAabb* nodes;
+  uint32_t node_count;
+  const uint32_t* cnt_e;
+  DMNode* mnodes;
+  uint32_t m_total;
+  uint2* queue[2];
+  uint32_t* qcount;  // 3 rotating counters
+  GridBarrier* bar;
+  uint32_t* status;
+};
+
+__device__ __forceinline__ void set_slot_box(DMNode& m, int i, const DAabb& b) {
+  m.min_x[i] = b.min[0]; m.min_y[i] = b.min[1]; m.min_z[i] = b.min[2];
+  m.max_x[i] = b.max[0]; m.max_y[i] = b.max[1]; m.max_z[i] = b.max[2];
+}
+
+// merge_nodes(mi, c) without the recursion: fills quad node mi and appends
+// its interior slots (bvh node, quad index) to `next`.
+__device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint2* next, uint32_t* next_count) {
+  const DAabb cur = load_aabb(p.nodes + c);
+  DMNode m;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    set_slot_box(m, i, cur);
+    m.children[i] = -1;
+    m.counts[i] = -1;
+  }
+  int32_t nodes_[4] = {-1, -1, -1, -1};
+  int32_t leafs[4] = {-1, -1, -1, -1};
+  if (cur.left_first >= 0) {
+    const uint32_t lf = (uint32_t)cur.left_first;
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int s0 = 2 * side;
+      const uint32_t child = lf + side;
+      if (child < p.node_count) {
+        const DAabb cn = load_aabb(p.nodes + child);
+        if (cn.left_first >= 0) {
+          const uint32_t clf = (uint32_t)cn.left_first;
+          if (cn.count >= 0) {
+            nodes_[s0] = (int32_t)clf;
+            leafs[s0] = cn.count;
+          } else if (clf + 1 < p.node_count) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              const DAabb g = load_aabb(p.nodes + clf + k);
+              if (g.count >= 0) {
+                nodes_[s0 + k] = g.left_first;
+                leafs[s0 + k] = g.count;
+              } else {
+                nodes_[s0 + k] = (int32_t)(clf + k);
+              }
+              set_slot_box(m, s0 + k, g);
+            }
+          } else {
+            atomicOr(p.status, kStatusBadIndex);
+          }
+        }
+      }
+    }
+  }
+  uint32_t next_index = mi + 1u;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int32_t node = nodes_[i];
+    const int32_t count = leafs[i];
+    if (node >= 0 && count >= 0) {
+      m.children[i] = node;
+      m.counts[i] = count;
+      continue;
+    } else if (node == -1) {
+      continue;
+    }
+    const uint32_t g = (uint32_t)node;
+    const uint32_t idx = next_index;
+    next_index += __ldg(p.cnt_e + g);
+    if (idx < p.m_total) {
+      m.children[i] = (int32_t)idx;
+      uint32_t slot = atomicAdd(next_count, 1u);
+      if (slot < p.m_total) next[slot] = make_uint2(g, idx);
+      else atomicOr(p.status, kStatusBadIndex);
+    } else {
+      atomicOr(p.status, kStatusBadIndex);
+    }
+  }
+  if (mi < p.m_total) {
+    float4* dst = reinterpret_cast<float4*>(p.mnodes + mi);
+    const float4* src = reinterpret_cast<const float4*>(&m);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dst[k] = src[k];
+  } else {
+    atomicOr(p.status, kStatusBadIndex);
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_collapse(CollapseParams p) {
+  const uint32_t G = gridDim.x;
+  const uint32_t tid = blockIdx.x * kBlock + threadIdx.x, nthreads = G * kBlock;
+  for (uint32_t level = 0; level < p.m_total + 1; ++level) {
+    uint32_t size = __ldcg(p.qcount + (level % 3));
+    if (size == 0) break;
+    if (size > p.m_total) size = p.m_total;  // only after a kStatusBadIndex
+    const uint2* q = p.queue[level & 1];
+    uint2* next = p.queue[(level + 1) & 1];
+    uint32_t* next_count = p.qcount + ((level + 1) % 3);
+    for (uint32_t k = tid; k < size; k += nthreads) {
+      uint2 item = __ldcg(q + k);
+      emit_quad(p, item.x, item.y, next, next_count);
+    }
+    if (tid == 0) p.qcount[(level + 2) % 3] = 0;
+    if (!grid_sync(p.bar, G, p.status)) return;
+  }
+}
+
+__global__ void k_collapse_init(const uint32_t* cnt_e, const DAabb* nodes, uint2* queue0, uint32_t* qcount,
+                                uint32_t* m_total_out) {
+  if (threadIdx.x == 0) {
+    queue0[0] = make_uint2(0u, 0u);
+    qcount[0] = 1;
+    qcount[1] = 0;
+    qcount[2] = 0;
+    DAabb r = *nodes;
+    uint32_t t = r.count < 0 ? cnt_e[0] : 1u;
+    *m_total_out = t;
+  }
+}
+
+// Bvh::refit (src/bvh.rs:176-205): leaf box = union of its primitives'
+// boxes + 1e-4, interior box = union of the two children + 1e-4, computed
+// bottom-up (the second child to arrive finishes the parent). Unions are
+// exact, so the boxes equal the reference's reverse-order loop bit for bit.
+// Unlike the reference, count/left_first are kept (see include/rtbvh.h).
+__global__ void __launch_bounds__(kBlock)
+    k_refit(DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices, uint32_t prim_count,
+            const DAabb* __restrict__ aabbs, const uint32_t* __restrict__ parent, uint32_t* __restrict__ arrive,
+            uint32_t* __restrict__ status) {
+  uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  DAabb nd = load_aabb_cg(nodes + c);
+  if (nd.count < 0 && nd.left_first >= 0) return;  // interior: finished by a child walk
+  DAabb box = nd;
+  for (int a = 0; a < 3; ++a) { box.min[a] = 1e34f; box.max[a] = -1e34f; }
+  if (nd.left_first >= 0) {
+    for (int32_t i = 0; i < nd.count; ++i) {
+      uint32_t slot = (uint32_t)nd.left_first + (uint32_t)i;
+      if (slot >= prim_count) { atomicOr(status, kStatusBadIndex); break; }
+      uint32_t p = __ldg(indices + slot);
+      if (p >= prim_count) { atomicOr(status, kStatusBadIndex); break; }
+      DAabb b = load_aabb(aabbs + p);
+      for (int a = 0; a < 3; ++a) { box.min[a] = rs_min(box.min[a], b.min[a]); box.max[a] = rs_max(box.max[a], b.max[a]); }
+    }
+    for (int a = 0; a < 3; ++a) { box.min[a] = box.min[a] - 0.0001f; box.max[a] = box.max[a] + 0.0001f; }
+  }
+  store_aabb(nodes + c, box);
+  if (nd.left_first < 0) return;
+  __threadfence();
+  uint32_t x = c;
+  for (uint32_t steps = 0; steps < node_count; ++steps) {
+    uint32_t p = __ldcg(parent + x);
+    if (p == kNone) break;
+    if (atomicAdd(arrive + p, 1u) == 0u) break;
+    __threadfence();
+    DAabb pn = load_aabb_cg(nodes + p);
+    const uint32_t lf = (uint32_t)pn.left_first;
+    DAabb l = load_aabb_cg(nodes + lf), r = load_aabb_cg(nodes + lf + 1);
+    for (int a = 0; a < 3; ++a) {
+      float mn = rs_min(rs_min(1e34f, l.min[a]), r.min[a]);
+      float mx = rs_max(rs_max(-1e34f, l.max[a]), r.max[a]);
+      pn.min[a] = mn - 0.0001f;
+      pn.max[a] = mx + 0.0001f;
+    }
+    store_aabb(nodes + p, pn);
+    __threadfence();
+    x = p;
+  }
+}
+
+}  // namespace
+
+ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes_out,
+                      uint32_t* mnode_count) {
+  *mnodes_out = nullptr;
+  *mnode_count = 0;
+  if (node_count == 0) return Ok;  // Mbvh::default()
+  cudaError_t e;
+  Scratch<uint32_t> parent, arrive, cnt_e, cnt_o, status, mtot;
+  if ((e = parent.alloc(node_count, s)) || (e = arrive.alloc(node_count, s)) || (e = cnt_e.alloc(node_count, s)) ||
+      (e = cnt_o.alloc(node_count, s)) || (e = status.alloc(4, s)) || (e = mtot.alloc(4, s)))
+    return cuda_rc(e);
+  if ((e = cudaMemsetAsync(parent.ptr, 0xff, (size_t)node_count * 4, s)) ||
+      (e = cudaMemsetAsync(status.ptr, 0, 16, s)))
+    return cuda_rc(e);
+  const unsigned blocks = (node_count + kBlock - 1) / kBlock;
+  k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, status.ptr);
+  k_counts_bottom_up<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, cnt_e.ptr, cnt_o.ptr);
+  Scratch<uint2> q0, q1;
+  Scratch<uint32_t> qcount;
+  Scratch<GridBarrier> bar;
+  if ((e = qcount.alloc(4, s)) || (e = bar.alloc(1, s))) return cuda_rc(e);
+  if ((e = q0.alloc(node_count, s)) || (e = q1.alloc(node_count, s))) return cuda_rc(e);
+  k_collapse_init<<<1, 32, 0, s>>>(cnt_e.ptr, nodes, q0.ptr, qcount.ptr, mtot.ptr);
+  uint32_t h[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(h, mtot.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+    return cuda_rc(e);
+  if (h[1] != 0) return Error;
+  const uint32_t m_total = h[0];
+  if (m_total == 0 || m_total > node_count) return Error;
+  DMNode* mnodes = nullptr;
+  if ((e = cudaMalloc(&mnodes, (size_t)m_total * sizeof(DMNode)))) return cuda_rc(e);
+  if ((e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s))) {
+    cudaFree(mnodes);
+    return cuda_rc(e);
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  unsigned grid = (unsigned)(sm_count() * per_sm);
+  const unsigned useful = (m_total + kBlock - 1) / kBlock;
+  if (grid > useful) grid = useful;
+  if (grid < 1) grid = 1;
+  CollapseParams p;
+  p.nodes = nodes;
+  p.node_count = node_count;
+  p.cnt_e = cnt_e.ptr;
+  p.mnodes = mnodes;
+  p.m_total = m_total;
+  p.queue[0] = q0.ptr;
+  p.queue[1] = q1.ptr;
+  p.qcount = qcount.ptr;
+  p.bar = bar.ptr;
+  p.status = status.ptr;
+  void* args[] = {&p};
+  if ((e = cudaLaunchCooperativeKernel((void*)k_collapse, dim3(grid), dim3(kBlock), args, 0, s))) {
+    cudaFree(mnodes);
+    return cuda_rc(e);
+  }
+  uint32_t st = 0;
+  if ((e = cudaMemcpyAsync(&st, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
+    cudaFree(mnodes);
+    return cuda_rc(e);
+  }
+  if (st != 0) {
+    cudaFree(mnodes);
+    return (st & kStatusTimeout) ? Timeout : Error;
+  }
+  *mnodes_out = mnodes;
+  *mnode_count = m_total;
+  return Ok;
+}
+
+}  // namespace rtbvh
+
+namespace rtbvh {
+
+ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
+                     const DAabb* aabbs, cudaStream_t s) {
+  if (node_count == 0) return Ok;
+  cudaError_t e;
+  Scratch<uint32_t> parent, arrive, status;
+  if ((e = parent.alloc(node_count, s)) || (e = arrive.alloc(node_count, s)) || (e = status.alloc(4, s)))
+    return cuda_rc(e);
+  if ((e = cudaMemsetAsync(parent.ptr, 0xff, (size_t)node_count * 4, s)) ||
+      (e = cudaMemsetAsync(status.ptr, 0, 16, s)))
+    return cuda_rc(e);
+  const unsigned blocks = (node_count + kBlock - 1) / kBlock;
+  k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, status.ptr);
+  k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, prim_count, aabbs, parent.ptr, arrive.ptr,
+                                    status.ptr);
+  uint32_t st = 0;
+  if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&st, status.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return cuda_rc(e);
+  return st ? Error : Ok;
+}
+
+}  // namespace rtbvh

@@ -1,0 +1,325 @@
+// Single-ray traversal with the fused triangle test, one ray per thread.
+//
+// trace_mbvh follows MbvhIndexIterator::next (src/iter_indices.rs:264-313)
+// step for step: the quad node's hit mask and slot order come from the
+// 4-wide slab test (src/mbvh_node.rs:176-240) evaluated with the ray's
+// current t when the node is entered; slots are visited far to near
+// (ids[3..0]); a leaf slot's primitives are tested at once, an interior slot
+// is pushed. The triangle test is SpatialTriangle::intersect
+// (src/builders/spatial_sah.rs:132-163). With the same arithmetic (no FMA,
+// IEEE division, SSE min/max rules) the hits, their order of discovery and
+// the node/triangle counts equal the reference's.
+//
+// trace_bvh follows BvhIndexIterator::next (src/iter_indices.rs:66-107) with
+// the sign-indexed slab test (src/aabb.rs:145-181) and sort_nodes
+// (src/bvh_node.rs:150-177).
+//
+// Kernels are persistent: each warp takes 32 rays at a time from an atomic
+// counter. The stack lives in local memory with a hard bound; a ray that
+// would exceed it stops, reports prim -2 and sets kStatusStackOverflow.
+#include "lib_internal.h"
+
+namespace rtbvh {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kStack = 64;
+
+struct RayState {
+  float ox, oy, oz, dx, dy, dz, ix, iy, iz;
+  float t;
+  int32_t sx, sy, sz;
+};
+
+__device__ __forceinline__ RayState load_ray(const float* rays, size_t r, const float* t_max) {
+  const float2* p = reinterpret_cast<const float2*>(rays + 6 * r);
+  float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  RayState s;
+  s.ox = a.x; s.oy = a.y; s.oz = b.x;
+  s.dx = b.y; s.dy = c.x; s.dz = c.y;
+  s.ix = 1.0f / s.dx; s.iy = 1.0f / s.dy; s.iz = 1.0f / s.dz;
+  s.sx = s.dx < 0.0f; s.sy = s.dy < 0.0f; s.sz = s.dz < 0.0f;
+  s.t = t_max ? __ldg(t_max + r) : 1e34f;
+  return s;
+}
+
+// SpatialTriangle::intersect with a leaf-ordered triangle {v0,prim},{e1},{e2}.
+__device__ __forceinline__ bool mt_test(const float4* tri, RayState& r, float& hu, float& hv, int32_t& prim) {
+  const float4 a = __ldg(tri), b = __ldg(tri + 1), c = __ldg(tri + 2);
+  const float e1x = b.x, e1y = b.y, e1z = b.z;
+  const float e2x = c.x, e2y = c.y, e2z = c.z;
+  // h = d x e2
+  const float hx = r.dy * e2z - e2y * r.dz;
+  const float hy = r.dz * e2x - e2z * r.dx;
+  const float hz = r.dx * e2y - e2x * r.dy;
+  const float det = ((e1x * hx) + (e1y * hy)) + (e1z * hz);
+  if (det > -1e-5f && det < 1e-5f) return false;
+  const float f = 1.0f / det;
+  const float sx = r.ox - a.x, sy = r.oy - a.y, sz = r.oz - a.z;
+  const float u = f * (((sx * hx) + (sy * hy)) + (sz * hz));
+  if (!(u >= 0.0f && u <= 1.0f)) return false;
+  // q = s x e1
+  const float qx = sy * e1z - e1y * sz;
+  const float qy = sz * e1x - e1z * sx;
+  const float qz = sx * e1y - e1x * sy;
+  const float v = f * (((r.dx * qx) + (r.dy * qy)) + (r.dz * qz));
+  if (v < 0.0f || (u + v) > 1.0f) return false;
+  const float t = f * (((e2x * qx) + (e2y * qy)) + (e2z * qz));
+  if (t > 1e-4f && t < r.t) {
+    r.t = t;
+    hu = u;
+    hv = v;
+    prim = __float_as_int(a.w);
+    return true;
+  }
+  return false;
+}
+
+// MbvhNode::intersect: mask bit i set when slot i is hit; ids packed as
+// 2-bit fields, ascending by t_min after the 5-compare network.
+__device__ __forceinline__ void quad_intersect(const DMNode* node, const RayState& r, uint32_t& mask, uint32_t& ids,
+                                               int4& children, int4& counts) {
+  const float4* q = reinterpret_cast<const float4*>(node);
+  const float4 mnx = __ldg(q + 0), mxx = __ldg(q + 1), mny = __ldg(q + 2), mxy = __ldg(q + 3);
+  const float4 mnz = __ldg(q + 4), mxz = __ldg(q + 5);
+  const float4 ch = __ldg(q + 6), ct = __ldg(q + 7);
+  children = make_int4(__float_as_int(ch.x), __float_as_int(ch.y), __float_as_int(ch.z), __float_as_int(ch.w));
+  counts = make_int4(__float_as_int(ct.x), __float_as_int(ct.y), __float_as_int(ct.z), __float_as_int(ct.w));
+  float tmin[4];
+  uint32_t m = 0;
+  const float a_mnx[4] = {mnx.x, mnx.y, mnx.z, mnx.w}, a_mxx[4] = {mxx.x, mxx.y, mxx.z, mxx.w};
+  const float a_mny[4] = {mny.x, mny.y, mny.z, mny.w}, a_mxy[4] = {mxy.x, mxy.y, mxy.z, mxy.w};
+  const float a_mnz[4] = {mnz.x, mnz.y, mnz.z, mnz.w}, a_mxz[4] = {mxz.x, mxz.y, mxz.z, mxz.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float tx0 = (a_mnx[i] - r.ox) * r.ix, tx1 = (a_mxx[i] - r.ox) * r.ix;
+    const float ty0 = (a_mny[i] - r.oy) * r.iy, ty1 = (a_mxy[i] - r.oy) * r.iy;
+    const float tz0 = (a_mnz[i] - r.oz) * r.iz, tz1 = (a_mxz[i] - r.oz) * r.iz;
+    const float txn = sse_min(tx0, tx1), txx = sse_max(tx0, tx1);
+    const float tyn = sse_min(ty0, ty1), tyx = sse_max(ty0, ty1);
+    const float tzn = sse_min(tz0, tz1), tzx = sse_max(tz0, tz1);
+    const float tn = sse_max(txn, sse_max(tyn, tzn));
+    const float tx = sse_min(txx, sse_min(tyx, tzx));
+    tmin[i] = tn;
+    if ((tx >= tn) && (tn < r.t)) m |= 1u << i;
+  }
+  uint32_t i0 = 0, i1 = 1, i2 = 2, i3 = 3;
+  float t0 = tmin[0], t1 = tmin[1], t2 = tmin[2], t3 = tmin[3], tt;
+  uint32_t ti;
+  if (t0 > t1) { tt = t0; t0 = t1; t1 = tt; ti = i0; i0 = i1; i1 = ti; }
+  if (t2 > t3) { tt = t2; t2 = t3; t3 = tt; ti = i2; i2 = i3; i3 = ti; }
+  if (t0 > t2) { tt = t0; t0 = t2; t2 = tt; ti = i0; i0 = i2; i2 = ti; }
+  if (t1 > t3) { tt = t1; t1 = t3; t3 = tt; ti = i1; i1 = i3; i3 = ti; }
+  if (t2 > t3) { ti = i2; i2 = i3; i3 = ti; }
+  mask = m;
+  ids = i0 | (i1 << 2) | (i2 << 4) | (i3 << 6);
+}
+
+__device__ __forceinline__ int sel4(const int4& v, uint32_t i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+template <bool ANY_HIT, bool STATS>
+__device__ __forceinline__ void trace_one_mbvh(const TraceArgs& a, size_t r) {
+  RayState ray = load_ray(a.rays, r, a.t_max);
+  float hu = 0.0f, hv = 0.0f;
+  int32_t prim = -1;
+  uint32_t visits = 0, tests = 0, max_depth = 0;
+  int32_t stack[kStack];
+  int sp = -1;
+  uint32_t mask, ids;
+  int4 children, counts;
+  int32_t current = 0;
+  bool done = (a.node_count == 0);
+  if (!done) {
+    quad_intersect(a.mnodes, ray, mask, ids, children, counts);
+    if (STATS) ++visits;
+  }
+  while (!done) {
+#pragma unroll 1
+    for (int i = 0; i < 4 && !done; ++i) {
+      const uint32_t id = (ids >> (2 * (3 - i))) & 3u;
+      if (!((mask >> id) & 1u)) continue;
+      const int32_t count = sel4(counts, id);
+      const int32_t lf = sel4(children, id);
+      if (count > -1) {
+        if ((uint32_t)lf + (uint32_t)count > a.prim_count || lf < 0) {
+          atomicOr(a.status, kStatusBadIndex);
+          done = true;
+          break;
+        }
+        for (int32_t j = 0; j < count; ++j) {
+          if (STATS) ++tests;
+          if (mt_test(a.tris + 3 * (size_t)(lf + j), ray, hu, hv, prim) && ANY_HIT) {
+            done = true;
+            break;
+          }
+        }
+      } else if (lf > -1) {
+        if (sp + 1 >= kStack) {
+          atomicOr(a.status, kStatusStackOverflow);
+          prim = -2;
+          done = true;
+          break;
+        }
+        stack[++sp] = lf;
+        if (STATS && (uint32_t)(sp + 1) > max_depth) max_depth = (uint32_t)(sp + 1);
+      }
+    }
+    if (done) break;
+    if (sp < 0) break;
+    current = stack[sp--];
+    if ((uint32_t)current >= a.node_count) {
+      atomicOr(a.status, kStatusBadIndex);
+      break;
+    }
+    quad_intersect(a.mnodes + current, ray, mask, ids, children, counts);
+    if (STATS) ++visits;
+  }
+  a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
+  if (STATS) {
+    a.stats[3 * r + 0] = visits;
+    a.stats[3 * r + 1] = tests;
+    a.stats[3 * r + 2] = max_depth;
+  }
+}
+
+// Aabb::intersect (src/aabb.rs:145-181): far t or miss; t_min fixed at 1e-4.
+__device__ __forceinline__ bool slab_far(const DAabb& b, const RayState& r, float& out) {
+  float ray_min = ((r.sx ? b.max[0] : b.min[0]) - r.ox) * r.ix;
+  float ray_max = ((r.sx ? b.min[0] : b.max[0]) - r.ox) * r.ix;
+  const float y_min = ((r.sy ? b.max[1] : b.min[1]) - r.oy) * r.iy;
+  const float y_max = ((r.sy ? b.min[1] : b.max[1]) - r.oy) * r.iy;
+  if ((ray_min > y_max) || (y_min > ray_max)) return false;
+  if (y_min > ray_min) ray_min = y_min;
+  if (y_max < ray_max) ray_max = y_max;
+  const float z_min = ((r.sz ? b.max[2] : b.min[2]) - r.oz) * r.iz;
+  const float z_max = ((r.sz ? b.min[2] : b.max[2]) - r.oz) * r.iz;
+  if ((ray_min > z_max) || (z_min > ray_max)) return false;
+  if (z_max < ray_max) ray_max = z_max;
+  if (ray_max > 1e-4f) {
+    out = ray_max;
+    return true;
+  }
+  return false;
+}
+
+template <bool ANY_HIT, bool STATS>
+__device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
+  RayState ray = load_ray(a.rays, r, a.t_max);
+  float hu = 0.0f, hv = 0.0f;
+  int32_t prim = -1;
+  uint32_t visits = 0, tests = 0, max_depth = 0;
+  const bool nan = (ray.ox != ray.ox) || (ray.oy != ray.oy) || (ray.oz != ray.oz) || (ray.dx != ray.dx) ||
+                   (ray.dy != ray.dy) || (ray.dz != ray.dz);
+  int32_t stack[kStack];
+  int sp = (a.node_count == 0 || nan) ? -1 : 0;
+  stack[0] = 0;
+  while (sp >= 0) {
+    const int32_t ni = stack[sp--];
+    if ((uint32_t)ni >= a.node_count) {
+      atomicOr(a.status, kStatusBadIndex);
+      break;
+    }
+    const DAabb node = load_aabb(a.nodes + ni);
+    if (node.count > -1) {
+      if (node.left_first < 0 || (uint32_t)node.left_first + (uint32_t)node.count > a.prim_count) {
+        atomicOr(a.status, kStatusBadIndex);
+        break;
+      }
+      bool stop = false;
+      for (int32_t j = 0; j < node.count; ++j) {
+        if (STATS) ++tests;
+        if (mt_test(a.tris + 3 * (size_t)(node.left_first + j), ray, hu, hv, prim) && ANY_HIT) {
+          stop = true;
+          break;
+        }
+      }
+      if (stop) break;
+    } else if (node.left_first > -1) {
+      if (STATS) ++visits;
+      const int32_t lf = node.left_first;
+      if ((uint32_t)lf + 1u >= a.node_count) {
+        atomicOr(a.status, kStatusBadIndex);
+        break;
+      }
+      float lt = 0.0f, rt = 0.0f;
+      const bool lh = slab_far(load_aabb(a.nodes + lf), ray, lt);
+      const bool rh = slab_far(load_aabb(a.nodes + lf + 1), ray, rt);
+      if (sp + 2 >= kStack) {
+        atomicOr(a.status, kStatusStackOverflow);
+        prim = -2;
+        break;
+      }
+      if (lh && rh) {
+        if (lt < rt) { stack[++sp] = lf; stack[++sp] = lf + 1; }
+        else { stack[++sp] = lf + 1; stack[++sp] = lf; }
+      } else if (lh) {
+        stack[++sp] = lf;
+      } else if (rh) {
+        stack[++sp] = lf + 1;
+      }
+      if (STATS && (uint32_t)(sp + 1) > max_depth) max_depth = (uint32_t)(sp + 1);
+    }
+  }
+  a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
+  if (STATS) {
+    a.stats[3 * r + 0] = visits;
+    a.stats[3 * r + 1] = tests;
+    a.stats[3 * r + 2] = max_depth;
+  }
+}
+
+template <bool MBVH, bool ANY_HIT, bool STATS>
+__global__ void __launch_bounds__(kBlock) k_trace(TraceArgs a, unsigned int* work) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned int base = 0;
+    if (lane == 0) base = atomicAdd(work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((size_t)base >= a.ray_count) break;
+    const size_t r = (size_t)base + lane;
+    if (r < a.ray_count) {
+      if (MBVH) trace_one_mbvh<ANY_HIT, STATS>(a, r);
+      else trace_one_bvh<ANY_HIT, STATS>(a, r);
+    }
+  }
+}
+
+template <bool MBVH, bool ANY_HIT, bool STATS>
+cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<MBVH, ANY_HIT, STATS>, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  size_t grid = (size_t)sm_count() * per_sm;
+  const size_t need = (a.ray_count + kBlock - 1) / kBlock;
+  if (grid > need) grid = need;
+  k_trace<MBVH, ANY_HIT, STATS><<<(unsigned)grid, kBlock, 0, s>>>(a, work);
+  return cudaGetLastError();
+}
+
+template <bool MBVH>
+cudaError_t launch_any(const TraceArgs& a, cudaStream_t s) {
+  if (a.ray_count == 0) return cudaSuccess;
+  if (a.ray_count > 0xffffffffull - 64) return cudaErrorInvalidValue;
+  unsigned int* work = nullptr;
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&work), sizeof(unsigned int), s);
+  if (e) return e;
+  if ((e = cudaMemsetAsync(work, 0, sizeof(unsigned int), s))) {
+    cudaFreeAsync(work, s);
+    return e;
+  }
+  const bool st = a.stats != nullptr;
+  if (a.any_hit) e = st ? launch3<MBVH, true, true>(a, s, work) : launch3<MBVH, true, false>(a, s, work);
+  else e = st ? launch3<MBVH, false, true>(a, s, work) : launch3<MBVH, false, false>(a, s, work);
+  cudaFreeAsync(work, s);
+  return e;
+}
+
+}  // namespace
+
+cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s) { return launch_any<true>(a, s); }
+cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s) { return launch_any<false>(a, s); }
+
+}  // namespace rtbvh

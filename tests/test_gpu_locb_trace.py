@@ -1,0 +1,208 @@
+"""GPU parity: locally-ordered clustering, MBVH collapse and traversal
+against the oracle, bit for bit (integer results exactly; float results by
+their bit patterns, since the arithmetic is the same IEEE single sequence)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import rtbvh_gb300 as rb
+from rtbvh_gb300 import _ffi, scenes
+from gpu_helpers import gpu_build, oracle_build, rays_for, scene, to_cuda, u32
+
+pytestmark = pytest.mark.gpu
+
+SCENES = ["teapot", "sphere", "incoherent_20k", "incoherent_300k"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device(lib):
+    torch.cuda.set_device(0)
+    yield
+    torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_locb_nodes_bit_exact(name):
+    tris = scene(name)
+    g = gpu_build(tris, "locb")
+    on, oi = oracle_build(tris, "locb")
+    assert np.array_equal(g.indices(), oi), "Morton order differs"
+    assert np.array_equal(u32(g.nodes()), u32(on)), "node arrays differ"
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 16, 17, 31, 100, 257, 2047, 2048, 2049, 4097, 9000])
+def test_locb_sizes(n):
+    tris = scenes.incoherent(n, seed=100 + n)
+    g = gpu_build(tris, "locb")
+    on, oi = oracle_build(tris, "locb")
+    assert np.array_equal(g.indices(), oi)
+    assert np.array_equal(u32(g.nodes()), u32(on))
+
+
+def test_locb_identical_primitives():
+    # every box and centre equal: all distances tie, the lowest index wins
+    t = np.tile(np.asarray([[[0.1, 0.2, 0.3], [0.4, 0.2, 0.3], [0.1, 0.6, 0.3]]], np.float32), (777, 1, 1))
+    g = gpu_build(t, "locb")
+    on, oi = oracle_build(t, "locb")
+    assert np.array_equal(g.indices(), oi)
+    assert np.array_equal(u32(g.nodes()), u32(on))
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_mbvh_bit_exact(name):
+    tris = scene(name)
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    on, oi = oracle_build(tris, "locb")
+    om = oracle.mbvh(on)
+    assert np.array_equal(u32(m.quad_nodes()), u32(om))
+    assert np.array_equal(m.indices(), oi)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_trace_closest_bit_exact(name):
+    tris = scene(name)
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    rays, _ = rays_for(name)
+    hits, st = m.intersect(to_cuda(rays), stats=True)
+    assert m.status() == rb.ResultCode.Ok
+    hits, st = hits.cpu().numpy(), st.cpu().numpy().view(np.uint32)
+    on, oi = oracle_build(tris, "locb")
+    om = oracle.mbvh(on)
+    oh, ost, bad = oracle.trace("mbvh", om, oi, tris.reshape(-1, 9), rays)
+    assert bad == 0
+    assert np.array_equal(u32(hits), u32(oh)), "t/u/v/prim differ"
+    assert np.array_equal(st, ost), "node-visit / triangle-test / stack counts differ"
+    assert (rb.hit_prims(hits) >= 0).sum() > 0
+
+
+@pytest.mark.parametrize("name", ["teapot", "incoherent_300k"])
+def test_trace_any_hit_bit_exact(name):
+    tris = scene(name)
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    rays, tmax = rays_for(name)
+    if tmax is None:
+        tmax = np.full(len(rays), 9.0, np.float32)
+    hits, st = m.intersect(to_cuda(rays), t_max=to_cuda(tmax), any_hit=True, stats=True)
+    hits, st = hits.cpu().numpy(), st.cpu().numpy().view(np.uint32)
+    on, oi = oracle_build(tris, "locb")
+    oh, ost, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, t_max=tmax, any_hit=True)
+    assert np.array_equal(u32(hits), u32(oh))
+    assert np.array_equal(st, ost)
+
+
+@pytest.mark.parametrize("name", ["teapot", "incoherent_20k"])
+def test_trace_bvh2_bit_exact(name):
+    tris = scene(name)
+    g = gpu_build(tris, "locb")
+    rays, _ = rays_for(name)
+    hits, st = g.intersect(to_cuda(rays), stats=True)
+    hits, st = hits.cpu().numpy(), st.cpu().numpy().view(np.uint32)
+    on, oi = oracle_build(tris, "locb")
+    oh, ost, _ = oracle.trace("bvh", on, oi, tris.reshape(-1, 9), rays)
+    assert np.array_equal(u32(hits), u32(oh))
+    assert np.array_equal(st, ost)
+
+
+def test_host_buffer_entry_matches_device_entry():
+    tris = scene("incoherent_20k")
+    m = rb.Mbvh.construct(gpu_build(tris, "locb"))
+    rays, tmax = scenes.incoherent_rays(3_000_000, seed=9)  # more than one internal chunk
+    dev, _ = m.intersect(to_cuda(rays))
+    host = m.intersect_host(rays)
+    assert np.array_equal(u32(host), u32(dev.cpu().numpy()))
+    dev_a, _ = m.intersect(to_cuda(rays), t_max=to_cuda(tmax), any_hit=True)
+    host_a = m.intersect_host(rays, t_max=tmax, any_hit=True)
+    assert np.array_equal(u32(host_a), u32(dev_a.cpu().numpy()))
+
+
+def test_legacy_c_abi_roundtrip(lib):
+    # create_bvh / create_mbvh / intersect_mbvh / free_* with host inputs,
+    # as a C caller of the reference uses them
+    tris = scene("teapot")
+    a, c = oracle.triangle_prep(tris)
+    c4 = np.zeros((len(c), 4), np.float32)
+    c4[:, :3] = c
+    out = _ffi.RTBvh()
+    for stride, cc in ((12, c), (16, c4)):
+        cc = np.ascontiguousarray(cc)
+        rc = lib.create_bvh(a.ctypes.data_as(ctypes.POINTER(_ffi.RTAabb)), len(a),
+                            cc.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), stride, 1, 0, ctypes.byref(out))
+        assert rc == 0
+        on, oi = oracle.build(a, c, "locb")
+        assert out.node_count == len(on) and out.index_count == len(oi)
+        nodes = np.ctypeslib.as_array(ctypes.cast(out.nodes, ctypes.POINTER(ctypes.c_float)), (out.node_count * 8,))
+        assert np.array_equal(u32(nodes.reshape(-1, 8)), u32(on))
+        mo = _ffi.RTMbvh()
+        assert lib.create_mbvh(out, ctypes.byref(mo)) == 0
+        mn = np.ctypeslib.as_array(ctypes.cast(mo.nodes, ctypes.POINTER(ctypes.c_float)), (mo.node_count * 32,))
+        assert np.array_equal(u32(mn.reshape(-1, 32)), u32(oracle.mbvh(on)))
+        lib.free_mbvh(mo)
+        lib.free_bvh(out)
+
+
+def test_legacy_create_bvh_without_aabbs(lib):
+    # aabbs NULL: the boxes are the points themselves (rtbvh_ffi/src/lib.rs:396-422)
+    pts = np.random.default_rng(1).uniform(-1, 1, size=(5000, 3)).astype(np.float32)
+    out = _ffi.RTBvh()
+    rc = lib.create_bvh(None, len(pts), pts.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), 12, 1, 0,
+                        ctypes.byref(out))
+    assert rc == 0
+    a = np.zeros((len(pts), 8), np.float32)
+    a[:, 0:3] = pts
+    a[:, 4:7] = pts
+    on, oi = oracle.build(a, pts, "locb")
+    nodes = np.ctypeslib.as_array(ctypes.cast(out.nodes, ctypes.POINTER(ctypes.c_float)), (out.node_count * 8,))
+    assert np.array_equal(u32(nodes.reshape(-1, 8)), u32(on))
+    lib.free_bvh(out)
+
+
+def test_refit_bounds_bit_exact():
+    tris = scene("incoherent_20k")
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    before = g.nodes()
+    moved = (tris + np.random.default_rng(2).normal(scale=1e-3, size=tris.shape)).astype(np.float32)
+    g.refit(triangles=to_cuda(moved), mbvh=m)
+    after = g.nodes()
+    # topology is kept ...
+    assert np.array_equal(u32(after)[:, [3, 7]], u32(before)[:, [3, 7]])
+    # ... and the boxes equal the reference's refit bit for bit
+    a2, _ = oracle.triangle_prep(moved)
+    ref = oracle.refit(before, g.indices(), a2)
+    cols = [0, 1, 2, 4, 5, 6]
+    assert np.array_equal(u32(after)[:, cols], u32(ref)[:, cols])
+    # the re-collapsed MBVH equals the collapse of the refitted tree
+    assert np.array_equal(u32(m.quad_nodes()), u32(oracle.mbvh(after)))
+    # and tracing the moved triangles matches the oracle
+    rays, _ = scenes.incoherent_rays(8192, seed=4)
+    hits, _ = m.intersect(to_cuda(rays))
+    oh, _, _ = oracle.trace("mbvh", oracle.mbvh(after), g.indices(), moved.reshape(-1, 9), rays)
+    assert np.array_equal(u32(hits.cpu().numpy()), u32(oh))
+
+
+def test_morton_order_1m_is_a_stable_sort():
+    tris = scenes.incoherent(1_000_000, seed=2)
+    g = rb.Builder(primitives=rb.Triangles(to_cuda(tris))).construct_locally_ordered_clustered(host_mirror=True)
+    a, c = oracle.triangle_prep(tris)
+    codes, idx = oracle.morton_codes(a, c)
+    gi = g.indices()
+    assert np.array_equal(gi, idx)
+    assert (np.diff(codes[gi].astype(np.int64)) >= 0).all()
+
+
+def test_locb_1m_bit_exact_and_valid():
+    tris = scenes.incoherent(1_000_000, seed=2)
+    g = gpu_build(tris, "locb")
+    nodes = g.nodes()
+    assert len(nodes) == 2 * len(tris) - 1
+    assert g.validate(len(tris))
+    on, oi = oracle_build(tris, "locb")
+    assert np.array_equal(u32(nodes), u32(on))
+    m = rb.Mbvh.construct(g)
+    assert np.array_equal(u32(m.quad_nodes()), u32(oracle.mbvh(on)))
