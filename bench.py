@@ -54,6 +54,18 @@ def make_scene():
     return tris, rays, tmax
 
 
+def apply_size_overrides(args):
+    """--rays/--tris shrink the workload for profiling captures only; the
+    benchmark line is always taken at the full size."""
+    global N_RAYS, N_TRIS, METRIC
+    if args.rays:
+        N_RAYS = args.rays
+    if args.tris:
+        N_TRIS = args.tris
+    if args.rays or args.tris:
+        METRIC = METRIC + f" [reduced: {N_TRIS} tris, {N_RAYS} rays]"
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -330,7 +342,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rays", type=int, default=0, help="profiling only: fewer rays")
+    ap.add_argument("--tris", type=int, default=0, help="profiling only: fewer triangles")
     args = ap.parse_args()
+    apply_size_overrides(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
