@@ -78,6 +78,14 @@ __device__ __forceinline__ bool mt_test(const float4* tri, RayState& r, float& h
 
 // MbvhNode::intersect: mask bit i set when slot i is hit; ids packed as
 // 2-bit fields, ascending by t_min after the 5-compare network.
+//
+// FAST: for a ray whose origin, direction and inverse direction are all
+// finite, no slab value can be NaN ((m - o) * inv with finite factors), and
+// then the SSE select rule (a < b ? a : b) and the native min/max instruction
+// return the same value; at most the sign of a zero differs, which no later
+// comparison can see. So the fast form takes every decision the exact form
+// takes. Rays with a zero or non-finite component use the exact form.
+template <bool FAST>
 __device__ __forceinline__ void quad_intersect(const DMNode* node, const RayState& r, uint32_t& mask, uint32_t& ids,
                                                int4& children, int4& counts) {
   const float4* q = reinterpret_cast<const float4*>(node);
@@ -96,11 +104,17 @@ __device__ __forceinline__ void quad_intersect(const DMNode* node, const RayStat
     const float tx0 = (a_mnx[i] - r.ox) * r.ix, tx1 = (a_mxx[i] - r.ox) * r.ix;
     const float ty0 = (a_mny[i] - r.oy) * r.iy, ty1 = (a_mxy[i] - r.oy) * r.iy;
     const float tz0 = (a_mnz[i] - r.oz) * r.iz, tz1 = (a_mxz[i] - r.oz) * r.iz;
-    const float txn = sse_min(tx0, tx1), txx = sse_max(tx0, tx1);
-    const float tyn = sse_min(ty0, ty1), tyx = sse_max(ty0, ty1);
-    const float tzn = sse_min(tz0, tz1), tzx = sse_max(tz0, tz1);
-    const float tn = sse_max(txn, sse_max(tyn, tzn));
-    const float tx = sse_min(txx, sse_min(tyx, tzx));
+    float tn, tx;
+    if (FAST) {
+      tn = fmaxf(fminf(tx0, tx1), fmaxf(fminf(ty0, ty1), fminf(tz0, tz1)));
+      tx = fminf(fmaxf(tx0, tx1), fminf(fmaxf(ty0, ty1), fmaxf(tz0, tz1)));
+    } else {
+      const float txn = sse_min(tx0, tx1), txx = sse_max(tx0, tx1);
+      const float tyn = sse_min(ty0, ty1), tyx = sse_max(ty0, ty1);
+      const float tzn = sse_min(tz0, tz1), tzx = sse_max(tz0, tz1);
+      tn = sse_max(txn, sse_max(tyn, tzn));
+      tx = sse_min(txx, sse_min(tyx, tzx));
+    }
     tmin[i] = tn;
     if ((tx >= tn) && (tn < r.t)) m |= 1u << i;
   }
@@ -116,45 +130,130 @@ __device__ __forceinline__ void quad_intersect(const DMNode* node, const RayStat
   ids = i0 | (i1 << 2) | (i2 << 4) | (i3 << 6);
 }
 
+__device__ __forceinline__ bool finite_ray(const RayState& r) {
+  return isfinite(r.ox) && isfinite(r.oy) && isfinite(r.oz) && isfinite(r.dx) && isfinite(r.dy) && isfinite(r.dz) &&
+         isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
+}
+
 __device__ __forceinline__ int sel4(const int4& v, uint32_t i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// Persistent MBVH traversal with per-lane ray refill: a lane whose ray has
+// finished takes the next ray from a warp-local pool (refilled 128 rays at a
+// time from the global counter), so the warp's lanes stay busy instead of
+// idling until the warp's slowest ray ends. Each loop iteration visits one
+// quad node per lane; a ray's node/triangle order is the reference's.
+constexpr uint32_t kPoolBatch = 128;
+
 template <bool ANY_HIT, bool STATS>
-__device__ __forceinline__ void trace_one_mbvh(const TraceArgs& a, size_t r) {
-  RayState ray = load_ray(a.rays, r, a.t_max);
+__global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int* work) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  RayState ray;
   float hu = 0.0f, hv = 0.0f;
   int32_t prim = -1;
   uint32_t visits = 0, tests = 0, max_depth = 0;
   int32_t stack[kStack];
   int sp = -1;
-  uint32_t mask, ids;
-  int4 children, counts;
-  int32_t current = 0;
-  bool done = (a.node_count == 0);
-  if (!done) {
-    quad_intersect(a.mnodes, ray, mask, ids, children, counts);
+  size_t r = 0;
+  bool active = false, fast = true;
+  size_t pool_next = 0, pool_end = 0;  // warp-uniform
+  bool exhausted = false;              // warp-uniform
+  auto start_ray = [&](size_t rr) {
+    r = rr;
+    ray = load_ray(a.rays, r, a.t_max);
+    fast = finite_ray(ray);
+    hu = hv = 0.0f;
+    prim = -1;
+    visits = tests = max_depth = 0;
+    if (a.node_count == 0) {
+      a.hits[r] = make_float4(ray.t, 0.0f, 0.0f, __int_as_float(-1));
+      if (STATS) {
+        a.stats[3 * r + 0] = 0;
+        a.stats[3 * r + 1] = 0;
+        a.stats[3 * r + 2] = 0;
+      }
+    } else {
+      sp = 0;
+      stack[0] = 0;
+      active = true;
+    }
+  };
+  for (;;) {
+    if (!exhausted) {
+      uint32_t need = __ballot_sync(0xffffffffu, !active);
+      if (need) {
+        // first from what is left in the pool ...
+        const uint32_t avail = (uint32_t)(pool_end - pool_next);
+        if (avail) {
+          const uint32_t rank = __popc(need & lt_mask);
+          if (!active && rank < avail) start_ray(pool_next + rank);
+          const uint32_t c = __popc(need);
+          pool_next += c < avail ? c : avail;
+          need = __ballot_sync(0xffffffffu, !active && rank >= avail);
+        }
+        // ... then from a fresh batch of the global counter
+        if (need) {
+          unsigned int base = 0;
+          if (lane == 0) base = atomicAdd(work, kPoolBatch);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if ((size_t)base >= a.ray_count) {
+            exhausted = true;
+          } else {
+            pool_next = base;
+            pool_end = min((size_t)base + kPoolBatch, a.ray_count);
+            const uint32_t avail2 = (uint32_t)(pool_end - pool_next);
+            const bool mine = (need >> lane) & 1u;
+            const uint32_t rank = __popc(need & lt_mask);
+            if (mine && rank < avail2) start_ray(pool_next + rank);
+            const uint32_t c = __popc(need);
+            pool_next += c < avail2 ? c : avail2;
+          }
+        }
+      }
+    }
+    if (!__any_sync(0xffffffffu, active)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (!active) continue;
+    // ---- one quad node
+    const int32_t current = stack[sp--];
+    if ((uint32_t)current >= a.node_count) {
+      atomicOr(a.status, kStatusBadIndex);
+      active = false;
+      continue;
+    }
+    uint32_t mask, ids;
+    int4 children, counts;
+    if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
+    else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
     if (STATS) ++visits;
-  }
-  while (!done) {
+    bool done = false;
 #pragma unroll 1
-    for (int i = 0; i < 4 && !done; ++i) {
+    for (int i = 0; i < 4; ++i) {
       const uint32_t id = (ids >> (2 * (3 - i))) & 3u;
       if (!((mask >> id) & 1u)) continue;
       const int32_t count = sel4(counts, id);
       const int32_t lf = sel4(children, id);
       if (count > -1) {
-        if ((uint32_t)lf + (uint32_t)count > a.prim_count || lf < 0) {
+        if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
           atomicOr(a.status, kStatusBadIndex);
           done = true;
           break;
         }
+        bool hit_stop = false;
         for (int32_t j = 0; j < count; ++j) {
           if (STATS) ++tests;
           if (mt_test(a.tris + 3 * (size_t)(lf + j), ray, hu, hv, prim) && ANY_HIT) {
-            done = true;
+            hit_stop = true;
             break;
           }
+        }
+        if (hit_stop) {
+          done = true;
+          break;
         }
       } else if (lf > -1) {
         if (sp + 1 >= kStack) {
@@ -167,21 +266,15 @@ __device__ __forceinline__ void trace_one_mbvh(const TraceArgs& a, size_t r) {
         if (STATS && (uint32_t)(sp + 1) > max_depth) max_depth = (uint32_t)(sp + 1);
       }
     }
-    if (done) break;
-    if (sp < 0) break;
-    current = stack[sp--];
-    if ((uint32_t)current >= a.node_count) {
-      atomicOr(a.status, kStatusBadIndex);
-      break;
+    if (done || sp < 0) {
+      a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
+      if (STATS) {
+        a.stats[3 * r + 0] = visits;
+        a.stats[3 * r + 1] = tests;
+        a.stats[3 * r + 2] = max_depth;
+      }
+      active = false;
     }
-    quad_intersect(a.mnodes + current, ray, mask, ids, children, counts);
-    if (STATS) ++visits;
-  }
-  a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
-  if (STATS) {
-    a.stats[3 * r + 0] = visits;
-    a.stats[3 * r + 1] = tests;
-    a.stats[3 * r + 2] = max_depth;
   }
 }
 
@@ -271,8 +364,8 @@ __device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
   }
 }
 
-template <bool MBVH, bool ANY_HIT, bool STATS>
-__global__ void __launch_bounds__(kBlock) k_trace(TraceArgs a, unsigned int* work) {
+template <bool ANY_HIT, bool STATS>
+__global__ void __launch_bounds__(kBlock) k_trace_bvh(TraceArgs a, unsigned int* work) {
   const int lane = threadIdx.x & 31;
   for (;;) {
     unsigned int base = 0;
@@ -280,22 +373,20 @@ __global__ void __launch_bounds__(kBlock) k_trace(TraceArgs a, unsigned int* wor
     base = __shfl_sync(0xffffffffu, base, 0);
     if ((size_t)base >= a.ray_count) break;
     const size_t r = (size_t)base + lane;
-    if (r < a.ray_count) {
-      if (MBVH) trace_one_mbvh<ANY_HIT, STATS>(a, r);
-      else trace_one_bvh<ANY_HIT, STATS>(a, r);
-    }
+    if (r < a.ray_count) trace_one_bvh<ANY_HIT, STATS>(a, r);
   }
 }
 
 template <bool MBVH, bool ANY_HIT, bool STATS>
 cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
+  auto kern = MBVH ? k_trace_mbvh<ANY_HIT, STATS> : k_trace_bvh<ANY_HIT, STATS>;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace<MBVH, ANY_HIT, STATS>, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
   size_t grid = (size_t)sm_count() * per_sm;
   const size_t need = (a.ray_count + kBlock - 1) / kBlock;
   if (grid > need) grid = need;
-  k_trace<MBVH, ANY_HIT, STATS><<<(unsigned)grid, kBlock, 0, s>>>(a, work);
+  kern<<<(unsigned)grid, kBlock, 0, s>>>(a, work);
   return cudaGetLastError();
 }
 
