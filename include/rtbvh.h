@@ -230,6 +230,28 @@ ResultCode rtbvh_gpu_view(uint32_t structure_id, int is_mbvh, RTGpuView *view);
 ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float *vertices, const RTAabb *aabbs, uint32_t mbvh_id,
                            rtbvh_stream_t stream);
 
+/* Largest tree (in nodes) that rtbvh_gpu_refit_noalloc accepts: 1,048,576
+ * nodes, i.e. a BVH over up to 524,288 primitives. */
+#define RTBVH_REFIT_NOALLOC_MAX_NODES 1048576u
+
+/* No counterpart in the reference. The refit of rtbvh_gpu_refit (new
+ * primitive boxes, device pointer) for callers that cannot allocate device
+ * memory while they run, such as a per-frame animation loop that must not
+ * call cudaMalloc (it can synchronise the device or fail mid-frame). It
+ * allocates nothing: its scratch is a fixed array inside the library
+ * (8 MiB + 256 bytes, reserved on every GPU that loads the library until
+ * the process exits).
+ * - Updates the Bvh's device nodes only, asynchronously on `stream`; the
+ *   host mirror behind the handle's node pointer and any Mbvh made from the
+ *   Bvh are left as they were.
+ * - Trees with more than RTBVH_REFIT_NOALLOC_MAX_NODES nodes are rejected
+ *   with InvalidArgument before anything runs.
+ * - The first call on a device looks up the array's device address, so make
+ *   that first call before any stream capture.
+ * - All calls share the one array: calls that can overlap on the GPU (other
+ *   streams, other host threads) race and must be serialised by the caller. */
+ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb *aabbs, rtbvh_stream_t stream);
+
 /* Backward pass of the closest-hit triangle test for rays traced with
  * rtbvh_gpu_intersect_mbvh (hits as written there). Maps upstream
  * (dL/dt, dL/du, dL/dv) per ray (R x 3 float) to dL/dvertices (n x 9 float,

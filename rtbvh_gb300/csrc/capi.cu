@@ -800,6 +800,24 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
   return Ok;
 }
 
+ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb* aabbs, rtbvh_stream_t stream) {
+  if (aabbs == nullptr) return Error;
+  DAabb* nodes;
+  uint32_t node_count, prim_count;
+  const uint32_t* indices;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* b = lookup(bvh_id, false);
+    if (!b) return Error;
+    nodes = b->d_nodes;
+    node_count = b->node_count;
+    prim_count = b->prim_count;
+    indices = b->d_indices;
+  }
+  return refit_bvh_noalloc(nodes, node_count, indices, prim_count, reinterpret_cast<const DAabb*>(aabbs),
+                           static_cast<cudaStream_t>(stream));
+}
+
 ResultCode rtbvh_gpu_intersect_backward(const float* vertices, uintptr_t prim_count, const float* rays,
                                         const float* hits, const float* grad_tuv, uintptr_t ray_count,
                                         float* grad_vertices, float* grad_rays, rtbvh_stream_t stream) {

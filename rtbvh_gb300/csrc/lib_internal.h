@@ -81,6 +81,11 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
 ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
                      const DAabb* aabbs, cudaStream_t s);
 
+// refit_bvh with its scratch in a static device array instead of per-call
+// allocations (see rtbvh_gpu_refit_noalloc). Asynchronous on `s`.
+ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
+                             const DAabb* aabbs, cudaStream_t s);
+
 // ------------------------------------------------------------------ traversal
 struct TraceArgs {
   const DMNode* mnodes = nullptr;

@@ -15,6 +15,8 @@
 // The slot contents reproduce merge_nodes line by line, including its quirks
 // (a leaf child keeps the parent's box in its slot; the second slot of that
 // side stays empty with the parent's box).
+#include <mutex>
+
 #include "lib_internal.h"
 
 namespace rtbvh {
@@ -343,6 +345,68 @@ ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices,
       (e = cudaStreamSynchronize(s)))
     return cuda_rc(e);
   return st ? Error : Ok;
+}
+
+}  // namespace rtbvh
+
+// ---------------------------------------------------------------- refit without allocation
+// Variant of refit_bvh for callers that must not allocate device memory,
+// for example a renderer that refits every frame inside a region where it
+// is not allowed to call cudaMalloc (an allocation can synchronise the
+// device and can fail mid-frame). Its scratch (parent pointers, arrival
+// counters, a status word) lives in this file-scope array instead of being
+// allocated per call. The array is reserved on every GPU that loads the
+// library and stays reserved until the process exits.
+namespace rtbvh {
+
+namespace {
+
+constexpr uint32_t kNoAllocStatusWords = 64;  // 256 bytes, keeps the arrays 256-byte aligned
+static __device__ __align__(256) uint32_t g_refit_scratch[kNoAllocStatusWords + 2u * RTBVH_REFIT_NOALLOC_MAX_NODES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_refit_scratch on the current device, looked up once
+// per device (with that device current) on its first use.
+cudaError_t noalloc_scratch(uint32_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_refit_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = static_cast<uint32_t*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
+                             const DAabb* aabbs, cudaStream_t s) {
+  if (node_count == 0) return Ok;
+  if (node_count > RTBVH_REFIT_NOALLOC_MAX_NODES) return InvalidArgument;
+  uint32_t* base = nullptr;
+  cudaError_t e = noalloc_scratch(&base);
+  if (e != cudaSuccess) return cuda_rc(e);
+  uint32_t* status = base;
+  uint32_t* parent = base + kNoAllocStatusWords;
+  uint32_t* arrive = parent + RTBVH_REFIT_NOALLOC_MAX_NODES;
+  // The array keeps the previous call's contents: reset what must start
+  // clean (k_parents zeroes the arrival counters itself).
+  if ((e = cudaMemsetAsync(parent, 0xff, (size_t)node_count * 4, s)) ||
+      (e = cudaMemsetAsync(status, 0, kNoAllocStatusWords * 4, s)))
+    return cuda_rc(e);
+  const unsigned blocks = (node_count + kBlock - 1) / kBlock;
+  k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent, arrive, status);
+  k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, prim_count, aabbs, parent, arrive, status);
+  return cuda_rc(cudaGetLastError());
 }
 
 }  // namespace rtbvh
