@@ -9,6 +9,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -644,6 +645,15 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
   return Ok;
 }
 
+// Kernel variant for the traversal (RTBVH_TRACE_VARIANT overrides the default).
+static int trace_variant() {
+  static int v = []() {
+    const char* e = std::getenv("RTBVH_TRACE_VARIANT");
+    return e ? std::atoi(e) : 0;
+  }();
+  return v;
+}
+
 static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
                                float* hits, uint32_t flags, uint32_t* stats, cudaStream_t s) {
   TraceArgs a;
@@ -667,6 +677,7 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
   a.hits = reinterpret_cast<float4*>(hits);
   a.stats = (flags & RTBVH_TRACE_STATS) ? stats : nullptr;
   a.any_hit = (flags & RTBVH_TRACE_ANY_HIT) != 0;
+  a.variant = trace_variant();
   cudaError_t err = mbvh ? launch_trace_mbvh(a, s) : launch_trace_bvh(a, s);
   return cuda_rc(err);
 }

@@ -100,6 +100,7 @@ struct TraceArgs {
   uint32_t* stats = nullptr;
   uint32_t* status = nullptr;
   bool any_hit = false;
+  int variant = 0;  // register-budget variant of the MBVH kernel (see traverse.cu)
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
