@@ -167,6 +167,7 @@ typedef void *rtbvh_stream_t;
 /* flags for the trace entry points */
 #define RTBVH_TRACE_ANY_HIT 1u /* stop at the first accepted triangle (occlusion) */
 #define RTBVH_TRACE_STATS 2u   /* write per-ray node visits / triangle tests / max stack depth */
+#define RTBVH_TRACE_REORDER 4u /* MBVH: trace in (origin cell, direction)-sorted order; results are unchanged */
 
 /* Builder::construct_binned_sah / construct_locally_ordered_clustered on
  * device triangles (src/bvh.rs:87-137, with aabbs = Triangle::aabb and

@@ -35,6 +35,7 @@ class BvhType(enum.IntEnum):
 FLAG_NO_HOST_MIRROR = 1
 TRACE_ANY_HIT = 1
 TRACE_STATS = 2
+TRACE_REORDER = 4
 
 
 class RTAabb(ctypes.Structure):

@@ -241,11 +241,12 @@ class Mbvh:
         buf = ctypes.cast(h.indices, ctypes.POINTER(ctypes.c_uint32 * h.index_count)).contents
         return np.frombuffer(buf, dtype=np.uint32).copy()
 
-    def intersect(self, rays, t_max=None, any_hit=False, stats=False, stream=None):
+    def intersect(self, rays, t_max=None, any_hit=False, stats=False, stream=None, reorder=False):
         """GPU MbvhIndexIterator + triangle test for a batch of rays.
         rays: (R, 6) float32 (CUDA tensor or array). Returns (hits (R,4)
-        float32 CUDA tensor [t, u, v, prim bits], stats (R,3) int32 or None)."""
-        return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream)
+        float32 CUDA tensor [t, u, v, prim bits], stats (R,3) int32 or None).
+        reorder: trace in (origin, direction)-sorted order (same results)."""
+        return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream, reorder)
 
     def intersect_host(self, rays, t_max=None, any_hit=False):
         """Same, with host (numpy) rays and hits, copies included
@@ -269,13 +270,14 @@ class Mbvh:
             pass
 
 
-def _trace(fn, handle, rays, t_max, any_hit, stats, stream):
+def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False):
     r = _cuda_f32(rays, 6)
     n = r.shape[0]
     tm = _cuda_f32(t_max).reshape(-1) if t_max is not None else None
     hits = torch.empty((n, 4), dtype=torch.float32, device=r.device)
     st = torch.empty((n, 3), dtype=torch.int32, device=r.device) if stats else None
     flags = (_ffi.TRACE_ANY_HIT if any_hit else 0) | (_ffi.TRACE_STATS if stats else 0)
+    flags |= _ffi.TRACE_REORDER if reorder else 0
     check(fn(handle, _ptr(r), _ptr(tm), n, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect")
     return hits, st
 

@@ -160,9 +160,11 @@ __global__ void __launch_bounds__(kPrepBlock)
   float x0 = __ldg(t), y0 = __ldg(t + 1), z0 = __ldg(t + 2);
   float x1 = __ldg(t + 3), y1 = __ldg(t + 4), z1 = __ldg(t + 5);
   float x2 = __ldg(t + 6), y2 = __ldg(t + 7), z2 = __ldg(t + 8);
-  out[3 * k + 0] = make_float4(x0, y0, z0, __uint_as_float(p));
-  out[3 * k + 1] = make_float4(x1 - x0, y1 - y0, z1 - z0, 0.0f);
-  out[3 * k + 2] = make_float4(x2 - x0, y2 - y0, z2 - z0, 0.0f);
+  float4* o = out + (size_t)kTriFloat4 * k;
+  o[0] = make_float4(x0, y0, z0, __uint_as_float(p));
+  o[1] = make_float4(x1 - x0, y1 - y0, z1 - z0, 0.0f);
+  o[2] = make_float4(x2 - x0, y2 - y0, z2 - z0, 0.0f);
+  o[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 inline unsigned grid_for(size_t n, int block) { return (unsigned)((n + block - 1) / block); }

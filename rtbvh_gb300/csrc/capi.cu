@@ -162,7 +162,7 @@ ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t
   if (d_vertices) {
     if ((err = dmalloc(&e->d_vertices, 9 * n)) ||
         (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
-        (err = dmalloc(&e->d_tris, 3 * n)) ||
+        (err = dmalloc(&e->d_tris, (size_t)kTriFloat4 * n)) ||
         (err = launch_gather_triangles(e->d_vertices, e->d_indices, n, e->d_tris, s))) {
       e->release();
       return cuda_rc(err);
@@ -598,6 +598,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
+
   if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
       (err = dmalloc(&e->d_indices, prim_count)) ||
       (err = cudaMemcpyAsync(e->d_indices, d_indices, (size_t)prim_count * 4, cudaMemcpyDeviceToDevice, s))) {
@@ -605,8 +606,9 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     return cuda_rc(err);
   }
   if (d_tris) {
-    if ((err = dmalloc(&e->d_tris, 3 * (size_t)prim_count)) ||
-        (err = cudaMemcpyAsync(e->d_tris, d_tris, 48 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
+    if ((err = dmalloc(&e->d_tris, (size_t)kTriFloat4 * prim_count)) ||
+        (err = cudaMemcpyAsync(e->d_tris, d_tris, 16 * (size_t)kTriFloat4 * prim_count, cudaMemcpyDeviceToDevice,
+                               s)) ||
         (err = dmalloc(&e->d_vertices, 9 * (size_t)prim_count)) ||
         (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s))) {
       e->release();
@@ -638,20 +640,11 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
   if (prim_count != e->prim_count) return InequalAabbsAndPrimitives;
   cudaError_t err;
   if (!e->d_vertices && (err = dmalloc(&e->d_vertices, 9 * (size_t)prim_count))) return cuda_rc(err);
-  if (!e->d_tris && (err = dmalloc(&e->d_tris, 3 * (size_t)prim_count))) return cuda_rc(err);
+  if (!e->d_tris && (err = dmalloc(&e->d_tris, (size_t)kTriFloat4 * prim_count))) return cuda_rc(err);
   if ((err = cudaMemcpyAsync(e->d_vertices, vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
       (err = launch_gather_triangles(e->d_vertices, e->d_indices, prim_count, e->d_tris, s)))
     return cuda_rc(err);
   return Ok;
-}
-
-// Kernel variant for the traversal (RTBVH_TRACE_VARIANT overrides the default).
-static int trace_variant() {
-  static int v = []() {
-    const char* e = std::getenv("RTBVH_TRACE_VARIANT");
-    return e ? std::atoi(e) : 0;
-  }();
-  return v;
 }
 
 static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
@@ -677,7 +670,7 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
   a.hits = reinterpret_cast<float4*>(hits);
   a.stats = (flags & RTBVH_TRACE_STATS) ? stats : nullptr;
   a.any_hit = (flags & RTBVH_TRACE_ANY_HIT) != 0;
-  a.variant = trace_variant();
+  a.reorder = (flags & RTBVH_TRACE_REORDER) != 0;
   cudaError_t err = mbvh ? launch_trace_mbvh(a, s) : launch_trace_bvh(a, s);
   return cuda_rc(err);
 }
@@ -800,7 +793,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     m->d_mnodes = fresh;
     if (vertices) {
       if (!m->d_vertices && (err = dmalloc(&m->d_vertices, 9 * n))) return cuda_rc(err);
-      if (!m->d_tris && (err = dmalloc(&m->d_tris, 3 * n))) return cuda_rc(err);
+      if (!m->d_tris && (err = dmalloc(&m->d_tris, (size_t)kTriFloat4 * n))) return cuda_rc(err);
       if ((err = cudaMemcpyAsync(m->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
           (err = launch_gather_triangles(m->d_vertices, m->d_indices, n, m->d_tris, s)))
         return cuda_rc(err);

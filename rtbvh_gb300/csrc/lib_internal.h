@@ -47,8 +47,9 @@ cudaError_t launch_world_bounds(const DAabb* aabbs, size_t n, DAabb* world, uint
 // vals[i] = i.
 cudaError_t launch_morton(const float4* centers, size_t n, const DAabb* world, uint32_t* keys, uint32_t* vals,
                           cudaStream_t s);
-// Leaf-ordered triangles: out[3k..3k+2] = {v0, prim}, {v1 - v0, 0}, {v2 - v0, 0}
-// for p = indices[k].
+// Leaf-ordered triangles, kTriFloat4 float4 (64 bytes) per index slot:
+// {v0, prim}, {v1 - v0, 0}, {v2 - v0, 0}, {0} for p = indices[k].
+constexpr int kTriFloat4 = 4;
 cudaError_t launch_gather_triangles(const float* vertices, const uint32_t* indices, size_t n, float4* out,
                                     cudaStream_t s);
 
@@ -91,7 +92,7 @@ struct TraceArgs {
   const DMNode* mnodes = nullptr;
   const DAabb* nodes = nullptr;
   uint32_t node_count = 0;
-  const float4* tris = nullptr;  // leaf-ordered, 3 float4 per index slot
+  const float4* tris = nullptr;  // leaf-ordered, kTriFloat4 float4 per index slot
   uint32_t prim_count = 0;       // index slots (bounds of leaf ranges)
   const float* rays = nullptr;
   const float* t_max = nullptr;
@@ -100,7 +101,8 @@ struct TraceArgs {
   uint32_t* stats = nullptr;
   uint32_t* status = nullptr;
   bool any_hit = false;
-  int variant = 0;  // register-budget variant of the MBVH kernel (see traverse.cu)
+  const uint32_t* order = nullptr;  // optional: position k of the launch traces ray order[k]
+  bool reorder = false;             // sort rays by (origin cell, direction) before tracing
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);

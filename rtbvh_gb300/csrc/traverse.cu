@@ -18,7 +18,10 @@
 // a ray that would exceed it stops, reports prim -2 and sets
 // kStatusStackOverflow. A quad node (one 128-byte line) is read with four
 // 256-bit loads: the kernel is bound by L1 wavefronts (each lane reads its
-// own node), and halving the load count per node is worth 13 %.
+// own node), and halving the load count per node is worth 13 %. Leaf
+// triangles are 64 bytes ({v0, prim}, {e1}, {e2}, pad): two 256-bit loads.
+#include <cstdlib>
+
 #include "lib_internal.h"
 
 namespace rtbvh {
@@ -46,9 +49,20 @@ __device__ __forceinline__ RayState load_ray(const float* rays, size_t r, const 
   return s;
 }
 
+// One 256-bit read-only load (sm_100+): 8 floats from a 32-byte aligned address.
+__device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+               : "l"(p));
+}
+
 // SpatialTriangle::intersect with a leaf-ordered triangle {v0,prim},{e1},{e2}.
 __device__ __forceinline__ bool mt_test(const float4* tri, RayState& r, float& hu, float& hv, int32_t& prim) {
-  const float4 a = __ldg(tri), b = __ldg(tri + 1), c = __ldg(tri + 2);
+  float t0[8], t1[8];
+  ld8(reinterpret_cast<const float*>(tri), t0);
+  ld8(reinterpret_cast<const float*>(tri) + 8, t1);
+  const float4 a = make_float4(t0[0], t0[1], t0[2], t0[3]), b = make_float4(t0[4], t0[5], t0[6], t0[7]);
+  const float4 c = make_float4(t1[0], t1[1], t1[2], t1[3]);
   const float e1x = b.x, e1y = b.y, e1z = b.z;
   const float e2x = c.x, e2y = c.y, e2z = c.z;
   // h = d x e2
@@ -76,13 +90,6 @@ __device__ __forceinline__ bool mt_test(const float4* tri, RayState& r, float& h
     return true;
   }
   return false;
-}
-
-// One 256-bit read-only load (sm_100+): 8 floats from a 32-byte aligned address.
-__device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
-  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
-               : "l"(p));
 }
 
 // MbvhNode::intersect: mask bit i set when slot i is hit; ids packed as
@@ -169,14 +176,19 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   float hu = 0.0f, hv = 0.0f;
   int32_t prim = -1;
   uint32_t visits = 0, tests = 0, max_depth = 0;
+  // The node to visit next is kept in `next` instead of on the stack: the
+  // last child a node pushes is always the next one popped, so holding it in
+  // a register saves one store and one load per visited node. The logical
+  // stack is stack[0..sp] followed by `next` (when next >= 0).
   int32_t stack[kStack];
   int sp = -1;
+  int32_t next = -1;
   size_t r = 0;
   bool active = false, fast = true;
   size_t pool_next = 0, pool_end = 0;  // warp-uniform
   bool exhausted = false;              // warp-uniform
   auto start_ray = [&](size_t rr) {
-    r = rr;
+    r = a.order ? (size_t)__ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
     fast = finite_ray(ray);
     hu = hv = 0.0f;
@@ -190,8 +202,8 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         a.stats[3 * r + 2] = 0;
       }
     } else {
-      sp = 0;
-      stack[0] = 0;
+      sp = -1;
+      next = 0;
       active = true;
     }
   };
@@ -234,7 +246,8 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     }
     if (!active) continue;
     // ---- one quad node
-    const int32_t current = stack[sp--];
+    const int32_t current = next >= 0 ? next : stack[sp--];
+    next = -1;
     if ((uint32_t)current >= a.node_count) {
       atomicOr(a.status, kStatusBadIndex);
       active = false;
@@ -261,7 +274,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         bool hit_stop = false;
         for (int32_t j = 0; j < count; ++j) {
           if (STATS) ++tests;
-          if (mt_test(a.tris + 3 * (size_t)(lf + j), ray, hu, hv, prim) && ANY_HIT) {
+          if (mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim) && ANY_HIT) {
             hit_stop = true;
             break;
           }
@@ -271,17 +284,20 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
           break;
         }
       } else if (lf > -1) {
-        if (sp + 1 >= kStack) {
-          atomicOr(a.status, kStatusStackOverflow);
-          prim = -2;
-          done = true;
-          break;
+        if (next >= 0) {
+          if (sp + 1 >= kStack) {
+            atomicOr(a.status, kStatusStackOverflow);
+            prim = -2;
+            done = true;
+            break;
+          }
+          stack[++sp] = next;
         }
-        stack[++sp] = lf;
-        if (STATS && (uint32_t)(sp + 1) > max_depth) max_depth = (uint32_t)(sp + 1);
+        next = lf;
+        if (STATS && (uint32_t)(sp + 2) > max_depth) max_depth = (uint32_t)(sp + 2);
       }
     }
-    if (done || sp < 0) {
+    if (done || (next < 0 && sp < 0)) {
       a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
       if (STATS) {
         a.stats[3 * r + 0] = visits;
@@ -339,7 +355,7 @@ __device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
       bool stop = false;
       for (int32_t j = 0; j < node.count; ++j) {
         if (STATS) ++tests;
-        if (mt_test(a.tris + 3 * (size_t)(node.left_first + j), ray, hu, hv, prim) && ANY_HIT) {
+        if (mt_test(a.tris + kTriFloat4 * (size_t)(node.left_first + j), ray, hu, hv, prim) && ANY_HIT) {
           stop = true;
           break;
         }
@@ -392,6 +408,103 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh(TraceArgs a, unsigned int*
   }
 }
 
+// ------------------------------------------------------------------ ray order
+// Incoherent rays are traced in an order that groups rays with nearby
+// origins and similar directions, so that the lanes of a warp walk similar
+// nodes (fewer distinct cache lines per warp load, more L1 hits). Each ray's
+// traversal is unchanged; only the assignment of rays to lanes differs, and
+// hits are written to the ray's own slot.
+
+__global__ void __launch_bounds__(256) k_ray_origin_bounds(const float* __restrict__ rays, size_t n,
+                                                           uint32_t* __restrict__ acc) {
+  float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float2* p = reinterpret_cast<const float2*>(rays + 6 * i);
+    const float2 a = __ldg(p), b = __ldg(p + 1);
+    const float o[3] = {a.x, a.y, b.x};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (isfinite(o[k])) {
+        mn[k] = fminf(mn[k], o[k]);
+        mx[k] = fmaxf(mx[k], o[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+      mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      atomicMin(acc + k, float_to_ordered(mn[k]));
+      atomicMax(acc + 3 + k, float_to_ordered(mx[k]));
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t spread3_bits(uint32_t v) {
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__device__ __forceinline__ uint32_t spread2_bits(uint32_t v) {
+  v = (v | (v << 8)) & 0x00FF00FFu;
+  v = (v | (v << 4)) & 0x0F0F0F0Fu;
+  v = (v | (v << 2)) & 0x33333333u;
+  v = (v | (v << 1)) & 0x55555555u;
+  return v;
+}
+__device__ __forceinline__ uint32_t quant6(float x) {  // x in [0, 1]
+  float q = x * 64.0f;
+  return q >= 63.0f ? 63u : (q > 0.0f ? (uint32_t)q : 0u);
+}
+
+// key = Morton(origin cell, 6 bits per axis) << 12 | Morton(octahedral
+// direction, 6 bits per coordinate)
+__global__ void __launch_bounds__(256) k_ray_keys(const float* __restrict__ rays, size_t n,
+                                                  const uint32_t* __restrict__ acc, uint32_t* __restrict__ keys,
+                                                  uint32_t* __restrict__ vals) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float lo[3], inv[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = ordered_to_float(__ldg(acc + k));
+    const float ext = ordered_to_float(__ldg(acc + 3 + k)) - lo[k];
+    inv[k] = ext > 0.0f ? 1.0f / ext : 0.0f;
+  }
+  const float2* p = reinterpret_cast<const float2*>(rays + 6 * i);
+  const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  const float o[3] = {a.x, a.y, b.x};
+  const float d[3] = {b.y, c.x, c.y};
+  uint32_t oc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) oc[k] = quant6((o[k] - lo[k]) * inv[k]);
+  const float l1 = fabsf(d[0]) + fabsf(d[1]) + fabsf(d[2]);
+  float u = 0.0f, v = 0.0f;
+  if (l1 > 0.0f && isfinite(l1)) {
+    u = d[0] / l1;
+    v = d[1] / l1;
+    if (d[2] < 0.0f) {
+      const float uu = (1.0f - fabsf(v)) * (u >= 0.0f ? 1.0f : -1.0f);
+      const float vv = (1.0f - fabsf(u)) * (v >= 0.0f ? 1.0f : -1.0f);
+      u = uu;
+      v = vv;
+    }
+  }
+  const uint32_t du = quant6(u * 0.5f + 0.5f), dv = quant6(v * 0.5f + 0.5f);
+  const uint32_t ko = spread3_bits(oc[0]) | (spread3_bits(oc[1]) << 1) | (spread3_bits(oc[2]) << 2);
+  keys[i] = (ko << 12) | spread2_bits(du) | (spread2_bits(dv) << 1);
+  vals[i] = (uint32_t)i;
+}
+
 template <bool MBVH, bool ANY_HIT, bool STATS>
 cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
   auto kern = MBVH ? k_trace_mbvh<ANY_HIT, STATS> : k_trace_bvh<ANY_HIT, STATS>;
@@ -406,20 +519,32 @@ cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
 }
 
 template <bool MBVH>
-cudaError_t launch_any(const TraceArgs& a, cudaStream_t s) {
-  if (a.ray_count == 0) return cudaSuccess;
-  if (a.ray_count > 0xffffffffull - 64) return cudaErrorInvalidValue;
-  unsigned int* work = nullptr;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&work), sizeof(unsigned int), s);
-  if (e) return e;
-  if ((e = cudaMemsetAsync(work, 0, sizeof(unsigned int), s))) {
-    cudaFreeAsync(work, s);
-    return e;
+cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
+  if (a0.ray_count == 0) return cudaSuccess;
+  if (a0.ray_count > 0xffffffffull - 1024) return cudaErrorInvalidValue;
+  TraceArgs a = a0;
+  Scratch<unsigned int> work;
+  Scratch<uint32_t> keys, order, acc;
+  Scratch<char> sort_temp;
+  cudaError_t e;
+  if ((e = work.alloc(1, s)) || (e = cudaMemsetAsync(work.ptr, 0, sizeof(unsigned int), s))) return e;
+  if (MBVH && a.order == nullptr && a.reorder && a.ray_count < (1u << 30)) {
+    const size_t n = a.ray_count;
+    const size_t tb = radix_sort_temp_bytes(n);
+    if ((e = keys.alloc(n, s)) || (e = order.alloc(n, s)) || (e = acc.alloc(8, s)) || (e = sort_temp.alloc(tb, s)))
+      return e;
+    const uint32_t init[8] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u, 0u, 0u};
+    if ((e = cudaMemcpyAsync(acc.ptr, init, sizeof(init), cudaMemcpyHostToDevice, s))) return e;
+    unsigned blocks = (unsigned)((n + 255) / 256);
+    const unsigned cap = (unsigned)sm_count() * 8u;
+    k_ray_origin_bounds<<<blocks < cap ? blocks : cap, 256, 0, s>>>(a.rays, n, acc.ptr);
+    k_ray_keys<<<blocks, 256, 0, s>>>(a.rays, n, acc.ptr, keys.ptr, order.ptr);
+    if ((e = radix_sort_pairs(keys.ptr, order.ptr, n, 30, sort_temp.ptr, tb, a.status, s))) return e;
+    a.order = order.ptr;
   }
   const bool st = a.stats != nullptr;
-  if (a.any_hit) e = st ? launch3<MBVH, true, true>(a, s, work) : launch3<MBVH, true, false>(a, s, work);
-  else e = st ? launch3<MBVH, false, true>(a, s, work) : launch3<MBVH, false, false>(a, s, work);
-  cudaFreeAsync(work, s);
+  if (a.any_hit) e = st ? launch3<MBVH, true, true>(a, s, work.ptr) : launch3<MBVH, true, false>(a, s, work.ptr);
+  else e = st ? launch3<MBVH, false, true>(a, s, work.ptr) : launch3<MBVH, false, false>(a, s, work.ptr);
   return e;
 }
 

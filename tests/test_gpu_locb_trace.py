@@ -206,3 +206,26 @@ def test_locb_1m_bit_exact_and_valid():
     assert np.array_equal(u32(nodes), u32(on))
     m = rb.Mbvh.construct(g)
     assert np.array_equal(u32(m.quad_nodes()), u32(oracle.mbvh(on)))
+
+
+def test_sorted_large_batch_matches_oracle():
+    # with RTBVH_TRACE_REORDER rays are traced in (origin, direction)-sorted
+    # order; each ray's result and counts must be unchanged
+    tris = scene("incoherent_300k")
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    rays, tmax = scenes.incoherent_rays(1_000_000, seed=31)
+    hits, st = m.intersect(to_cuda(rays), stats=True, reorder=True)
+    hits, st = hits.cpu().numpy(), st.cpu().numpy().view(np.uint32)
+    plain, _ = m.intersect(to_cuda(rays))
+    assert np.array_equal(u32(hits), u32(plain.cpu().numpy()))
+    on, oi = oracle_build(tris, "locb")
+    om = oracle.mbvh(on)
+    pick = np.random.default_rng(3).choice(len(rays), 20000, replace=False)
+    oh, ost, _ = oracle.trace("mbvh", om, oi, tris.reshape(-1, 9), rays[pick])
+    assert np.array_equal(u32(hits[pick]), u32(oh))
+    assert np.array_equal(st[pick], ost)
+    ha, sta = m.intersect(to_cuda(rays), t_max=to_cuda(tmax), any_hit=True, stats=True, reorder=True)
+    oha, osta, _ = oracle.trace("mbvh", om, oi, tris.reshape(-1, 9), rays[pick], t_max=tmax[pick], any_hit=True)
+    assert np.array_equal(u32(ha.cpu().numpy()[pick]), u32(oha))
+    assert np.array_equal(sta.cpu().numpy().view(np.uint32)[pick], osta)
