@@ -244,8 +244,12 @@ def run_gpu(args):
             traffic = json.load(f).get("bytes_per_launch")
 
     cpu = None
+    workloads = {}
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(tris, rays)
+    if rank == 0 and not args.no_extra:
+        workloads["sphere_6400_binned_sah"] = workload_sphere_sah(not args.no_cpu_baseline)
+        workloads["differentiable_200k"] = workload_differentiable()
 
     if rank == 0:
         line = {
@@ -271,10 +275,121 @@ def run_gpu(args):
             "any_hit": {"value": round(ws * N_RAYS / (any_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
                         "t_max": "0.5 x distance"},
             "max_stack_depth": max_stack,
+            "workloads": workloads,
         }
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+
+
+def _cuda_time(fn, reps=5, warmup=2):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def workload_sphere_sah(with_cpu):
+    """6,400-triangle sphere, binned SAH + MBVH, 1024x1024 camera rays."""
+    import torch
+
+    import rtbvh_gb300 as rb
+    from rtbvh_gb300 import scenes
+    tris = scenes.sphere()
+    rays = scenes.camera_rays(1024, 1024)
+    d_tris, d_rays = torch.from_numpy(tris).cuda(), torch.from_numpy(rays).cuda()
+    holder = {}
+
+    def build():
+        holder["bvh"] = rb.Builder(primitives=rb.Triangles(d_tris)).construct_binned_sah(host_mirror=False)
+        holder["mbvh"] = rb.Mbvh.construct(holder["bvh"], host_mirror=False)
+
+    sah_ms = _cuda_time(lambda: rb.Builder(primitives=rb.Triangles(d_tris)).construct_binned_sah(host_mirror=False))
+    build()
+    mbvh_ms = _cuda_time(lambda: rb.Mbvh.construct(holder["bvh"], host_mirror=False))
+    m = holder["mbvh"]
+    trace_ms = _cuda_time(lambda: m.intersect(d_rays), reps=10)
+    out = {"triangles": len(tris), "rays": len(rays), "sah_build_ms": round(sah_ms, 3),
+           "mbvh_ms": round(mbvh_ms, 3), "closest_hit_mrays": round(len(rays) / (trace_ms * 1e-3) / 1e6, 1)}
+    if with_cpu:
+        import oracle
+        threads = os.cpu_count() or 1
+        a, c = oracle.triangle_prep(tris)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            nodes, idx = oracle.build(a, c, "sah", spawn_threshold=1024, threads=threads)
+        cpu_build = (time.perf_counter() - t0) / 5 * 1e3
+        mn = oracle.mbvh(nodes)
+        t0 = time.perf_counter()
+        oracle.trace("mbvh", mn, idx, tris.reshape(-1, 9), rays, threads=threads, stats=False)
+        cpu_rays = len(rays) / (time.perf_counter() - t0) / 1e6
+        out["cpu_baseline"] = {"sah_build_ms": round(cpu_build, 3), "closest_hit_mrays": round(cpu_rays, 2),
+                               "cores": threads, "kind": "port"}
+    return out
+
+
+def workload_differentiable():
+    """200,000-triangle sphere, 2048x2048 camera: forward (closest hit),
+    backward (hand-written kernel + sorted per-triangle sums), one vertex
+    step and the GPU refit; against the plain per-call path that recomputes
+    the triangle test with PyTorch autograd (index_add scatter)."""
+    import torch
+
+    import rtbvh_gb300 as rb
+    from rtbvh_gb300 import diff, scenes
+    tris = scenes.sphere_fast(500, 200, radius=1.0, noise=0.05, seed=5)
+    rays = scenes.camera_rays(2048, 2048)
+    verts = torch.from_numpy(tris).cuda()
+    d_rays = torch.from_numpy(rays).cuda()
+    g = torch.from_numpy(np.random.default_rng(7).normal(size=(len(rays), 3)).astype(np.float32)).cuda()
+    bvh = rb.Builder(primitives=rb.Triangles(verts)).construct_binned_sah(host_mirror=False)
+    m = rb.Mbvh.construct(bvh, host_mirror=False)
+    hits, _ = m.intersect(d_rays)
+    gv = torch.empty_like(verts)
+    gr = torch.empty_like(d_rays)
+
+    def fused():
+        h, _ = m.intersect(d_rays)
+        diff.intersect_backward(verts, d_rays, h, g, gv, gr)
+
+    def plain():
+        h, _ = m.intersect(d_rays)
+        prim = h[:, 3].contiguous().view(torch.int32)
+        hit = (prim >= 0).float()
+        idx = prim.clamp(min=0).long()
+        v = verts.detach().requires_grad_(True)
+        r = d_rays.detach().requires_grad_(True)
+        tri = v[idx]
+        o, d = r[:, :3], r[:, 3:]
+        e1, e2 = tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]
+        hh = torch.cross(d, e2, dim=1)
+        f = 1.0 / (e1 * hh).sum(1)
+        s = o - tri[:, 0]
+        u = f * (s * hh).sum(1)
+        q = torch.cross(s, e1, dim=1)
+        vv = f * (d * q).sum(1)
+        t = f * (e2 * q).sum(1)
+        loss = ((g[:, 0] * t + g[:, 1] * u + g[:, 2] * vv) * hit).sum()
+        loss.backward()
+        return v.grad, r.grad
+
+    fwd_ms = _cuda_time(lambda: m.intersect(d_rays))
+    fused_ms = _cuda_time(fused)
+    plain_ms = _cuda_time(plain)
+    step_ms = _cuda_time(lambda: bvh.refit(triangles=verts, mbvh=m), reps=3)
+    return {"triangles": len(tris), "rays": len(rays), "forward_ms": round(fwd_ms, 3),
+            "forward_backward_ms": round(fused_ms, 3), "plain_forward_backward_ms": round(plain_ms, 3),
+            "speedup_vs_plain": round(plain_ms / fused_ms, 2), "refit_and_recollapse_ms": round(step_ms, 3),
+            "plain": "same trace, then the triangle test recomputed and differentiated by PyTorch autograd"}
 
 
 def cpu_baseline(tris, rays, threads=None, sample=1_000_000):
@@ -342,6 +457,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--rays", type=int, default=0, help="profiling only: fewer rays")
     ap.add_argument("--tris", type=int, default=0, help="profiling only: fewer triangles")
     args = ap.parse_args()
