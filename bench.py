@@ -250,6 +250,7 @@ def run_gpu(args):
     if rank == 0 and not args.no_extra:
         workloads["sphere_6400_binned_sah"] = workload_sphere_sah(not args.no_cpu_baseline)
         workloads["differentiable_200k"] = workload_differentiable()
+        workloads["batched_512_meshes"] = workload_batched()
 
     if rank == 0:
         line = {
@@ -390,6 +391,58 @@ def workload_differentiable():
             "forward_backward_ms": round(fused_ms, 3), "plain_forward_backward_ms": round(plain_ms, 3),
             "speedup_vs_plain": round(plain_ms / fused_ms, 2), "refit_and_recollapse_ms": round(step_ms, 3),
             "plain": "same trace, then the triangle test recomputed and differentiated by PyTorch autograd"}
+
+
+def workload_batched(mesh_count=512, seed=44):
+    """512 perturbed spheres, triangle counts log-uniform in [64, 200,000],
+    round(2000 sqrt(n)) incoherent rays each: one captured build + trace for
+    all meshes against the per-mesh loop (build, collapse, trace per mesh)."""
+    import math
+
+    import torch
+
+    import rtbvh_gb300 as rb
+    from rtbvh_gb300 import scenes
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.exp(rng.uniform(math.log(64), math.log(200_000), size=mesh_count)).astype(np.int64)
+    parts, rays, po, ro = [], [], [0], [0]
+    for m, n in enumerate(counts):
+        cells = max(2, int(n) // 2)
+        n_lat = max(2, int(round(math.sqrt(cells / 2.0))))
+        n_lon = max(3, int(round(cells / n_lat)))
+        centre = tuple(rng.uniform(-5, 5, size=3))
+        t = scenes.sphere_fast(n_lon, n_lat, radius=1.0, noise=0.05, seed=seed * 10000 + m, center=centre)
+        r, _ = scenes.incoherent_rays(int(round(2000 * math.sqrt(len(t)))), seed=seed * 10000 + 5000 + m,
+                                      center=centre, radius=2.0, lo=-1.0, hi=1.0)
+        parts.append(t)
+        rays.append(r)
+        po.append(po[-1] + len(t))
+        ro.append(ro[-1] + len(r))
+    tris = np.concatenate(parts)
+    allr = np.concatenate(rays)
+    d_tris, d_rays = torch.from_numpy(tris).cuda(), torch.from_numpy(allr).cuda()
+    batch = rb.Batch(d_tris, po, d_rays, ro)
+    graph_ms = _cuda_time(lambda: batch.run(), reps=5, warmup=1)
+    eager_ms = _cuda_time(lambda: batch.run(graph=False), reps=3, warmup=1)
+    if batch.status() != rb.ResultCode.Ok:
+        raise RuntimeError("batched run reported an error")
+
+    def per_mesh():
+        for m in range(mesh_count):
+            b = rb.Builder(primitives=rb.Triangles(d_tris[po[m]:po[m + 1]])).construct_locally_ordered_clustered(
+                host_mirror=False)
+            mb = rb.Mbvh.construct(b, host_mirror=False)
+            mb.intersect(d_rays[ro[m]:ro[m + 1]])
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    per_mesh()
+    torch.cuda.synchronize()
+    loop_ms = (time.perf_counter() - t0) * 1e3
+    return {"meshes": mesh_count, "triangles": int(po[-1]), "rays": int(ro[-1]),
+            "graph_build_trace_ms": round(graph_ms, 2), "uncaptured_build_trace_ms": round(eager_ms, 2),
+            "per_mesh_loop_ms": round(loop_ms, 2), "speedup_vs_per_mesh_loop": round(loop_ms / graph_ms, 2),
+            "mrays_including_build": round(ro[-1] / (graph_ms * 1e-3) / 1e6, 1)}
 
 
 def cpu_baseline(tris, rays, threads=None, sample=1_000_000):

@@ -263,6 +263,46 @@ ResultCode rtbvh_gpu_intersect_backward(const float *vertices, uintptr_t prim_co
                                         const float *hits, const float *grad_tuv, uintptr_t ray_count,
                                         float *grad_vertices, float *grad_rays, rtbvh_stream_t stream);
 
+/* ---- many meshes in one build + trace (no counterpart in the reference)
+ * The meshes are concatenated: mesh m owns triangles
+ * [prim_offsets[m], prim_offsets[m + 1]) of `vertices` (every mesh needs at
+ * least one triangle) and rays [ray_offsets[m], ray_offsets[m + 1]) of
+ * `rays`. Each mesh gets the locally-ordered clustering build + MBVH of its
+ * own triangles (Builder::construct_locally_ordered_clustered + Mbvh::from),
+ * and its rays are traced against it; hit prim ids are indices into the
+ * concatenated triangles. All meshes share one set of launches: a stable
+ * (mesh, Morton) sort, one block per mesh for the clustering and the
+ * collapse, and one persistent traversal launch. create() allocates every
+ * buffer and captures the whole pipeline in a CUDA graph; run() replays it
+ * on the same device buffers (update their contents in place between runs).
+ * prim_offsets / ray_offsets are host arrays of mesh_count + 1 entries. */
+typedef struct RTBatch {
+  uint32_t id;
+} RTBatch;
+
+typedef struct RTGpuBatchView {
+  const RTBvhNode *nodes;        /* forest: mesh m's nodes start at 2 prim_offsets[m] - m */
+  uint32_t node_capacity;
+  const uint32_t *indices;       /* primitive order of every mesh, global indices */
+  const RTMbvhNode *mnodes;      /* mesh m's quad nodes: [mnode_base[m], mnode_base[m + 1]) */
+  const uint32_t *mnode_base;    /* device, mesh_count + 1 */
+  const uint32_t *prim_offsets;  /* device, mesh_count + 1 */
+  uint32_t mesh_count;
+  const float *leaf_triangles;
+} RTGpuBatchView;
+
+ResultCode rtbvh_gpu_batch_create(const float *vertices, const uint32_t *prim_offsets, uint32_t mesh_count,
+                                  const float *rays, const float *t_max, const uint32_t *ray_offsets, float *hits,
+                                  uint32_t flags, rtbvh_stream_t stream, RTBatch *result);
+/* Replays the captured build + trace on `stream`. */
+ResultCode rtbvh_gpu_batch_run(RTBatch batch, rtbvh_stream_t stream);
+/* The same pipeline issued as individual launches (no graph). */
+ResultCode rtbvh_gpu_batch_run_uncaptured(RTBatch batch, rtbvh_stream_t stream);
+ResultCode rtbvh_gpu_batch_view(RTBatch batch, RTGpuBatchView *view);
+/* Reads and clears the device status of the last runs (synchronises). */
+ResultCode rtbvh_gpu_batch_status(RTBatch batch);
+void rtbvh_gpu_batch_free(RTBatch batch);
+
 /* Library version string. */
 const char *rtbvh_gpu_version(void);
 

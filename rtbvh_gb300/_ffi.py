@@ -63,6 +63,16 @@ class RTMbvh(ctypes.Structure):
                 ("index_count", ctypes.c_uint32), ("indices", ctypes.POINTER(ctypes.c_uint32))]
 
 
+class RTBatch(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint32)]
+
+
+class RTGpuBatchView(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_void_p), ("node_capacity", ctypes.c_uint32), ("indices", ctypes.c_void_p),
+                ("mnodes", ctypes.c_void_p), ("mnode_base", ctypes.c_void_p), ("prim_offsets", ctypes.c_void_p),
+                ("mesh_count", ctypes.c_uint32), ("leaf_triangles", ctypes.c_void_p)]
+
+
 class RTGpuView(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_void_p), ("node_count", ctypes.c_uint32),
                 ("indices", ctypes.c_void_p), ("index_count", ctypes.c_uint32),
@@ -100,6 +110,12 @@ SIGNATURES = {
     "rtbvh_gpu_refit": (_rc, [_u32, _vp, _vp, _u32, _vp]),
     "rtbvh_gpu_refit_noalloc": (_rc, [_u32, _vp, _vp]),
     "rtbvh_gpu_intersect_backward": (_rc, [_vp, _sz, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "rtbvh_gpu_batch_create": (_rc, [_vp, _vp, _u32, _vp, _vp, _vp, _vp, _u32, _vp, ctypes.POINTER(RTBatch)]),
+    "rtbvh_gpu_batch_run": (_rc, [RTBatch, _vp]),
+    "rtbvh_gpu_batch_run_uncaptured": (_rc, [RTBatch, _vp]),
+    "rtbvh_gpu_batch_view": (_rc, [RTBatch, ctypes.POINTER(RTGpuBatchView)]),
+    "rtbvh_gpu_batch_status": (_rc, [RTBatch]),
+    "rtbvh_gpu_batch_free": (None, [RTBatch]),
     "rtbvh_gpu_version": (ctypes.c_char_p, []),
 }
 

@@ -340,6 +340,64 @@ class Builder:
         return Bvh(out, build_type, n)
 
 
+class Batch:
+    """Many meshes built and traced together (rtbvh_gpu_batch_*): mesh m owns
+    triangles [prim_offsets[m], prim_offsets[m + 1]) of `vertices` and rays
+    [ray_offsets[m], ray_offsets[m + 1]) of `rays`. The whole build + trace
+    is captured in a CUDA graph at construction; run() replays it. The
+    vertex/ray tensors are bound by address: change their contents in place."""
+
+    def __init__(self, vertices, prim_offsets, rays, ray_offsets, t_max=None, any_hit=False, stream=None):
+        self._lib = _ffi.load()
+        self.vertices = _cuda_f32(vertices).reshape(-1, 3, 3)
+        self.rays = _cuda_f32(rays, 6)
+        self.t_max = _cuda_f32(t_max).reshape(-1) if t_max is not None else None
+        self.prim_offsets = np.ascontiguousarray(np.asarray(prim_offsets, dtype=np.uint32))
+        self.ray_offsets = np.ascontiguousarray(np.asarray(ray_offsets, dtype=np.uint32))
+        self.mesh_count = len(self.prim_offsets) - 1
+        self.hits = torch.empty((self.rays.shape[0], 4), dtype=torch.float32, device=self.rays.device)
+        self._b = _ffi.RTBatch()
+        flags = _ffi.TRACE_ANY_HIT if any_hit else 0
+        check(self._lib.rtbvh_gpu_batch_create(
+            _ptr(self.vertices), self.prim_offsets.ctypes.data_as(ctypes.c_void_p), self.mesh_count,
+            _ptr(self.rays), _ptr(self.t_max), self.ray_offsets.ctypes.data_as(ctypes.c_void_p), _ptr(self.hits),
+            flags, _stream(stream), ctypes.byref(self._b)), "batch_create")
+
+    def run(self, graph=True, stream=None):
+        fn = self._lib.rtbvh_gpu_batch_run if graph else self._lib.rtbvh_gpu_batch_run_uncaptured
+        check(fn(self._b, _stream(stream)), "batch_run")
+        return self.hits
+
+    def view(self):
+        v = _ffi.RTGpuBatchView()
+        check(self._lib.rtbvh_gpu_batch_view(self._b, ctypes.byref(v)), "batch_view")
+        return v
+
+    def status(self):
+        return ResultCode(self._lib.rtbvh_gpu_batch_status(self._b))
+
+    def __del__(self):
+        try:
+            self._lib.rtbvh_gpu_batch_free(self._b)
+        except Exception:
+            pass
+
+
+class DeviceArray:
+    """Zero-copy view of library-owned device memory (for torch.as_tensor)."""
+
+    def __init__(self, ptr, shape, typestr="<f4"):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), True),
+                                         "version": 3}
+
+
+def device_copy(ptr, shape, dtype=np.float32):
+    """Host numpy copy of library-owned device memory."""
+    typestr = {np.float32: "<f4", np.uint32: "<u4", np.int32: "<i4"}[dtype]
+    t = torch.as_tensor(DeviceArray(ptr, shape, typestr), device="cuda")
+    return t.clone().cpu().numpy()
+
+
 def hit_prims(hits):
     """int32 primitive ids of a (R, 4) hits array/tensor (-1: miss)."""
     if isinstance(hits, torch.Tensor):

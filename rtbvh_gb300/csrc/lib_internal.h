@@ -103,9 +103,30 @@ struct TraceArgs {
   bool any_hit = false;
   const uint32_t* order = nullptr;  // optional: position k of the launch traces ray order[k]
   bool reorder = false;             // sort rays by (origin cell, direction) before tracing
+  // Forest of many meshes: ray r belongs to the mesh m with
+  // seg_ray_off[m] <= r < seg_ray_off[m + 1] and starts at quad node
+  // seg_root[m]; a mesh without quad nodes (seg_root[m] == seg_root[m + 1])
+  // is empty and its rays miss.
+  const uint32_t* seg_ray_off = nullptr;
+  const uint32_t* seg_root = nullptr;
+  uint32_t seg_count = 0;
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
+
+// ------------------------------------------------------------------ many meshes
+// Per-mesh clustering of a concatenated forest (see locb.cu).
+cudaError_t launch_locb_segments(const DAabb* aabbs, const uint32_t* sorted, uint32_t* indices,
+                                 const uint32_t* prim_off, const uint32_t* order, const DAabb* worlds,
+                                 uint32_t mesh_count, uint32_t total_prims, DAabb* lvl0, DAabb* lvl1,
+                                 DAabb* final_nodes, uint32_t* nb, uint32_t* status, unsigned blocks,
+                                 cudaStream_t s);
+// Per-mesh MBVH collapse of a concatenated forest (see mbvh.cu).
+cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, const uint32_t* prim_off,
+                                     const uint32_t* order, uint32_t mesh_count, uint32_t* parent, uint32_t* arrive,
+                                     uint32_t* cnt_e, uint32_t* cnt_o, uint32_t* mbase, uint2* q0, uint2* q1,
+                                     DMNode* mnodes, uint32_t m_capacity, uint32_t* status, unsigned blocks,
+                                     cudaStream_t s);
 
 // ------------------------------------------------------------------ backward
 cudaError_t launch_intersect_backward(const float* vertices, size_t prim_count, const float* rays,

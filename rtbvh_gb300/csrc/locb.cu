@@ -100,8 +100,6 @@ __device__ void nn_tile(const DAabb* in, uint32_t* nb, uint32_t begin, uint32_t 
 __device__ uint32_t scatter_tile(const DAabb* in, DAabb* out, DAabb* final_nodes, const uint32_t* nb, uint32_t begin,
                                  uint32_t end, uint32_t s0, uint32_t c1, uint32_t carry, uint32_t mc,
                                  uint32_t* s_flag, uint32_t* s_warp, uint32_t* status) {
-  const uint32_t node_total = 2u * 0u;  // unused marker (kept for symmetry)
-  (void)node_total;
   for (int k = threadIdx.x; k < kBlock + kRadius; k += kBlock) {
     uint32_t idx = s0 + k;
     s_flag[k] = idx < end ? merge_flag(nb, idx) : 0u;
@@ -149,12 +147,45 @@ __device__ uint32_t scatter_tile(const DAabb* in, DAabb* out, DAabb* final_nodes
   return carry + tile_total;
 }
 
+// Clustering levels of the range [begin, end) run by one block (block
+// barriers only) until one node is left, which is stored at final[begin].
+// Returns false (status set) on a level without a merge.
+__device__ bool locb_block_finish(DAabb* const lvl[2], DAabb* final_nodes, uint32_t* nb, uint32_t& begin,
+                                  uint32_t& end, int& cur, uint32_t& levels, SBox* s_box, uint32_t* s_flag,
+                                  uint32_t* s_warp, uint32_t* status) {
+  while (end - begin > 1) {
+    const DAabb* in = lvl[cur];
+    DAabb* out = lvl[cur ^ 1];
+    for (uint32_t t0 = begin; t0 < end; t0 += kBlock) nn_tile(in, nb, begin, end, t0, s_box, status);
+    __threadfence_block();
+    __syncthreads();
+    uint32_t local = 0;
+    for (uint32_t i = begin + threadIdx.x; i < end; i += kBlock) local += merge_flag(nb, i);
+    uint32_t mc;
+    block_inclusive_scan<kBlock>(local, s_warp, &mc);
+    if (mc == 0) {
+      if (threadIdx.x == 0) atomicOr(status, kStatusNoMerge);
+      return false;
+    }
+    uint32_t carry = 0;
+    for (uint32_t s0 = begin; s0 < end; s0 += kBlock)
+      carry = scatter_tile(in, out, final_nodes, nb, begin, end, s0, end, carry, mc, s_flag, s_warp, status);
+    __threadfence_block();
+    __syncthreads();
+    begin -= mc;
+    end -= 2u * mc;
+    cur ^= 1;
+    ++levels;
+  }
+  if (threadIdx.x == 0) store_aabb(final_nodes + begin, load_aabb_cg(lvl[cur] + begin));
+  __syncthreads();
+  return true;
+}
+
 __global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
   __shared__ SBox s_box[kBlock + 2 * kRadius];
   __shared__ uint32_t s_flag[kBlock + kRadius];
   __shared__ uint32_t s_warp[kBlock / 32];
-  __shared__ uint32_t s_red[2];
-
   const uint32_t node_count = 2u * p.n - 1u;
   uint32_t begin = p.n - 1u, end = node_count;
   int cur = 0;
@@ -206,38 +237,12 @@ __global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
 
   // ---------------------------------------------------------------- tail (block 0)
   if (blockIdx.x != 0) return;
-  while (end - begin > 1) {
-    const uint32_t m = end - begin;
-    const DAabb* in = p.lvl[cur];
-    DAabb* out = p.lvl[cur ^ 1];
-    for (uint32_t t0 = begin; t0 < end; t0 += kBlock) nn_tile(in, p.nb, begin, end, t0, s_box, p.status);
-    __threadfence_block();
-    __syncthreads();
-    uint32_t local = 0;
-    for (uint32_t i = begin + threadIdx.x; i < end; i += kBlock) local += merge_flag(p.nb, i);
-    uint32_t mc;
-    block_inclusive_scan<kBlock>(local, s_warp, &mc);
-    if (mc == 0) {
-      if (threadIdx.x == 0) atomicOr(p.status, kStatusNoMerge);
-      return;
-    }
-    uint32_t carry = 0;
-    for (uint32_t s0 = begin; s0 < end; s0 += kBlock)
-      carry = scatter_tile(in, out, p.final_nodes, p.nb, begin, end, s0, end, carry, mc, s_flag, s_warp, p.status);
-    __threadfence_block();
-    __syncthreads();
-    (void)m;
-    begin -= mc;
-    end -= 2u * mc;
-    cur ^= 1;
-    ++levels;
-  }
+  if (!locb_block_finish(p.lvl, p.final_nodes, p.nb, begin, end, cur, levels, s_box, s_flag, s_warp, p.status))
+    return;
   if (threadIdx.x == 0) {
-    store_aabb(p.final_nodes + begin, load_aabb_cg(p.lvl[cur] + begin));
     p.info[0] = levels;
     p.info[1] = begin;
   }
-  (void)s_red;
 }
 
 // Leaves: sorted boxes + 1e-4, count 1, left_first = i (locb.rs:289-294).
@@ -266,6 +271,80 @@ __global__ void k_locb_single(const DAabb* world, uint32_t n, DAabb* nodes, uint
     store_aabb(nodes, w);
   }
   if (threadIdx.x < n) indices[threadIdx.x] = threadIdx.x;
+}
+
+
+// ---------------------------------------------------------------- many meshes
+// One block per mesh clusters the mesh's own node range of a concatenated
+// forest. Mesh m owns primitives [off_m, off_m + n_m) and nodes
+// [2 off_m - m, 2 off_m - m + 2 n_m - 1); the placement arithmetic of a level
+// depends only on differences of indices, so every node, left_first and
+// leaf offset comes out as the single-mesh build's shifted by the mesh's
+// offsets.
+struct SegParams {
+  DAabb* lvl[2];
+  DAabb* final_nodes;
+  uint32_t* nb;
+  const uint32_t* prim_off;   // mesh_count + 1
+  const uint32_t* order;      // meshes in processing order (largest first)
+  const DAabb* worlds;        // per-mesh union_of_list boxes
+  uint32_t* indices;          // sorted primitive indices (global); identity for n <= 2
+  uint32_t* status;
+  uint32_t mesh_count;
+};
+
+__global__ void __launch_bounds__(kBlock) k_locb_segments(SegParams p) {
+  __shared__ SBox s_box[kBlock + 2 * kRadius];
+  __shared__ uint32_t s_flag[kBlock + kRadius];
+  __shared__ uint32_t s_warp[kBlock / 32];
+  for (uint32_t q = blockIdx.x; q < p.mesh_count; q += gridDim.x) {
+    const uint32_t m = p.order[q];
+    const uint32_t off = p.prim_off[m], n = p.prim_off[m + 1] - off;
+    if (n == 0) continue;
+    const uint32_t nbase = 2u * off - m;
+    if (n <= 2) {
+      if (threadIdx.x == 0) {
+        DAabb w = p.worlds[m];
+        w.count = (int32_t)n;
+        w.left_first = (int32_t)off;
+        store_aabb(p.final_nodes + nbase, w);
+      }
+      if (threadIdx.x < n) p.indices[off + threadIdx.x] = off + threadIdx.x;
+      continue;
+    }
+    uint32_t begin = nbase + n - 1u, end = nbase + 2u * n - 1u, levels = 0;
+    int cur = 0;
+    if (!locb_block_finish(p.lvl, p.final_nodes, p.nb, begin, end, cur, levels, s_box, s_flag, s_warp, p.status))
+      return;
+  }
+}
+
+// Leaves of every mesh: sorted position k of mesh m (off_m <= k < off_m + n_m)
+// becomes node 2 off_m - m + n_m - 1 + (k - off_m) with the primitive's box
+// + 1e-4, count 1, left_first = k.
+__global__ void __launch_bounds__(kBlock)
+    k_locb_segment_leaves(const DAabb* __restrict__ aabbs, const uint32_t* __restrict__ sorted,
+                          const uint32_t* __restrict__ prim_off, uint32_t mesh_count, uint32_t total,
+                          DAabb* __restrict__ lvl) {
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+  if (k >= total) return;
+  uint32_t lo = 0, hi = mesh_count;  // mesh with prim_off[m] <= k < prim_off[m + 1]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(prim_off + mid) <= k) lo = mid;
+    else hi = mid;
+  }
+  const uint32_t m = lo, off = __ldg(prim_off + m), n = __ldg(prim_off + m + 1) - off;
+  if (n <= 2) return;
+  DAabb b = load_aabb(aabbs + __ldg(sorted + k));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    b.min[a] = b.min[a] - 0.0001f;
+    b.max[a] = b.max[a] + 0.0001f;
+  }
+  b.count = 1;
+  b.left_first = (int32_t)k;
+  store_aabb(lvl + (2u * off - m) + (n - 1u) + (k - off), b);
 }
 
 }  // namespace
@@ -352,6 +431,33 @@ ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n_, cuda
   out->indices = indices;
   out->node_count = node_count;
   return Ok;
+}
+
+}  // namespace rtbvh
+
+namespace rtbvh {
+
+cudaError_t launch_locb_segments(const DAabb* aabbs, const uint32_t* sorted, uint32_t* indices,
+                                 const uint32_t* prim_off, const uint32_t* order, const DAabb* worlds,
+                                 uint32_t mesh_count, uint32_t total_prims, DAabb* lvl0, DAabb* lvl1,
+                                 DAabb* final_nodes, uint32_t* nb, uint32_t* status, unsigned blocks,
+                                 cudaStream_t s) {
+  if (total_prims == 0 || mesh_count == 0) return cudaSuccess;
+  k_locb_segment_leaves<<<(total_prims + kBlock - 1) / kBlock, kBlock, 0, s>>>(aabbs, sorted, prim_off, mesh_count,
+                                                                                total_prims, lvl0);
+  SegParams p;
+  p.lvl[0] = lvl0;
+  p.lvl[1] = lvl1;
+  p.final_nodes = final_nodes;
+  p.nb = nb;
+  p.prim_off = prim_off;
+  p.order = order;
+  p.worlds = worlds;
+  p.indices = indices;
+  p.status = status;
+  p.mesh_count = mesh_count;
+  k_locb_segments<<<blocks, kBlock, 0, s>>>(p);
+  return cudaGetLastError();
 }
 
 }  // namespace rtbvh

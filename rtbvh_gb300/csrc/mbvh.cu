@@ -198,6 +198,78 @@ __global__ void k_collapse_init(const uint32_t* cnt_e, const DAabb* nodes, uint2
   }
 }
 
+
+// ---------------------------------------------------------------- many meshes
+// A concatenated forest: mesh m's root is BVH2 node 2 off_m - m. Its quad
+// nodes get the contiguous index range [mbase[m], mbase[m+1]) (the
+// single-mesh numbering shifted by mbase[m]), and one block per mesh runs
+// the top-down frontier of k_collapse with block barriers.
+__global__ void __launch_bounds__(1024) k_seg_mbase(const DAabb* __restrict__ nodes, const uint32_t* __restrict__ cnt_e,
+                                                    const uint32_t* __restrict__ prim_off, uint32_t mesh_count,
+                                                    uint32_t* __restrict__ mbase) {
+  __shared__ uint32_t s_warp[32];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < mesh_count; base += 1024) {
+    const uint32_t m = base + threadIdx.x;
+    uint32_t q = 0;
+    if (m < mesh_count) {
+      const uint32_t off = prim_off[m], n = prim_off[m + 1] - off;
+      if (n > 0) {
+        const uint32_t root = 2u * off - m;
+        q = load_aabb(nodes + root).count < 0 ? cnt_e[root] : 1u;
+      }
+    }
+    uint32_t total;
+    const uint32_t incl = block_inclusive_scan<1024>(q, s_warp, &total);
+    if (m < mesh_count) mbase[m] = carry + incl - q;
+    carry += total;
+  }
+  if (threadIdx.x == 0) mbase[mesh_count] = carry;
+}
+
+struct SegCollapseParams {
+  CollapseParams c;
+  const uint32_t* prim_off;
+  const uint32_t* order;
+  const uint32_t* mbase;
+  uint2* queue[2];
+  uint32_t mesh_count;
+};
+
+__global__ void __launch_bounds__(kBlock) k_collapse_segments(SegCollapseParams p) {
+  __shared__ uint32_t s_count[2];
+  for (uint32_t q = blockIdx.x; q < p.mesh_count; q += gridDim.x) {
+    const uint32_t m = p.order[q];
+    const uint32_t off = p.prim_off[m], n = p.prim_off[m + 1] - off;
+    if (n == 0) continue;
+    const uint32_t base = p.mbase[m];
+    const uint32_t quads = p.mbase[m + 1] - base;
+    if (threadIdx.x == 0) {
+      p.queue[0][base] = make_uint2(2u * off - m, base);
+      s_count[0] = 1;
+      s_count[1] = 0;
+    }
+    __syncthreads();
+    int cur = 0;
+    for (uint32_t level = 0; level <= quads; ++level) {
+      uint32_t size = s_count[cur];
+      if (size == 0) break;
+      if (size > quads) size = quads;
+      const uint2* qin = p.queue[cur] + base;
+      uint2* qout = p.queue[cur ^ 1] + base;
+      for (uint32_t k = threadIdx.x; k < size; k += kBlock) {
+        const uint2 item = qin[k];
+        emit_quad(p.c, item.x, item.y, qout, &s_count[cur ^ 1]);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) s_count[cur] = 0;
+      __syncthreads();
+      cur ^= 1;
+    }
+    __syncthreads();
+  }
+}
+
 // Bvh::refit (src/bvh.rs:176-205): leaf box = union of its primitives'
 // boxes + 1e-4, interior box = union of the two children + 1e-4, computed
 // bottom-up (the second child to arrive finishes the parent). Unions are
@@ -407,6 +479,43 @@ ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* 
   k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent, arrive, status);
   k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, prim_count, aabbs, parent, arrive, status);
   return cuda_rc(cudaGetLastError());
+}
+
+}  // namespace rtbvh
+
+namespace rtbvh {
+
+cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, const uint32_t* prim_off,
+                                     const uint32_t* order, uint32_t mesh_count, uint32_t* parent, uint32_t* arrive,
+                                     uint32_t* cnt_e, uint32_t* cnt_o, uint32_t* mbase, uint2* q0, uint2* q1,
+                                     DMNode* mnodes, uint32_t m_capacity, uint32_t* status, unsigned blocks,
+                                     cudaStream_t s) {
+  if (node_count == 0 || mesh_count == 0) return cudaSuccess;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(parent, 0xff, (size_t)node_count * 4, s))) return e;
+  const unsigned nb = (node_count + kBlock - 1) / kBlock;
+  k_parents<<<nb, kBlock, 0, s>>>(nodes, node_count, parent, arrive, status);
+  k_counts_bottom_up<<<nb, kBlock, 0, s>>>(nodes, node_count, parent, arrive, cnt_e, cnt_o);
+  k_seg_mbase<<<1, 1024, 0, s>>>(nodes, cnt_e, prim_off, mesh_count, mbase);
+  SegCollapseParams p;
+  p.c.nodes = nodes;
+  p.c.node_count = node_count;
+  p.c.cnt_e = cnt_e;
+  p.c.mnodes = mnodes;
+  p.c.m_total = m_capacity;
+  p.c.queue[0] = q0;
+  p.c.queue[1] = q1;
+  p.c.qcount = nullptr;
+  p.c.bar = nullptr;
+  p.c.status = status;
+  p.prim_off = prim_off;
+  p.order = order;
+  p.mbase = mbase;
+  p.queue[0] = q0;
+  p.queue[1] = q1;
+  p.mesh_count = mesh_count;
+  k_collapse_segments<<<blocks, kBlock, 0, s>>>(p);
+  return cudaGetLastError();
 }
 
 }  // namespace rtbvh

@@ -205,6 +205,25 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
       sp = -1;
       next = 0;
       active = true;
+      if (a.seg_count) {
+        uint32_t lo = 0, hi = a.seg_count;  // mesh with seg_ray_off[m] <= r < seg_ray_off[m + 1]
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if ((size_t)__ldg(a.seg_ray_off + mid) <= r) lo = mid;
+          else hi = mid;
+        }
+        const uint32_t root = __ldg(a.seg_root + lo);
+        if (root == __ldg(a.seg_root + lo + 1)) {
+          active = false;
+          a.hits[r] = make_float4(ray.t, 0.0f, 0.0f, __int_as_float(-1));
+          if (STATS) {
+            a.stats[3 * r + 0] = 0;
+            a.stats[3 * r + 1] = 0;
+            a.stats[3 * r + 2] = 0;
+          }
+        }
+        next = (int32_t)root;
+      }
     }
   };
   for (;;) {

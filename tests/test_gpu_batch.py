@@ -1,0 +1,103 @@
+"""GPU parity: many meshes built and traced in one captured pipeline
+(rtbvh_gpu_batch_*) against the same meshes built and traced one by one.
+Per mesh, nodes, primitive order, quad nodes and hits must be the
+single-mesh results with indices shifted by the mesh's offsets."""
+import numpy as np
+import pytest
+import torch
+
+import rtbvh_gb300 as rb
+from rtbvh_gb300 import scenes
+from gpu_helpers import gpu_build, to_cuda, u32
+
+pytestmark = pytest.mark.gpu
+
+
+def make_meshes(sizes, seed=0):
+    tris, rays, po, ro = [], [], [0], [0]
+    for i, n in enumerate(sizes):
+        t = scenes.incoherent(n, seed=seed * 1000 + i)
+        t = (t * np.float32(0.5 + 0.1 * i)).astype(np.float32)  # different world boxes per mesh
+        r, _ = scenes.incoherent_rays(max(64, int(round(20 * np.sqrt(n)))), seed=seed * 1000 + 500 + i,
+                                      center=tuple(0.25 * (1 + 0.1 * i) * np.ones(3)), radius=1.5)
+        tris.append(t)
+        rays.append(r)
+        po.append(po[-1] + n)
+        ro.append(ro[-1] + len(r))
+    return np.concatenate(tris), np.concatenate(rays), po, ro
+
+
+def shifted_nodes(nodes, nbase, off):
+    out = nodes.copy()
+    ints = out.view(np.int32)
+    leaf = ints[:, 3] >= 0
+    ints[leaf, 7] += off
+    ints[~leaf, 7] += nbase
+    return out
+
+
+def shifted_quads(q, mbase, off):
+    out = q.copy()
+    ints = out.view(np.int32)
+    ch, cnt = ints[:, 24:28], ints[:, 28:32]
+    leaf = cnt >= 0
+    inner = (cnt < 0) & (ch >= 0)
+    ch[leaf] += off
+    ch[inner] += mbase
+    return out
+
+
+@pytest.mark.parametrize("sizes", [[1, 2, 3, 17, 300, 5000, 2, 40000, 1, 900, 64, 12000],
+                                   [2049, 2048, 2047, 4096, 33, 7]])
+def test_batch_matches_single_mesh_builds(lib, sizes):
+    torch.cuda.set_device(0)
+    tris, rays, po, ro = make_meshes(sizes, seed=len(sizes))
+    batch = rb.Batch(to_cuda(tris), po, to_cuda(rays), ro)
+    hits = batch.run().cpu().numpy()
+    assert batch.status() == rb.ResultCode.Ok
+    v = batch.view()
+    M = len(sizes)
+    nodes = rb.device_copy(v.nodes, (v.node_capacity, 8))
+    idx = rb.device_copy(v.indices, (po[-1],), np.uint32)
+    mbase = rb.device_copy(v.mnode_base, (M + 1,), np.uint32)
+    quads = rb.device_copy(v.mnodes, (int(mbase[-1]), 32))
+    for m, n in enumerate(sizes):
+        off, nbase = po[m], 2 * po[m] - m
+        g = gpu_build(tris[off:off + n], "locb")
+        gn = g.nodes()
+        assert np.array_equal(u32(nodes[nbase:nbase + len(gn)]), u32(shifted_nodes(gn, nbase, off))), m
+        assert np.array_equal(idx[off:off + n], g.indices() + off), m
+        gm = rb.Mbvh.construct(g)
+        gq = gm.quad_nodes()
+        assert mbase[m + 1] - mbase[m] == len(gq), m
+        assert np.array_equal(u32(quads[mbase[m]:mbase[m + 1]]), u32(shifted_quads(gq, mbase[m], off))), m
+        h1, _ = gm.intersect(to_cuda(rays[ro[m]:ro[m + 1]]))
+        h1 = h1.cpu().numpy()
+        hb = hits[ro[m]:ro[m + 1]]
+        assert np.array_equal(u32(hb[:, :3]), u32(h1[:, :3])), m
+        p1 = rb.hit_prims(h1)
+        assert np.array_equal(rb.hit_prims(hb), np.where(p1 >= 0, p1 + off, p1)), m
+
+
+def test_batch_graph_replay_and_uncaptured_agree(lib):
+    torch.cuda.set_device(0)
+    tris, rays, po, ro = make_meshes([500, 3000, 40, 8000, 2], seed=3)
+    d_tris = to_cuda(tris)
+    batch = rb.Batch(d_tris, po, to_cuda(rays), ro)
+    a = batch.run().clone()
+    b = batch.run().clone()
+    c = batch.run(graph=False).clone()
+    torch.cuda.synchronize()
+    assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    assert torch.equal(a.view(torch.int32), c.view(torch.int32))
+    # the graph reads the bound vertex buffer: moving the geometry in place changes the result
+    d_tris.mul_(1.5)
+    d = batch.run().clone()
+    torch.cuda.synchronize()
+    assert not torch.equal(a.view(torch.int32), d.view(torch.int32))
+
+
+def test_batch_rejects_empty_meshes(lib):
+    tris, rays, po, ro = make_meshes([10, 20], seed=4)
+    with pytest.raises(rb.RtbvhError):
+        rb.Batch(to_cuda(tris), [0, 10, 10, 30], to_cuda(rays), [0, ro[1], ro[1], ro[2]])
