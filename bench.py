@@ -21,6 +21,7 @@ the slowest rank's time.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -251,6 +252,7 @@ def run_gpu(args):
         workloads["sphere_6400_binned_sah"] = workload_sphere_sah(not args.no_cpu_baseline)
         workloads["differentiable_200k"] = workload_differentiable()
         workloads["batched_512_meshes"] = workload_batched()
+        workloads["clustered_10M_binned_sah"] = workload_clustered()
 
     if rank == 0:
         line = {
@@ -393,6 +395,90 @@ def workload_differentiable():
             "plain": "same trace, then the triangle test recomputed and differentiated by PyTorch autograd"}
 
 
+def secondary_rays(rays, hits, vertices, per_hit=3, total_hits=None, seed=9):
+    """Cosine-weighted hemisphere rays at closest-hit points: origin = hit
+    point + 1e-4 * geometric normal (facing the incoming ray), ``per_hit``
+    directions per hit point. Hit points are cycled until ``total_hits``
+    points are used (default: one per primary ray)."""
+    import torch
+    R = rays.shape[0]
+    total_hits = total_hits or R
+    prim = hits[:, 3].contiguous().view(torch.int32)
+    hit_idx = torch.nonzero(prim >= 0).squeeze(1)
+    if hit_idx.numel() == 0:
+        raise RuntimeError("no primary hits to spawn secondary rays from")
+    slots = hit_idx[torch.arange(total_hits, device=rays.device) % hit_idx.numel()]
+    d = rays[slots, 3:]
+    p = rays[slots, :3] + hits[slots, 0:1] * d
+    tri = vertices.reshape(-1, 3, 3)[prim[slots].long()]
+    n = torch.linalg.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    n = n / n.norm(dim=1, keepdim=True).clamp_min(1e-30)
+    n = torch.where(((n * d).sum(1, keepdim=True) > 0), -n, n)
+    origin = p + 1e-4 * n
+    # orthonormal frame around n
+    a = torch.where(n[:, 0:1].abs() > 0.9, torch.tensor([0.0, 1.0, 0.0], device=rays.device),
+                    torch.tensor([1.0, 0.0, 0.0], device=rays.device))
+    t1 = torch.linalg.cross(n, a)
+    t1 = t1 / t1.norm(dim=1, keepdim=True)
+    t2 = torch.linalg.cross(n, t1)
+    g = torch.Generator(device=rays.device)
+    g.manual_seed(seed)
+    out = []
+    for _ in range(per_hit):
+        u1 = torch.rand(total_hits, 1, device=rays.device, generator=g)
+        u2 = torch.rand(total_hits, 1, device=rays.device, generator=g)
+        r, phi = torch.sqrt(u1), 2.0 * math.pi * u2
+        w = r * torch.cos(phi) * t1 + r * torch.sin(phi) * t2 + torch.sqrt((1.0 - u1).clamp_min(0.0)) * n
+        w = w / w.norm(dim=1, keepdim=True)
+        out.append(torch.cat([origin, w], dim=1))
+    return torch.stack(out, dim=1).reshape(-1, 6).contiguous()
+
+
+def workload_clustered(with_stats=True):
+    """64 spheres (10,000,000 triangles, radii log-uniform in [0.01, 0.2],
+    Gaussian-mixture centres), binned SAH + MBVH; 4096x4096 camera rays plus
+    3 cosine-weighted secondary rays per primary hit point (64M rays)."""
+    import torch
+
+    import rtbvh_gb300 as rb
+    from rtbvh_gb300 import scenes
+    tris = scenes.clustered(10_000_000)
+    d_tris = torch.from_numpy(tris).cuda()
+    del tris
+    sah_ms = _cuda_time(lambda: rb.Builder(primitives=rb.Triangles(d_tris)).construct_binned_sah(host_mirror=False),
+                        reps=2, warmup=1)
+    bvh = rb.Builder(primitives=rb.Triangles(d_tris)).construct_binned_sah(host_mirror=False)
+    mbvh_ms = _cuda_time(lambda: rb.Mbvh.construct(bvh, host_mirror=False), reps=3, warmup=1)
+    m = rb.Mbvh.construct(bvh, host_mirror=False)
+    primary = torch.from_numpy(scenes.camera_rays(4096, 4096)).cuda()
+    ph, _ = m.intersect(primary)
+    primary_hits = int((ph[:, 3].contiguous().view(torch.int32) >= 0).sum())
+    sec = secondary_rays(primary, ph, d_tris, per_hit=3)
+    del ph
+    allr = torch.cat([primary, sec])
+    del sec
+    R = allr.shape[0]
+    ms = _cuda_time(lambda: m.intersect(allr), reps=3, warmup=2)
+    sec_ms = _cuda_time(lambda: m.intersect(allr[primary.shape[0]:]), reps=3, warmup=1)
+    out = {"triangles": int(d_tris.shape[0]), "rays": int(R), "primary_hits": primary_hits,
+           "sah_build_ms": round(sah_ms, 2), "mbvh_ms": round(mbvh_ms, 2),
+           "closest_hit_mrays": round(R / (ms * 1e-3) / 1e6, 1),
+           "secondary_only_mrays": round((R - primary.shape[0]) / (sec_ms * 1e-3) / 1e6, 1)}
+    if with_stats:
+        _, st = m.intersect(allr, stats=True)
+        st = st.to(torch.int64)
+        nv, nt = float(st[:, 0].sum()) / R, float(st[:, 1].sum()) / R
+        bpr = B_IN + B_OUT + B_NODE * nv + B_TRI * nt
+        peak, kind = measured_peak()
+        ach = bpr * R / (ms * 1e-3) / 1e9
+        out["roofline"] = {"bytes_per_ray": round(bpr, 1), "mean_node_visits": round(nv, 3),
+                           "mean_tri_tests": round(nt, 3), "achieved_gbs": round(ach, 1),
+                           "frac": round(ach / peak, 3), "peak_source": kind}
+    if m.status() != rb.ResultCode.Ok:
+        raise RuntimeError("clustered traversal reported an error")
+    return out
+
+
 def workload_batched(mesh_count=512, seed=44):
     """512 perturbed spheres, triangle counts log-uniform in [64, 200,000],
     round(2000 sqrt(n)) incoherent rays each: one captured build + trace for
@@ -413,7 +499,8 @@ def workload_batched(mesh_count=512, seed=44):
         centre = tuple(rng.uniform(-5, 5, size=3))
         t = scenes.sphere_fast(n_lon, n_lat, radius=1.0, noise=0.05, seed=seed * 10000 + m, center=centre)
         r, _ = scenes.incoherent_rays(int(round(2000 * math.sqrt(len(t)))), seed=seed * 10000 + 5000 + m,
-                                      center=centre, radius=2.0, lo=-1.0, hi=1.0)
+                                      center=(0.0, 0.0, 0.0), radius=2.0, lo=-1.0, hi=1.0)
+        r[:, :3] += np.asarray(centre, dtype=np.float32)  # origins and targets move with the mesh
         parts.append(t)
         rays.append(r)
         po.append(po[-1] + len(t))

@@ -384,18 +384,21 @@ class Batch:
 
 
 class DeviceArray:
-    """Zero-copy view of library-owned device memory (for torch.as_tensor)."""
+    """Zero-copy view of library-owned device memory (for torch.as_tensor).
+    torch accepts only writable views; callers must not write through it."""
 
     def __init__(self, ptr, shape, typestr="<f4"):
-        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), True),
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
                                          "version": 3}
 
 
 def device_copy(ptr, shape, dtype=np.float32):
-    """Host numpy copy of library-owned device memory."""
-    typestr = {np.float32: "<f4", np.uint32: "<u4", np.int32: "<i4"}[dtype]
-    t = torch.as_tensor(DeviceArray(ptr, shape, typestr), device="cuda")
-    return t.clone().cpu().numpy()
+    """Host numpy copy of library-owned device memory (4-byte element types)."""
+    dtype = np.dtype(dtype)
+    if dtype.itemsize != 4:
+        raise ValueError("device_copy handles 4-byte element types")
+    t = torch.as_tensor(DeviceArray(ptr, shape, "<i4"), device="cuda")
+    return t.clone().cpu().numpy().view(dtype)
 
 
 def hit_prims(hits):

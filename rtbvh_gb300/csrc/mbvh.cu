@@ -244,8 +244,31 @@ __global__ void __launch_bounds__(kBlock) k_collapse_segments(SegCollapseParams 
     if (n == 0) continue;
     const uint32_t base = p.mbase[m];
     const uint32_t quads = p.mbase[m + 1] - base;
+    const uint32_t root = 2u * off - m;
+    const DAabb rb = load_aabb(p.c.nodes + root);
+    if (rb.count >= 0) {
+      // Root leaf (n <= 2): the single-mesh tree has this one node, so
+      // merge_nodes finds only the root itself in slot 0. emit_quad would
+      // read the next mesh's nodes as the root's second child here.
+      if (threadIdx.x == 0 && quads >= 1) {
+        DMNode q;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          set_slot_box(q, i, rb);
+          q.children[i] = -1;
+          q.counts[i] = -1;
+        }
+        q.children[0] = rb.left_first;
+        q.counts[0] = rb.count;
+        float4* dst = reinterpret_cast<float4*>(p.c.mnodes + base);
+        const float4* src = reinterpret_cast<const float4*>(&q);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k] = src[k];
+      }
+      continue;
+    }
     if (threadIdx.x == 0) {
-      p.queue[0][base] = make_uint2(2u * off - m, base);
+      p.queue[0][base] = make_uint2(root, base);
       s_count[0] = 1;
       s_count[1] = 0;
     }
