@@ -6,7 +6,8 @@
 //   2. Morton codes against each mesh's own world box, then a stable sort by
 //      code followed by a stable sort by mesh id: (mesh, code) order, i.e.
 //      every mesh's own MortonEncoder::get_sorted_indices order;
-//   3. one block per mesh runs the clustering levels (locb.cu);
+//   3. the clustering levels (locb.cu): a thread-block cluster per large
+//      mesh, one block per small mesh, the two sets concurrently;
 //   4. parent pointers and quad-subtree counts over the whole forest, then
 //      one block per mesh for the top-down MBVH collapse (mbvh.cu);
 //   5. leaf-ordered triangles and ONE persistent traversal launch for all
@@ -146,11 +147,20 @@ struct Plan {
   DevBuf<uint2> q0, q1;
   DevBuf<char> sort_temp;
   size_t sort_bytes = 0;
+  // meshes order[0, big_count) get a thread-block cluster each (locb.cu)
+  uint32_t big_count = 0;
+  unsigned clusters = 0;
+  DevBuf<uint32_t> cluster_sums;
+  cudaStream_t side = nullptr;  // small meshes' clustering runs here, forked from the main stream
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   ~Plan() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (side) cudaStreamDestroy(side);
   }
 };
 
@@ -178,7 +188,8 @@ cudaError_t run_pipeline(Plan& p, cudaStream_t s) {
     return e;
   if ((e = cudaMemsetAsync(p.nodes.ptr, 0xff, (size_t)p.node_cap * sizeof(DAabb), s))) return e;
   if ((e = launch_locb_segments(p.aabbs.ptr, p.vals.ptr, p.vals.ptr, p.prim_off.ptr, p.order.ptr, p.worlds.ptr, M, N,
-                                p.lvl0.ptr, p.lvl1.ptr, p.nodes.ptr, p.nb.ptr, p.status.ptr, mesh_blocks(M), s)))
+                                p.lvl0.ptr, p.lvl1.ptr, p.nodes.ptr, p.nb.ptr, p.status.ptr, mesh_blocks(M),
+                                p.big_count, p.cluster_sums.ptr, p.clusters, s, p.side, p.fork, p.join)))
     return e;
   if ((e = launch_collapse_segments(p.nodes.ptr, p.node_cap, p.prim_off.ptr, p.order.ptr, M, p.parent.ptr,
                                     p.arrive.ptr, p.cnt_e.ptr, p.cnt_o.ptr, p.mbase.ptr, p.q0.ptr, p.q1.ptr,
@@ -248,7 +259,18 @@ ResultCode rtbvh_gpu_batch_create(const float* vertices, const uint32_t* prim_of
     return prim_offsets[a + 1] - prim_offsets[a] > prim_offsets[b + 1] - prim_offsets[b];
   });
   p->sort_bytes = radix_sort_temp_bytes(N);
+  while (p->big_count < mesh_count) {
+    const uint32_t m = order[p->big_count];
+    if (prim_offsets[m + 1] - prim_offsets[m] <= kSegClusterMinPrims) break;
+    ++p->big_count;
+  }
+  p->clusters = std::min<uint32_t>(p->big_count, 8192u);
   cudaError_t e;
+  if ((e = p->cluster_sums.alloc((size_t)kSegCluster * p->clusters)) ||
+      (e = cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking)) ||
+      (e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming)) ||
+      (e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming)))
+    return cuda_rc(e);
   if ((e = p->prim_off.alloc(mesh_count + 1)) || (e = p->ray_off.alloc(mesh_count + 1)) ||
       (e = p->order.alloc(mesh_count)) || (e = p->keys.alloc(N)) || (e = p->vals.alloc(N)) ||
       (e = p->nb.alloc(p->node_cap)) || (e = p->parent.alloc(p->node_cap)) || (e = p->arrive.alloc(p->node_cap)) ||

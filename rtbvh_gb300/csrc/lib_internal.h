@@ -116,11 +116,19 @@ cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
 
 // ------------------------------------------------------------------ many meshes
 // Per-mesh clustering of a concatenated forest (see locb.cu).
+// Meshes order[0, big_count) (the largest, more than kSegClusterMinPrims
+// primitives) are clustered by `clusters` thread-block clusters of
+// kSegCluster blocks (cluster_sums: kSegCluster words per cluster); the rest
+// by up to `blocks` single blocks, on `side` (between the events fork and
+// join) when it is given.
+constexpr uint32_t kSegCluster = 8;
+constexpr uint32_t kSegClusterMinPrims = 4096;
 cudaError_t launch_locb_segments(const DAabb* aabbs, const uint32_t* sorted, uint32_t* indices,
                                  const uint32_t* prim_off, const uint32_t* order, const DAabb* worlds,
                                  uint32_t mesh_count, uint32_t total_prims, DAabb* lvl0, DAabb* lvl1,
                                  DAabb* final_nodes, uint32_t* nb, uint32_t* status, unsigned blocks,
-                                 cudaStream_t s);
+                                 uint32_t big_count, uint32_t* cluster_sums, unsigned clusters, cudaStream_t s,
+                                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join);
 // Per-mesh MBVH collapse of a concatenated forest (see mbvh.cu).
 cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, const uint32_t* prim_off,
                                      const uint32_t* order, uint32_t mesh_count, uint32_t* parent, uint32_t* arrive,

@@ -15,6 +15,7 @@
 // Node positions follow the reference exactly (locb.rs:178-215), so the
 // output is bit-identical to the reference's node array. Levels of at most
 // kTailNodes nodes are finished by block 0 alone with block barriers.
+#include <algorithm>
 #include <cstdio>
 
 #include "lib_internal.h"
@@ -293,11 +294,11 @@ struct SegParams {
   uint32_t mesh_count;
 };
 
-__global__ void __launch_bounds__(kBlock) k_locb_segments(SegParams p) {
+__global__ void __launch_bounds__(kBlock) k_locb_segments(SegParams p, uint32_t first) {
   __shared__ SBox s_box[kBlock + 2 * kRadius];
   __shared__ uint32_t s_flag[kBlock + kRadius];
   __shared__ uint32_t s_warp[kBlock / 32];
-  for (uint32_t q = blockIdx.x; q < p.mesh_count; q += gridDim.x) {
+  for (uint32_t q = first + blockIdx.x; q < p.mesh_count; q += gridDim.x) {
     const uint32_t m = p.order[q];
     const uint32_t off = p.prim_off[m], n = p.prim_off[m + 1] - off;
     if (n == 0) continue;
@@ -316,6 +317,76 @@ __global__ void __launch_bounds__(kBlock) k_locb_segments(SegParams p) {
     int cur = 0;
     if (!locb_block_finish(p.lvl, p.final_nodes, p.nb, begin, end, cur, levels, s_box, s_flag, s_warp, p.status))
       return;
+  }
+}
+
+// Large meshes: a cluster of kSegCluster blocks per mesh runs the wide
+// levels of k_locb_levels (tiles and chunks split over the cluster's
+// blocks, hardware cluster barriers between the phases) and block rank 0
+// finishes the last kTailNodes nodes alone. Every block of a cluster runs
+// the same mesh sequence and the same level count (all loop bounds are
+// computed from values every block reads identically), so each barrier is
+// reached by all of them; nothing waits on another cluster.
+__device__ __forceinline__ void cluster_barrier() {
+  __threadfence();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__global__ void __cluster_dims__(kSegCluster, 1, 1) __launch_bounds__(kBlock)
+    k_locb_segments_cluster(SegParams p, uint32_t* cluster_sums, uint32_t big_count) {
+  __shared__ SBox s_box[kBlock + 2 * kRadius];
+  __shared__ uint32_t s_flag[kBlock + kRadius];
+  __shared__ uint32_t s_warp[kBlock / 32];
+  const uint32_t rank = blockIdx.x % kSegCluster;  // 1-D clusters of consecutive blocks
+  const uint32_t cid = blockIdx.x / kSegCluster, ncl = gridDim.x / kSegCluster;
+  uint32_t* sums = cluster_sums + (size_t)cid * kSegCluster;
+  for (uint32_t q = cid; q < big_count; q += ncl) {
+    const uint32_t m = p.order[q];
+    const uint32_t off = p.prim_off[m], n = p.prim_off[m + 1] - off;
+    if (n <= 2) continue;  // the host sends only meshes above kSegClusterMinPrims
+    const uint32_t nbase = 2u * off - m;
+    uint32_t begin = nbase + n - 1u, end = nbase + 2u * n - 1u, levels = 0;
+    int cur = 0;
+    bool ok = true;
+    while (end - begin > kTailNodes) {
+      const uint32_t count = end - begin;
+      const DAabb* in = p.lvl[cur];
+      DAabb* out = p.lvl[cur ^ 1];
+      for (uint32_t tile = rank; (size_t)tile * kBlock < count; tile += kSegCluster)
+        nn_tile(in, p.nb, begin, end, begin + tile * kBlock, s_box, p.status);
+      cluster_barrier();
+      const uint32_t chunk = (count + kSegCluster - 1) / kSegCluster;
+      const uint32_t c0 = min(begin + rank * chunk, end);
+      const uint32_t c1 = min(c0 + chunk, end);
+      uint32_t local = 0;
+      for (uint32_t i = c0 + threadIdx.x; i < c1; i += kBlock) local += merge_flag(p.nb, i);
+      uint32_t tot;
+      block_inclusive_scan<kBlock>(local, s_warp, &tot);
+      if (threadIdx.x == 0) sums[rank] = tot;
+      cluster_barrier();
+      uint32_t pre = 0, mc = 0;
+#pragma unroll
+      for (uint32_t b = 0; b < kSegCluster; ++b) {
+        const uint32_t v = __ldcg(sums + b);
+        mc += v;
+        if (b < rank) pre += v;
+      }
+      if (mc == 0) {  // same value in every block of the cluster
+        if (rank == 0 && threadIdx.x == 0) atomicOr(p.status, kStatusNoMerge);
+        ok = false;
+        break;
+      }
+      uint32_t carry = pre;
+      for (uint32_t s0 = c0; s0 < c1; s0 += kBlock)
+        carry = scatter_tile(in, out, p.final_nodes, p.nb, begin, end, s0, c1, carry, mc, s_flag, s_warp, p.status);
+      cluster_barrier();
+      begin -= mc;
+      end -= 2u * mc;
+      cur ^= 1;
+      ++levels;
+    }
+    if (ok && rank == 0)
+      locb_block_finish(p.lvl, p.final_nodes, p.nb, begin, end, cur, levels, s_box, s_flag, s_warp, p.status);
   }
 }
 
@@ -441,8 +512,12 @@ cudaError_t launch_locb_segments(const DAabb* aabbs, const uint32_t* sorted, uin
                                  const uint32_t* prim_off, const uint32_t* order, const DAabb* worlds,
                                  uint32_t mesh_count, uint32_t total_prims, DAabb* lvl0, DAabb* lvl1,
                                  DAabb* final_nodes, uint32_t* nb, uint32_t* status, unsigned blocks,
-                                 cudaStream_t s) {
+                                 uint32_t big_count, uint32_t* cluster_sums, unsigned clusters, cudaStream_t s,
+                                 cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
   if (total_prims == 0 || mesh_count == 0) return cudaSuccess;
+  if (big_count > mesh_count || (big_count > 0 && (clusters == 0 || cluster_sums == nullptr)))
+    return cudaErrorInvalidValue;
+  cudaError_t e;
   k_locb_segment_leaves<<<(total_prims + kBlock - 1) / kBlock, kBlock, 0, s>>>(aabbs, sorted, prim_off, mesh_count,
                                                                                 total_prims, lvl0);
   SegParams p;
@@ -456,8 +531,27 @@ cudaError_t launch_locb_segments(const DAabb* aabbs, const uint32_t* sorted, uin
   p.indices = indices;
   p.status = status;
   p.mesh_count = mesh_count;
-  k_locb_segments<<<blocks, kBlock, 0, s>>>(p);
-  return cudaGetLastError();
+  // small meshes (one block each) on the side stream, concurrently with the
+  // clusters of the large ones; the two sets of meshes share no memory
+  const bool fork_side = side != nullptr && big_count > 0 && big_count < mesh_count;
+  cudaStream_t small_s = s;
+  if (fork_side) {
+    if ((e = cudaEventRecord(fork, s)) || (e = cudaStreamWaitEvent(side, fork, 0))) return e;
+    small_s = side;
+  }
+  if (big_count < mesh_count) {
+    const unsigned nb_small = std::min<unsigned>(blocks, mesh_count - big_count);
+    k_locb_segments<<<nb_small, kBlock, 0, small_s>>>(p, big_count);
+    if ((e = cudaGetLastError())) return e;
+  }
+  if (big_count > 0) {
+    k_locb_segments_cluster<<<clusters * kSegCluster, kBlock, 0, s>>>(p, cluster_sums, big_count);
+    if ((e = cudaGetLastError())) return e;
+  }
+  if (fork_side) {
+    if ((e = cudaEventRecord(join, side)) || (e = cudaStreamWaitEvent(s, join, 0))) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace rtbvh

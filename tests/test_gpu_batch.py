@@ -48,7 +48,8 @@ def shifted_quads(q, mbase, off):
 
 
 @pytest.mark.parametrize("sizes", [[1, 2, 3, 17, 300, 5000, 2, 40000, 1, 900, 64, 12000],
-                                   [2049, 2048, 2047, 4096, 33, 7]])
+                                   [2049, 2048, 2047, 4096, 33, 7],
+                                   [4097, 8193, 65537, 3, 100000, 6000, 4096]])
 def test_batch_matches_single_mesh_builds(lib, sizes):
     torch.cuda.set_device(0)
     tris, rays, po, ro = make_meshes(sizes, seed=len(sizes))
