@@ -509,6 +509,8 @@ def workload_batched(mesh_count=512, seed=44):
     allr = np.concatenate(rays)
     d_tris, d_rays = torch.from_numpy(tris).cuda(), torch.from_numpy(allr).cuda()
     batch = rb.Batch(d_tris, po, d_rays, ro)
+    default_ms = _cuda_time(lambda: batch.run(), reps=5, warmup=1)
+    tuning = batch.tune()
     graph_ms = _cuda_time(lambda: batch.run(), reps=5, warmup=1)
     eager_ms = _cuda_time(lambda: batch.run(graph=False), reps=3, warmup=1)
     if batch.status() != rb.ResultCode.Ok:
@@ -527,7 +529,9 @@ def workload_batched(mesh_count=512, seed=44):
     torch.cuda.synchronize()
     loop_ms = (time.perf_counter() - t0) * 1e3
     return {"meshes": mesh_count, "triangles": int(po[-1]), "rays": int(ro[-1]),
-            "graph_build_trace_ms": round(graph_ms, 2), "uncaptured_build_trace_ms": round(eager_ms, 2),
+            "graph_build_trace_ms": round(graph_ms, 2), "untuned_graph_ms": round(default_ms, 2),
+            "tuning": {k: (round(v, 2) if isinstance(v, float) else v) for k, v in tuning.items()},
+            "uncaptured_build_trace_ms": round(eager_ms, 2),
             "per_mesh_loop_ms": round(loop_ms, 2), "speedup_vs_per_mesh_loop": round(loop_ms / graph_ms, 2),
             "mrays_including_build": round(ro[-1] / (graph_ms * 1e-3) / 1e6, 1)}
 

@@ -272,7 +272,8 @@ ResultCode rtbvh_gpu_intersect_backward(const float *vertices, uintptr_t prim_co
  * and its rays are traced against it; hit prim ids are indices into the
  * concatenated triangles. All meshes share one set of launches: a stable
  * (mesh, Morton) sort, one block per mesh for the clustering and the
- * collapse, and one persistent traversal launch. create() allocates every
+ * collapse (a thread-block cluster per large mesh for the clustering), and
+ * one persistent traversal launch. create() allocates every
  * buffer and captures the whole pipeline in a CUDA graph; run() replays it
  * on the same device buffers (update their contents in place between runs).
  * prim_offsets / ray_offsets are host arrays of mesh_count + 1 entries. */
@@ -302,6 +303,22 @@ ResultCode rtbvh_gpu_batch_view(RTBatch batch, RTGpuBatchView *view);
 /* Reads and clears the device status of the last runs (synchronises). */
 ResultCode rtbvh_gpu_batch_status(RTBatch batch);
 void rtbvh_gpu_batch_free(RTBatch batch);
+
+/* Launch parameters of a batch; 0 in a field means the default. */
+typedef struct RTBatchTuning {
+  uint32_t trace_blocks_per_sm; /* resident traversal blocks per SM (default: occupancy limit) */
+  uint32_t trace_ray_batch;     /* rays a warp takes from the global ray counter at a time (default 128) */
+  uint32_t cluster_min_prims;   /* meshes with more primitives get a thread-block cluster (default 4096) */
+  float pipeline_ms;            /* tune: measured build + trace time with the chosen values */
+} RTBatchTuning;
+/* Times candidate values on this batch's own meshes and rays (the pipeline
+ * runs several times on `stream`, overwriting the hits), keeps the fastest
+ * and re-captures the graph with it; `result` (may be NULL) receives it.
+ * Results do not depend on these parameters. Synchronises. */
+ResultCode rtbvh_gpu_batch_tune(RTBatch batch, rtbvh_stream_t stream, RTBatchTuning *result);
+/* Reads (get) or sets and re-captures (set) the parameters. */
+ResultCode rtbvh_gpu_batch_get_tuning(RTBatch batch, RTBatchTuning *result);
+ResultCode rtbvh_gpu_batch_set_tuning(RTBatch batch, const RTBatchTuning *tuning, rtbvh_stream_t stream);
 
 /* Library version string. */
 const char *rtbvh_gpu_version(void);

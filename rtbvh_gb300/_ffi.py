@@ -73,6 +73,11 @@ class RTGpuBatchView(ctypes.Structure):
                 ("mesh_count", ctypes.c_uint32), ("leaf_triangles", ctypes.c_void_p)]
 
 
+class RTBatchTuning(ctypes.Structure):
+    _fields_ = [("trace_blocks_per_sm", ctypes.c_uint32), ("trace_ray_batch", ctypes.c_uint32),
+                ("cluster_min_prims", ctypes.c_uint32), ("pipeline_ms", ctypes.c_float)]
+
+
 class RTGpuView(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_void_p), ("node_count", ctypes.c_uint32),
                 ("indices", ctypes.c_void_p), ("index_count", ctypes.c_uint32),
@@ -116,6 +121,9 @@ SIGNATURES = {
     "rtbvh_gpu_batch_view": (_rc, [RTBatch, ctypes.POINTER(RTGpuBatchView)]),
     "rtbvh_gpu_batch_status": (_rc, [RTBatch]),
     "rtbvh_gpu_batch_free": (None, [RTBatch]),
+    "rtbvh_gpu_batch_tune": (_rc, [RTBatch, _vp, ctypes.POINTER(RTBatchTuning)]),
+    "rtbvh_gpu_batch_get_tuning": (_rc, [RTBatch, ctypes.POINTER(RTBatchTuning)]),
+    "rtbvh_gpu_batch_set_tuning": (_rc, [RTBatch, ctypes.POINTER(RTBatchTuning), _vp]),
     "rtbvh_gpu_version": (ctypes.c_char_p, []),
 }
 

@@ -151,6 +151,9 @@ struct Plan {
   uint32_t big_count = 0;
   unsigned clusters = 0;
   DevBuf<uint32_t> cluster_sums;
+  std::vector<uint32_t> sizes_in_order;  // host: primitive count of order[q]
+  // launch parameters (RTBatchTuning; 0 = default)
+  uint32_t trace_blocks_per_sm = 0, trace_ray_batch = 0, cluster_min = kSegClusterMinPrims;
   cudaStream_t side = nullptr;  // small meshes' clustering runs here, forked from the main stream
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -167,12 +170,24 @@ struct Plan {
 std::mutex g_plans_mu;
 std::vector<std::unique_ptr<Plan>> g_plans;
 
+constexpr uint32_t kMaxClusters = 8192;
+
+// Meshes above `min_prims` primitives (a prefix of the size-ordered mesh
+// list) are clustered by block clusters; meshes of at most 2 primitives
+// always take the single-block path.
+void set_cluster_min(Plan& p, uint32_t min_prims) {
+  p.cluster_min = min_prims < 2u ? 2u : min_prims;
+  p.big_count = 0;
+  while (p.big_count < p.mesh_count && p.sizes_in_order[p.big_count] > p.cluster_min) ++p.big_count;
+  p.clusters = std::min<uint32_t>(p.big_count, kMaxClusters);
+}
+
 unsigned mesh_blocks(uint32_t mesh_count) {
   const unsigned cap = (unsigned)sm_count() * 4u;
   return mesh_count < cap ? mesh_count : cap;
 }
 
-cudaError_t run_pipeline(Plan& p, cudaStream_t s) {
+cudaError_t run_build(Plan& p, cudaStream_t s) {
   cudaError_t e;
   const uint32_t N = p.total_prims, M = p.mesh_count;
   const unsigned gN = (N + kBlock - 1) / kBlock;
@@ -196,6 +211,12 @@ cudaError_t run_pipeline(Plan& p, cudaStream_t s) {
                                     p.mnodes.ptr, p.node_cap, p.status.ptr, mesh_blocks(M), s)))
     return e;
   if ((e = launch_gather_triangles(p.vertices, p.vals.ptr, N, p.tris.ptr, s))) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t run_trace(Plan& p, cudaStream_t s) {
+  cudaError_t e;
+  const uint32_t N = p.total_prims, M = p.mesh_count;
   if (p.total_rays) {
     TraceArgs a;
     a.mnodes = p.mnodes.ptr;
@@ -211,9 +232,65 @@ cudaError_t run_pipeline(Plan& p, cudaStream_t s) {
     a.seg_ray_off = p.ray_off.ptr;
     a.seg_root = p.mbase.ptr;
     a.seg_count = M;
+    a.blocks_per_sm = p.trace_blocks_per_sm;
+    a.ray_batch = p.trace_ray_batch;
     if ((e = launch_trace_mbvh(a, s))) return e;
   }
   return cudaGetLastError();
+}
+
+cudaError_t run_pipeline(Plan& p, cudaStream_t s) {
+  cudaError_t e = run_build(p, s);
+  if (e != cudaSuccess) return e;
+  return run_trace(p, s);
+}
+
+// (Re)captures the whole pipeline into p.graph / p.exec.
+cudaError_t capture(Plan& p) {
+  if (p.exec) {
+    cudaGraphExecDestroy(p.exec);
+    p.exec = nullptr;
+  }
+  if (p.graph) {
+    cudaGraphDestroy(p.graph);
+    p.graph = nullptr;
+  }
+  cudaStream_t cap;
+  cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t run = run_pipeline(p, cap);
+    e = cudaStreamEndCapture(cap, &p.graph);
+    if (run != cudaSuccess) e = run;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p.exec, p.graph, 0);
+  cudaStreamDestroy(cap);
+  return e;
+}
+
+// Best of `reps` timed runs of fn after one untimed run, in milliseconds.
+template <class F>
+cudaError_t time_ms(F fn, cudaStream_t s, int reps, float* best) {
+  cudaEvent_t a, b;
+  cudaError_t e;
+  if ((e = cudaEventCreate(&a))) return e;
+  if ((e = cudaEventCreate(&b))) {
+    cudaEventDestroy(a);
+    return e;
+  }
+  *best = 3.4e38f;
+  e = fn();
+  for (int i = 0; i < reps && e == cudaSuccess; ++i) {
+    if ((e = cudaEventRecord(a, s)) || (e = fn()) || (e = cudaEventRecord(b, s)) || (e = cudaEventSynchronize(b)))
+      break;
+    float ms = 0.0f;
+    if ((e = cudaEventElapsedTime(&ms, a, b))) break;
+    *best = std::min(*best, ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return e;
 }
 
 Plan* find_plan(uint32_t id) {
@@ -259,14 +336,11 @@ ResultCode rtbvh_gpu_batch_create(const float* vertices, const uint32_t* prim_of
     return prim_offsets[a + 1] - prim_offsets[a] > prim_offsets[b + 1] - prim_offsets[b];
   });
   p->sort_bytes = radix_sort_temp_bytes(N);
-  while (p->big_count < mesh_count) {
-    const uint32_t m = order[p->big_count];
-    if (prim_offsets[m + 1] - prim_offsets[m] <= kSegClusterMinPrims) break;
-    ++p->big_count;
-  }
-  p->clusters = std::min<uint32_t>(p->big_count, 8192u);
+  p->sizes_in_order.resize(mesh_count);
+  for (uint32_t q = 0; q < mesh_count; ++q) p->sizes_in_order[q] = prim_offsets[order[q] + 1] - prim_offsets[order[q]];
+  set_cluster_min(*p, kSegClusterMinPrims);
   cudaError_t e;
-  if ((e = p->cluster_sums.alloc((size_t)kSegCluster * p->clusters)) ||
+  if ((e = p->cluster_sums.alloc((size_t)kSegCluster * std::min<uint32_t>(mesh_count, kMaxClusters))) ||
       (e = cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking)) ||
       (e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming)) ||
       (e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming)))
@@ -288,17 +362,7 @@ ResultCode rtbvh_gpu_batch_create(const float* vertices, const uint32_t* prim_of
     return cuda_rc(e);
   // one direct run (also warms every lazily initialised path), then capture
   if ((e = run_pipeline(*p, s)) || (e = cudaStreamSynchronize(s))) return cuda_rc(e);
-  cudaStream_t cap;
-  if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking))) return cuda_rc(e);
-  e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess) {
-    cudaError_t run = run_pipeline(*p, cap);
-    e = cudaStreamEndCapture(cap, &p->graph);
-    if (run != cudaSuccess) e = run;
-  }
-  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
-  cudaStreamDestroy(cap);
-  if (e != cudaSuccess) return cuda_rc(e);
+  if ((e = capture(*p))) return cuda_rc(e);
   std::lock_guard<std::mutex> lock(g_plans_mu);
   g_plans.push_back(std::move(p));
   result->id = (uint32_t)(g_plans.size() - 1);
@@ -342,6 +406,83 @@ ResultCode rtbvh_gpu_batch_status(RTBatch batch) {
   if (st & kStatusStackOverflow) return StackOverflow;
   if (st & kStatusTimeout) return Timeout;
   return st ? Error : Ok;
+}
+
+ResultCode rtbvh_gpu_batch_get_tuning(RTBatch batch, RTBatchTuning* result) {
+  Plan* p = find_plan(batch.id);
+  if (!p || result == nullptr) return Error;
+  result->trace_blocks_per_sm = p->trace_blocks_per_sm;
+  result->trace_ray_batch = p->trace_ray_batch;
+  result->cluster_min_prims = p->cluster_min;
+  result->pipeline_ms = 0.0f;
+  return Ok;
+}
+
+ResultCode rtbvh_gpu_batch_set_tuning(RTBatch batch, const RTBatchTuning* t, rtbvh_stream_t stream) {
+  Plan* p = find_plan(batch.id);
+  if (!p || t == nullptr) return Error;
+  if (t->trace_blocks_per_sm > 64 || t->trace_ray_batch > (1u << 20)) return InvalidArgument;
+  cudaError_t e;
+  if ((e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream)))) return cuda_rc(e);
+  p->trace_blocks_per_sm = t->trace_blocks_per_sm;
+  p->trace_ray_batch = t->trace_ray_batch;
+  set_cluster_min(*p, t->cluster_min_prims ? t->cluster_min_prims : kSegClusterMinPrims);
+  return cuda_rc(capture(*p));
+}
+
+ResultCode rtbvh_gpu_batch_tune(RTBatch batch, rtbvh_stream_t stream, RTBatchTuning* result) {
+  Plan* p = find_plan(batch.id);
+  if (!p) return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if ((e = cudaStreamSynchronize(s))) return cuda_rc(e);
+  // 1. clustering threshold, timed on the build alone
+  static const uint32_t kClusterMin[] = {2048u, 4096u, 8192u, 16384u, 65536u};
+  uint32_t best_c = p->cluster_min;
+  float best = 3.4e38f;
+  for (uint32_t c : kClusterMin) {
+    set_cluster_min(*p, c);
+    float ms;
+    if ((e = time_ms([&] { return run_build(*p, s); }, s, 2, &ms))) return cuda_rc(e);
+    if (ms < best) {
+      best = ms;
+      best_c = c;
+    }
+  }
+  set_cluster_min(*p, best_c);
+  if ((e = run_build(*p, s))) return cuda_rc(e);
+  // 2. traversal launch shape, timed on the trace alone
+  static const uint32_t kBlocksPerSm[] = {2u, 4u, 0u};
+  static const uint32_t kRayBatch[] = {32u, 64u, 128u, 256u};
+  uint32_t best_b = 0, best_r = 0;
+  best = 3.4e38f;
+  if (p->total_rays) {
+    for (uint32_t b : kBlocksPerSm) {
+      for (uint32_t r : kRayBatch) {
+        p->trace_blocks_per_sm = b;
+        p->trace_ray_batch = r;
+        float ms;
+        if ((e = time_ms([&] { return run_trace(*p, s); }, s, 2, &ms))) return cuda_rc(e);
+        if (ms < best) {
+          best = ms;
+          best_b = b;
+          best_r = r;
+        }
+      }
+    }
+  }
+  p->trace_blocks_per_sm = best_b;
+  p->trace_ray_batch = best_r;
+  if ((e = capture(*p))) return cuda_rc(e);
+  float total = 0.0f;
+  if ((e = time_ms([&] { return cudaGraphLaunch(p->exec, s); }, s, 3, &total))) return cuda_rc(e);
+  if (result) {
+    result->trace_blocks_per_sm = best_b;
+    result->trace_ray_batch = best_r;
+    result->cluster_min_prims = best_c;
+    result->pipeline_ms = total;
+  }
+  return Ok;
 }
 
 void rtbvh_gpu_batch_free(RTBatch batch) {

@@ -110,6 +110,11 @@ struct TraceArgs {
   const uint32_t* seg_ray_off = nullptr;
   const uint32_t* seg_root = nullptr;
   uint32_t seg_count = 0;
+  // Launch shape of the persistent MBVH traversal (0: defaults): resident
+  // blocks per SM (capped at the occupancy limit) and the number of rays a
+  // warp takes from the global ray counter at a time.
+  uint32_t blocks_per_sm = 0;
+  uint32_t ray_batch = 0;
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
@@ -122,7 +127,7 @@ cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
 // by up to `blocks` single blocks, on `side` (between the events fork and
 // join) when it is given.
 constexpr uint32_t kSegCluster = 8;
-constexpr uint32_t kSegClusterMinPrims = 4096;
+constexpr uint32_t kSegClusterMinPrims = 4096;  // default threshold (RTBatchTuning::cluster_min_prims)
 cudaError_t launch_locb_segments(const DAabb* aabbs, const uint32_t* sorted, uint32_t* indices,
                                  const uint32_t* prim_off, const uint32_t* order, const DAabb* worlds,
                                  uint32_t mesh_count, uint32_t total_prims, DAabb* lvl0, DAabb* lvl1,

@@ -166,7 +166,7 @@ __device__ __forceinline__ int sel4(const int4& v, uint32_t i) {
 // time from the global counter), so the warp's lanes stay busy instead of
 // idling until the warp's slowest ray ends. Each loop iteration visits one
 // quad node per lane; a ray's node/triangle order is the reference's.
-constexpr uint32_t kPoolBatch = 128;
+constexpr uint32_t kPoolBatch = 128;  // default rays per pool refill (TraceArgs::ray_batch)
 
 template <bool ANY_HIT, bool STATS>
 __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int* work) {
@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   bool active = false, fast = true;
   size_t pool_next = 0, pool_end = 0;  // warp-uniform
   bool exhausted = false;              // warp-uniform
+  const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
   auto start_ray = [&](size_t rr) {
     r = a.order ? (size_t)__ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
@@ -242,13 +243,13 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         // ... then from a fresh batch of the global counter
         if (need) {
           unsigned int base = 0;
-          if (lane == 0) base = atomicAdd(work, kPoolBatch);
+          if (lane == 0) base = atomicAdd(work, batch);
           base = __shfl_sync(0xffffffffu, base, 0);
           if ((size_t)base >= a.ray_count) {
             exhausted = true;
           } else {
             pool_next = base;
-            pool_end = min((size_t)base + kPoolBatch, a.ray_count);
+            pool_end = min((size_t)base + batch, a.ray_count);
             const uint32_t avail2 = (uint32_t)(pool_end - pool_next);
             const bool mine = (need >> lane) & 1u;
             const uint32_t rank = __popc(need & lt_mask);
@@ -530,6 +531,7 @@ cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
+  if (a.blocks_per_sm > 0 && (int)a.blocks_per_sm < per_sm) per_sm = (int)a.blocks_per_sm;
   size_t grid = (size_t)sm_count() * per_sm;
   const size_t need = (a.ray_count + kBlock - 1) / kBlock;
   if (grid > need) grid = need;

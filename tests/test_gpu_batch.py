@@ -102,3 +102,27 @@ def test_batch_rejects_empty_meshes(lib):
     tris, rays, po, ro = make_meshes([10, 20], seed=4)
     with pytest.raises(rb.RtbvhError):
         rb.Batch(to_cuda(tris), [0, 10, 10, 30], to_cuda(rays), [0, ro[1], ro[1], ro[2]])
+
+
+def test_batch_tuning_keeps_results(lib):
+    """Launch parameters change the schedule, never the hits."""
+    torch.cuda.set_device(0)
+    tris, rays, po, ro = make_meshes([5000, 3, 20000, 700, 4097, 9000], seed=6)
+    batch = rb.Batch(to_cuda(tris), po, to_cuda(rays), ro)
+    ref = batch.run().clone()
+    torch.cuda.synchronize()
+    chosen = batch.tune()
+    assert chosen["cluster_min_prims"] in (2048, 4096, 8192, 16384, 65536)
+    assert chosen["trace_ray_batch"] in (32, 64, 128, 256)
+    assert chosen["trace_blocks_per_sm"] in (0, 2, 4)
+    assert chosen["pipeline_ms"] > 0
+    assert batch.tuning["cluster_min_prims"] == chosen["cluster_min_prims"]
+    out = batch.run().clone()
+    torch.cuda.synchronize()
+    assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
+    # extreme settings: every mesh of > 2 primitives clustered, one block per SM, 1-ray batches
+    batch.set_tuning(trace_blocks_per_sm=1, trace_ray_batch=1, cluster_min_prims=2)
+    out = batch.run().clone()
+    torch.cuda.synchronize()
+    assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
+    assert batch.status() == rb.ResultCode.Ok
