@@ -130,6 +130,26 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def t_error_vs_fp64(tris, rays, hits, sample=1 << 20):
+    """Relative error of the kernel's hit t against Möller-Trumbore in
+    float64 on the same hit triangle, over the first `sample` hitting rays."""
+    h = np.asarray(hits[:sample])
+    prim = np.ascontiguousarray(h[:, 3]).view(np.int32)
+    ok = prim >= 0
+    if not ok.any():
+        return None
+    t = tris[prim[ok]].astype(np.float64)
+    r = rays[:sample][ok].astype(np.float64)
+    o, d = r[:, :3], r[:, 3:]
+    e1, e2 = t[:, 1] - t[:, 0], t[:, 2] - t[:, 0]
+    q = np.cross(o - t[:, 0], e1)
+    det = np.einsum("ij,ij->i", e1, np.cross(d, e2))
+    t64 = np.einsum("ij,ij->i", e2, q) / det
+    rel = np.abs(h[ok, 0].astype(np.float64) - t64) / np.abs(t64)
+    return {"rays": int(ok.sum()), "max_rel": float(f"{rel.max():.3g}"), "p99_rel": float(f"{np.quantile(rel, 0.99):.3g}"),
+            "median_rel": float(f"{np.median(rel):.3g}")}
+
+
 def run_gpu(args):
     import torch
 
@@ -248,6 +268,9 @@ def run_gpu(args):
     workloads = {}
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(tris, rays)
+    t_err = None
+    if rank == 0:
+        t_err = t_error_vs_fp64(tris, rays, step()[: 1 << 20].cpu().numpy())
     if rank == 0 and not args.no_extra:
         workloads["sphere_6400_binned_sah"] = workload_sphere_sah(not args.no_cpu_baseline)
         workloads["differentiable_200k"] = workload_differentiable()
@@ -278,6 +301,7 @@ def run_gpu(args):
             "any_hit": {"value": round(ws * N_RAYS / (any_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
                         "t_max": "0.5 x distance"},
             "max_stack_depth": max_stack,
+            "t_error_vs_fp64": t_err,
             "workloads": workloads,
         }
         print(json.dumps(line))
