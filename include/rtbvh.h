@@ -168,6 +168,12 @@ typedef void *rtbvh_stream_t;
 #define RTBVH_TRACE_ANY_HIT 1u /* stop at the first accepted triangle (occlusion) */
 #define RTBVH_TRACE_STATS 2u   /* write per-ray node visits / triangle tests / max stack depth */
 #define RTBVH_TRACE_REORDER 4u /* MBVH: trace in (origin cell, direction)-sorted order; results are unchanged */
+/* MBVH closest hit without statistics reads a 64-byte compact copy of every
+ * quad node (8-bit outward-rounded child bounds) by default: the nearest
+ * hit (t, u, v and its triangle) is the reference's, but where two
+ * triangles are hit at exactly the same t either may be reported. This flag
+ * reads the exact 128-byte nodes in the reference's visit order instead. */
+#define RTBVH_TRACE_EXACT_NODES 8u
 
 /* Builder::construct_binned_sah / construct_locally_ordered_clustered on
  * device triangles (src/bvh.rs:87-137, with aabbs = Triangle::aabb and

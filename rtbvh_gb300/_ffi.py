@@ -36,6 +36,7 @@ FLAG_NO_HOST_MIRROR = 1
 TRACE_ANY_HIT = 1
 TRACE_STATS = 2
 TRACE_REORDER = 4
+TRACE_EXACT_NODES = 8
 
 
 class RTAabb(ctypes.Structure):

@@ -241,12 +241,17 @@ class Mbvh:
         buf = ctypes.cast(h.indices, ctypes.POINTER(ctypes.c_uint32 * h.index_count)).contents
         return np.frombuffer(buf, dtype=np.uint32).copy()
 
-    def intersect(self, rays, t_max=None, any_hit=False, stats=False, stream=None, reorder=False):
+    def intersect(self, rays, t_max=None, any_hit=False, stats=False, stream=None, reorder=False,
+                  exact_nodes=False):
         """GPU MbvhIndexIterator + triangle test for a batch of rays.
         rays: (R, 6) float32 (CUDA tensor or array). Returns (hits (R,4)
         float32 CUDA tensor [t, u, v, prim bits], stats (R,3) int32 or None).
-        reorder: trace in (origin, direction)-sorted order (same results)."""
-        return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream, reorder)
+        reorder: trace in (origin, direction)-sorted order (same results).
+        exact_nodes: closest hit over the exact 128-byte quad nodes in the
+        reference's visit order (default: compact nodes, same nearest hit,
+        either triangle where two are hit at exactly the same t)."""
+        return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream, reorder,
+                      exact_nodes)
 
     def intersect_host(self, rays, t_max=None, any_hit=False):
         """Same, with host (numpy) rays and hits, copies included
@@ -270,7 +275,7 @@ class Mbvh:
             pass
 
 
-def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False):
+def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False, exact_nodes=False):
     r = _cuda_f32(rays, 6)
     n = r.shape[0]
     tm = _cuda_f32(t_max).reshape(-1) if t_max is not None else None
@@ -278,6 +283,7 @@ def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False):
     st = torch.empty((n, 3), dtype=torch.int32, device=r.device) if stats else None
     flags = (_ffi.TRACE_ANY_HIT if any_hit else 0) | (_ffi.TRACE_STATS if stats else 0)
     flags |= _ffi.TRACE_REORDER if reorder else 0
+    flags |= _ffi.TRACE_EXACT_NODES if exact_nodes else 0
     check(fn(handle, _ptr(r), _ptr(tm), n, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect")
     return hits, st
 

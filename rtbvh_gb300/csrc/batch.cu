@@ -144,6 +144,7 @@ struct Plan {
   DevBuf<DAabb> aabbs, worlds, lvl0, lvl1, nodes;
   DevBuf<float4> centers, tris;
   DevBuf<DMNode> mnodes;
+  DevBuf<DQNode> qnodes;
   DevBuf<uint2> q0, q1;
   DevBuf<char> sort_temp;
   size_t sort_bytes = 0;
@@ -211,6 +212,11 @@ cudaError_t run_build(Plan& p, cudaStream_t s) {
                                     p.mnodes.ptr, p.node_cap, p.status.ptr, mesh_blocks(M), s)))
     return e;
   if ((e = launch_gather_triangles(p.vertices, p.vals.ptr, N, p.tris.ptr, s))) return e;
+  // compact quad nodes for the closest-hit traversal (slots past the last
+  // mesh's quads are converted too and never read)
+  if (!(p.flags & (RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_EXACT_NODES)) &&
+      (e = launch_quantize_mbvh(p.mnodes.ptr, p.node_cap, p.qnodes.ptr, s)))
+    return e;
   return cudaGetLastError();
 }
 
@@ -232,6 +238,7 @@ cudaError_t run_trace(Plan& p, cudaStream_t s) {
     a.seg_ray_off = p.ray_off.ptr;
     a.seg_root = p.mbase.ptr;
     a.seg_count = M;
+    a.qnodes = (p.flags & RTBVH_TRACE_EXACT_NODES) ? nullptr : p.qnodes.ptr;
     a.blocks_per_sm = p.trace_blocks_per_sm;
     a.ray_batch = p.trace_ray_batch;
     if ((e = launch_trace_mbvh(a, s))) return e;
@@ -352,7 +359,7 @@ ResultCode rtbvh_gpu_batch_create(const float* vertices, const uint32_t* prim_of
       (e = p->status.alloc(4)) || (e = p->aabbs.alloc(N)) || (e = p->worlds.alloc(mesh_count)) ||
       (e = p->lvl0.alloc(p->node_cap)) || (e = p->lvl1.alloc(p->node_cap)) || (e = p->nodes.alloc(p->node_cap)) ||
       (e = p->centers.alloc(N)) || (e = p->tris.alloc((size_t)kTriFloat4 * N)) ||
-      (e = p->mnodes.alloc(p->node_cap)) || (e = p->q0.alloc(2 * (size_t)p->node_cap)) ||
+      (e = p->mnodes.alloc(p->node_cap)) || (e = p->qnodes.alloc(p->node_cap)) || (e = p->q0.alloc(2 * (size_t)p->node_cap)) ||
       (e = p->q1.alloc(2 * (size_t)p->node_cap)) || (e = p->sort_temp.alloc(p->sort_bytes)))
     return cuda_rc(e);
   if ((e = cudaMemcpyAsync(p->prim_off.ptr, prim_offsets, 4 * (size_t)(mesh_count + 1), cudaMemcpyHostToDevice, s)) ||

@@ -28,6 +28,7 @@ struct Entry {
   uint32_t prim_count = 0;
   DAabb* d_nodes = nullptr;       // Bvh
   DMNode* d_mnodes = nullptr;     // Mbvh
+  DQNode* d_qnodes = nullptr;     // Mbvh: compact copies for closest hit
   uint32_t* d_indices = nullptr;
   float4* d_tris = nullptr;       // 3 per index slot
   float* d_vertices = nullptr;    // prim-id order, 9 floats each
@@ -40,12 +41,14 @@ struct Entry {
   void release() {
     cudaFree(d_nodes);
     cudaFree(d_mnodes);
+    cudaFree(d_qnodes);
     cudaFree(d_indices);
     cudaFree(d_tris);
     cudaFree(d_vertices);
     cudaFree(d_status);
     d_nodes = nullptr;
     d_mnodes = nullptr;
+    d_qnodes = nullptr;
     d_indices = nullptr;
     d_tris = nullptr;
     d_vertices = nullptr;
@@ -598,6 +601,11 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
+  if ((err = dmalloc(&e->d_qnodes, e->node_count)) ||
+      (err = launch_quantize_mbvh(e->d_mnodes, e->node_count, e->d_qnodes, s))) {
+    e->release();
+    return cuda_rc(err);
+  }
 
   if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
       (err = dmalloc(&e->d_indices, prim_count)) ||
@@ -656,6 +664,7 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
     if (!e) return Error;
     if (!e->d_tris && e->node_count > 0) return InvalidArgument;
     a.mnodes = e->d_mnodes;
+    a.qnodes = (flags & RTBVH_TRACE_EXACT_NODES) ? nullptr : e->d_qnodes;
     a.nodes = e->d_nodes;
     a.node_count = e->node_count;
     a.tris = e->d_tris;
@@ -791,6 +800,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     }
     cudaFree(m->d_mnodes);
     m->d_mnodes = fresh;
+    if (m->d_qnodes && (err = launch_quantize_mbvh(m->d_mnodes, m->node_count, m->d_qnodes, s))) return cuda_rc(err);
     if (vertices) {
       if (!m->d_vertices && (err = dmalloc(&m->d_vertices, 9 * n))) return cuda_rc(err);
       if (!m->d_tris && (err = dmalloc(&m->d_tris, (size_t)kTriFloat4 * n))) return cuda_rc(err);

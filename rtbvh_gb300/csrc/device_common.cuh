@@ -43,6 +43,25 @@ struct alignas(128) DMNode {
 };
 static_assert(sizeof(DMNode) == 128, "DMNode must be 128 bytes");
 
+// Half-size copy of a quad node for the closest-hit traversal. Per axis the
+// four slot boxes are stored as 8-bit steps on a power-of-two grid starting
+// at lo[axis], rounded outwards, so every decoded box contains the exact one;
+// children and counts are exact (counts as int16). A closest-hit traversal
+// over boxes that contain the reference's finds the same nearest triangle
+// (only its visit order, and so the winner among triangles hit at exactly
+// the same t, can differ). flags bit 0 (exps >> 24): values out of range,
+// read the exact node instead.
+struct alignas(64) DQNode {
+  float lo[3];
+  uint32_t exps;          // biased exponents of the steps: x | y << 8 | z << 16 | flags << 24
+  uint32_t qx[2], qy[2];  // [0] lower bounds, [1] upper bounds; slot i in byte i
+  uint32_t qz[2];
+  int32_t children[4];
+  int16_t counts[4];
+};
+static_assert(sizeof(DQNode) == 64, "DQNode must be 64 bytes");
+constexpr float kQuantRange = 1e18f;  // larger box values (or ray origins / inverse directions) use exact nodes
+
 // ------------------------------------------------------------- float helpers
 // Vec3::min / Vec3::max of the reference (Rust f32::min/max): NaN operands are
 // ignored; on a -0/+0 tie min gives -0 and max gives +0 (order-independent).

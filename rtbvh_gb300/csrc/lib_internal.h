@@ -77,6 +77,8 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n,
 // Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here.
 ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes,
                       uint32_t* mnode_count);
+// Compact (64-byte) copies of quad nodes for the closest-hit traversal.
+cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s);
 
 // Bvh::refit (src/bvh.rs:176-205) bounds, topology kept.
 ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
@@ -115,6 +117,9 @@ struct TraceArgs {
   // warp takes from the global ray counter at a time.
   uint32_t blocks_per_sm = 0;
   uint32_t ray_batch = 0;
+  // Optional compact copies of mnodes; closest-hit launches without
+  // statistics read them (any-hit and statistics keep the exact nodes).
+  const DQNode* qnodes = nullptr;
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);

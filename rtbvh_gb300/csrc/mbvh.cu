@@ -542,3 +542,98 @@ cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, co
 }
 
 }  // namespace rtbvh
+
+// ---------------------------------------------------------------- compact quad nodes
+namespace rtbvh {
+
+namespace {
+
+// One axis of a DQNode: grid start lo = the smallest bound of the four
+// slots, step 2^k with 255 * 2^k covering the axis extent, lower bounds
+// rounded down and upper bounds rounded up (checked in double, where
+// lo + q * 2^k is exact for these magnitudes). False if a value is out of
+// range or does not fit.
+__device__ bool quantize_axis(const float* mn, const float* mx, float* lo_out, uint32_t* e_out, uint32_t* qlo,
+                              uint32_t* qhi) {
+  float lo = mn[0], hi = mn[0];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (!(fabsf(mn[i]) <= kQuantRange) || !(fabsf(mx[i]) <= kQuantRange)) return false;
+    lo = fminf(lo, fminf(mn[i], mx[i]));
+    hi = fmaxf(hi, fmaxf(mn[i], mx[i]));
+  }
+  const double ext = (double)hi - (double)lo;
+  int k = -126;
+  if (ext > 0.0) {
+    int ex;
+    const double m = frexp(ext / 255.0, &ex);  // ext / 255 = m 2^ex, m in [0.5, 1)
+    k = (m == 0.5) ? ex - 1 : ex;
+    if (k < -126) k = -126;
+  }
+  for (int attempt = 0; attempt < 3; ++attempt, ++k) {
+    if (k > 127) return false;
+    const double step = ldexp(1.0, k);
+    uint32_t L = 0, H = 0;
+    bool ok = true;
+    for (int i = 0; i < 4 && ok; ++i) {
+      double dl = floor(((double)mn[i] - (double)lo) / step);
+      if (dl < 0.0) dl = 0.0;
+      while (dl > 0.0 && (double)lo + dl * step > (double)mn[i]) dl -= 1.0;
+      double dh = ceil(((double)mx[i] - (double)lo) / step);
+      if (dh < 0.0) dh = 0.0;
+      while (dh <= 255.0 && (double)lo + dh * step < (double)mx[i]) dh += 1.0;
+      if (dl > 255.0 || dh > 255.0) {
+        ok = false;
+      } else {
+        L |= (uint32_t)dl << (8 * i);
+        H |= (uint32_t)dh << (8 * i);
+      }
+    }
+    if (ok) {
+      *lo_out = lo;
+      *e_out = (uint32_t)(k + 127);
+      *qlo = L;
+      *qhi = H;
+      return true;
+    }
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(kBlock) k_quantize(const DMNode* __restrict__ in, uint32_t count,
+                                                      DQNode* __restrict__ out) {
+  const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= count) return;
+  const DMNode m = in[i];
+  DQNode q;
+  uint32_t ex = 0, ey = 0, ez = 0;
+  bool ok = quantize_axis(m.min_x, m.max_x, &q.lo[0], &ex, &q.qx[0], &q.qx[1]) &&
+            quantize_axis(m.min_y, m.max_y, &q.lo[1], &ey, &q.qy[0], &q.qy[1]) &&
+            quantize_axis(m.min_z, m.max_z, &q.lo[2], &ez, &q.qz[0], &q.qz[1]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    q.children[k] = m.children[k];
+    ok = ok && m.counts[k] >= -32768 && m.counts[k] <= 32767;
+    q.counts[k] = (int16_t)m.counts[k];
+  }
+  if (!ok) {
+    q.lo[0] = q.lo[1] = q.lo[2] = 0.0f;
+    q.qx[0] = q.qx[1] = q.qy[0] = q.qy[1] = q.qz[0] = q.qz[1] = 0u;
+    ex = ey = ez = 0;
+  }
+  q.exps = ex | (ey << 8) | (ez << 16) | ((ok ? 0u : 1u) << 24);
+  const float4* src = reinterpret_cast<const float4*>(&q);
+  float4* dst = reinterpret_cast<float4*>(out + i);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) dst[k] = src[k];
+}
+
+}  // namespace
+
+cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s) {
+  if (count == 0) return cudaSuccess;
+  k_quantize<<<(count + kBlock - 1) / kBlock, kBlock, 0, s>>>(mnodes, count, qnodes);
+  return cudaGetLastError();
+}
+
+}  // namespace rtbvh

@@ -152,6 +152,56 @@ __device__ __forceinline__ void quad_intersect(const DMNode* node, const RayStat
   ids = i0 | (i1 << 2) | (i2 << 4) | (i3 << 6);
 }
 
+// Slot bound i of a DQNode axis word as a float (exact): 2^23 + q is
+// assembled in the float's mantissa, then 2^23 is subtracted.
+__device__ __forceinline__ float qbyte(uint32_t w, uint32_t i) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7440u + i)) - 8388608.0f;
+}
+
+// The slab test of quad_intersect<true> on a DQNode: the plane of step q is
+// at lo + q * step, so its ray parameter is q * (step * inv) + (lo - o) * inv.
+// The decoded boxes contain the exact ones; the sort network and the mask
+// rule are the reference's.
+__device__ __forceinline__ void quad_intersect_q(const float (&h0)[8], const float (&h1)[8], const RayState& r,
+                                                 uint32_t& mask, uint32_t& ids, int4& children, int4& counts) {
+  const uint32_t exps = __float_as_uint(h0[3]);
+  const float sx = __uint_as_float((exps & 0xffu) << 23);
+  const float sy = __uint_as_float(((exps >> 8) & 0xffu) << 23);
+  const float sz = __uint_as_float(((exps >> 16) & 0xffu) << 23);
+  const float ax = sx * r.ix, bx = (h0[0] - r.ox) * r.ix;
+  const float ay = sy * r.iy, by = (h0[1] - r.oy) * r.iy;
+  const float az = sz * r.iz, bz = (h0[2] - r.oz) * r.iz;
+  const uint32_t xl = __float_as_uint(h0[4]), xh = __float_as_uint(h0[5]);
+  const uint32_t yl = __float_as_uint(h0[6]), yh = __float_as_uint(h0[7]);
+  const uint32_t zl = __float_as_uint(h1[0]), zh = __float_as_uint(h1[1]);
+  children = make_int4(__float_as_int(h1[2]), __float_as_int(h1[3]), __float_as_int(h1[4]), __float_as_int(h1[5]));
+  const uint32_t c01 = __float_as_uint(h1[6]), c23 = __float_as_uint(h1[7]);
+  counts = make_int4((int)(int16_t)(c01 & 0xffffu), (int)(int16_t)(c01 >> 16), (int)(int16_t)(c23 & 0xffffu),
+                     (int)(int16_t)(c23 >> 16));
+  float tmin[4];
+  uint32_t m = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float tx0 = fmaf(qbyte(xl, i), ax, bx), tx1 = fmaf(qbyte(xh, i), ax, bx);
+    const float ty0 = fmaf(qbyte(yl, i), ay, by), ty1 = fmaf(qbyte(yh, i), ay, by);
+    const float tz0 = fmaf(qbyte(zl, i), az, bz), tz1 = fmaf(qbyte(zh, i), az, bz);
+    const float tn = fmaxf(fminf(tx0, tx1), fmaxf(fminf(ty0, ty1), fminf(tz0, tz1)));
+    const float tx = fminf(fmaxf(tx0, tx1), fminf(fmaxf(ty0, ty1), fmaxf(tz0, tz1)));
+    tmin[i] = tn;
+    if ((tx >= tn) && (tn < r.t)) m |= 1u << i;
+  }
+  uint32_t i0 = 0, i1 = 1, i2 = 2, i3 = 3;
+  float t0 = tmin[0], t1 = tmin[1], t2 = tmin[2], t3 = tmin[3], tt;
+  uint32_t ti;
+  if (t0 > t1) { tt = t0; t0 = t1; t1 = tt; ti = i0; i0 = i1; i1 = ti; }
+  if (t2 > t3) { tt = t2; t2 = t3; t3 = tt; ti = i2; i2 = i3; i3 = ti; }
+  if (t0 > t2) { tt = t0; t0 = t2; t2 = tt; ti = i0; i0 = i2; i2 = ti; }
+  if (t1 > t3) { tt = t1; t1 = t3; t3 = tt; ti = i1; i1 = i3; i3 = ti; }
+  if (t2 > t3) { ti = i2; i2 = i3; i3 = ti; }
+  mask = m;
+  ids = i0 | (i1 << 2) | (i2 << 4) | (i3 << 6);
+}
+
 __device__ __forceinline__ bool finite_ray(const RayState& r) {
   return isfinite(r.ox) && isfinite(r.oy) && isfinite(r.oz) && isfinite(r.dx) && isfinite(r.dy) && isfinite(r.dz) &&
          isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
@@ -168,7 +218,7 @@ __device__ __forceinline__ int sel4(const int4& v, uint32_t i) {
 // quad node per lane; a ray's node/triangle order is the reference's.
 constexpr uint32_t kPoolBatch = 128;  // default rays per pool refill (TraceArgs::ray_batch)
 
-template <bool ANY_HIT, bool STATS>
+template <bool ANY_HIT, bool STATS, bool COMPACT>
 __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int* work) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
@@ -184,7 +234,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   int sp = -1;
   int32_t next = -1;
   size_t r = 0;
-  bool active = false, fast = true;
+  bool active = false, fast = true, compact = false;
   size_t pool_next = 0, pool_end = 0;  // warp-uniform
   bool exhausted = false;              // warp-uniform
   const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
@@ -192,6 +242,10 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     r = a.order ? (size_t)__ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
     fast = finite_ray(ray);
+    if (COMPACT)
+      compact = fast && fabsf(ray.ox) <= kQuantRange && fabsf(ray.oy) <= kQuantRange &&
+                fabsf(ray.oz) <= kQuantRange && fabsf(ray.ix) <= kQuantRange && fabsf(ray.iy) <= kQuantRange &&
+                fabsf(ray.iz) <= kQuantRange;
     hu = hv = 0.0f;
     prim = -1;
     visits = tests = max_depth = 0;
@@ -275,8 +329,21 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     }
     uint32_t mask, ids;
     int4 children, counts;
-    if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
-    else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
+    bool exact = true;
+    if (COMPACT && compact) {
+      const float* qn = reinterpret_cast<const float*>(a.qnodes + current);
+      float h0[8], h1[8];
+      ld8(qn, h0);
+      ld8(qn + 8, h1);
+      if (!(__float_as_uint(h0[3]) >> 24)) {
+        quad_intersect_q(h0, h1, ray, mask, ids, children, counts);
+        exact = false;
+      }
+    }
+    if (exact) {
+      if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
+      else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
+    }
     if (STATS) ++visits;
     bool done = false;
 #pragma unroll 1
@@ -525,9 +592,9 @@ __global__ void __launch_bounds__(256) k_ray_keys(const float* __restrict__ rays
   vals[i] = (uint32_t)i;
 }
 
-template <bool MBVH, bool ANY_HIT, bool STATS>
+template <bool MBVH, bool ANY_HIT, bool STATS, bool COMPACT = false>
 cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
-  auto kern = MBVH ? k_trace_mbvh<ANY_HIT, STATS> : k_trace_bvh<ANY_HIT, STATS>;
+  auto kern = MBVH ? k_trace_mbvh<ANY_HIT, STATS, COMPACT> : k_trace_bvh<ANY_HIT, STATS>;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
@@ -565,7 +632,9 @@ cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
   }
   const bool st = a.stats != nullptr;
   if (a.any_hit) e = st ? launch3<MBVH, true, true>(a, s, work.ptr) : launch3<MBVH, true, false>(a, s, work.ptr);
-  else e = st ? launch3<MBVH, false, true>(a, s, work.ptr) : launch3<MBVH, false, false>(a, s, work.ptr);
+  else if (st) e = launch3<MBVH, false, true>(a, s, work.ptr);
+  else if (MBVH && a.qnodes) e = launch3<MBVH, false, false, true>(a, s, work.ptr);
+  else e = launch3<MBVH, false, false>(a, s, work.ptr);
   return e;
 }
 

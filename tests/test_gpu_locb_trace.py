@@ -255,3 +255,78 @@ def test_hit_t_error_against_fp64():
     assert np.median(rel) < 2e-7
     assert np.quantile(rel, 0.99) < 2e-6
     assert rel.max() < 1e-4
+
+
+def _mt_t(tri, ray):
+    """The reference's triangle test in float32 (no contraction) for one
+    triangle and ray; t or None."""
+    f32 = np.float32
+    v0, v1, v2 = (tri[k].astype(f32) for k in range(3))
+    o, d = ray[:3].astype(f32), ray[3:].astype(f32)
+    e1, e2 = v1 - v0, v2 - v0
+    h = np.array([d[1] * e2[2] - e2[1] * d[2], d[2] * e2[0] - e2[2] * d[0], d[0] * e2[1] - e2[0] * d[1]], f32)
+    det = f32(f32(e1[0] * h[0]) + f32(e1[1] * h[1])) + f32(e1[2] * h[2])
+    if -1e-5 < det < 1e-5:
+        return None
+    f = f32(1.0) / det
+    s = o - v0
+    q = np.array([s[1] * e1[2] - e1[1] * s[2], s[2] * e1[0] - e1[2] * s[0], s[0] * e1[1] - e1[0] * s[1]], f32)
+    return f * (f32(f32(e2[0] * q[0]) + f32(e2[1] * q[1])) + f32(e2[2] * q[2]))
+
+
+def assert_same_nearest(hits, ref, tris, rays, max_tie_frac=1e-4):
+    """Same nearest hit as `ref`: t bit-identical on every ray; the triangle
+    (and its u, v) identical unless the reported one is hit at exactly the
+    same t (a tie, which the compact-node traversal may resolve differently)."""
+    assert np.array_equal(u32(hits[:, 0]), u32(ref[:, 0])), "t differs"
+    p, q = rb.hit_prims(hits), rb.hit_prims(ref)
+    diff = np.nonzero(p != q)[0]
+    for r in diff:
+        assert p[r] >= 0 and q[r] >= 0
+        t = _mt_t(tris[p[r]], rays[r])
+        assert t is not None and np.float32(t).view(np.uint32) == hits[r, 0].view(np.uint32), f"ray {r}: not a tie"
+    same = p == q
+    assert np.array_equal(u32(hits[same]), u32(ref[same]))
+    assert len(diff) <= max(1, int(max_tie_frac * len(hits))), f"{len(diff)} ties"
+
+
+@pytest.mark.parametrize("name", SCENES)
+@pytest.mark.parametrize("kind", ["locb", "sah"])
+def test_compact_nodes_same_nearest_hit(name, kind):
+    """Default closest hit (64-byte compact quad nodes) against the oracle's
+    traversal of the exact nodes, and against the exact-node GPU path."""
+    tris = scene(name)
+    g = gpu_build(tris, kind)
+    m = rb.Mbvh.construct(g)
+    rays, _ = rays_for(name, count=65536)
+    hits = m.intersect(to_cuda(rays))[0].cpu().numpy()
+    exact = m.intersect(to_cuda(rays), exact_nodes=True)[0].cpu().numpy()
+    assert m.status() == rb.ResultCode.Ok
+    assert_same_nearest(hits, exact, tris, rays)
+    if kind == "locb":
+        on, oi = oracle_build(tris, "locb")
+        oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, stats=False)
+        assert_same_nearest(hits, oh, tris, rays)
+    assert (rb.hit_prims(hits) >= 0).sum() > 0
+
+
+def test_compact_nodes_out_of_range_values():
+    """Triangles far outside the quantisable range put their quad nodes on
+    the exact path; rays with huge origins trace the exact nodes entirely.
+    Results equal the exact-node traversal."""
+    tris = scene("incoherent_20k").copy()
+    far = np.random.default_rng(5).choice(len(tris), 50, replace=False)
+    tris[far] *= np.float32(1e19)
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    rays, _ = rays_for("incoherent_20k", count=65536)
+    rays = rays.copy()
+    rays[:100, :3] = np.float32(2e18)  # beyond the compact path's range
+    rays[:100, 3:] = -rays[:100, :3] / np.linalg.norm(rays[:100, :3], axis=1, keepdims=True)
+    hits = m.intersect(to_cuda(rays))[0].cpu().numpy()
+    exact = m.intersect(to_cuda(rays), exact_nodes=True)[0].cpu().numpy()
+    assert m.status() == rb.ResultCode.Ok
+    assert_same_nearest(hits, exact, tris, rays)
+    on, oi = oracle_build(tris, "locb")
+    oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, stats=False)
+    assert_same_nearest(hits, oh, tris, rays)
