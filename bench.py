@@ -198,7 +198,7 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
 
     def step():
-        hits, _ = mbvh.intersect(d_rays)
+        hits, _ = mbvh.intersect(d_rays, exact_nodes=args.exact_nodes)
         return hits
 
     for _ in range(args.warmup):
@@ -628,6 +628,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--rays", type=int, default=0, help="profiling only: fewer rays")
     ap.add_argument("--tris", type=int, default=0, help="profiling only: fewer triangles")
+    ap.add_argument("--exact-nodes", action="store_true",
+                    help="profiling only: time the closest hit over the exact 128-byte quad nodes")
     args = ap.parse_args()
     apply_size_overrides(args)
     if args.warmup < 3:

@@ -212,10 +212,10 @@ cudaError_t run_build(Plan& p, cudaStream_t s) {
                                     p.mnodes.ptr, p.node_cap, p.status.ptr, mesh_blocks(M), s)))
     return e;
   if ((e = launch_gather_triangles(p.vertices, p.vals.ptr, N, p.tris.ptr, s))) return e;
-  // compact quad nodes for the closest-hit traversal (slots past the last
-  // mesh's quads are converted too and never read)
+  // compact quad nodes for the closest-hit traversal (the forest's quad
+  // count, mbase[M], is read on the device)
   if (!(p.flags & (RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_EXACT_NODES)) &&
-      (e = launch_quantize_mbvh(p.mnodes.ptr, p.node_cap, p.qnodes.ptr, s)))
+      (e = launch_quantize_mbvh(p.mnodes.ptr, p.node_cap, p.qnodes.ptr, s, p.mbase.ptr + M)))
     return e;
   return cudaGetLastError();
 }
@@ -428,7 +428,7 @@ ResultCode rtbvh_gpu_batch_get_tuning(RTBatch batch, RTBatchTuning* result) {
 ResultCode rtbvh_gpu_batch_set_tuning(RTBatch batch, const RTBatchTuning* t, rtbvh_stream_t stream) {
   Plan* p = find_plan(batch.id);
   if (!p || t == nullptr) return Error;
-  if (t->trace_blocks_per_sm > 64 || t->trace_ray_batch > (1u << 20)) return InvalidArgument;
+  if (t->trace_blocks_per_sm > 64 || t->trace_ray_batch > 4096u) return InvalidArgument;
   cudaError_t e;
   if ((e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream)))) return cuda_rc(e);
   p->trace_blocks_per_sm = t->trace_blocks_per_sm;

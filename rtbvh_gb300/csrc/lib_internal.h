@@ -77,8 +77,10 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n,
 // Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here.
 ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes,
                       uint32_t* mnode_count);
-// Compact (64-byte) copies of quad nodes for the closest-hit traversal.
-cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s);
+// Compact (64-byte) copies of quad nodes for the closest-hit traversal;
+// with live_count (device) only the first *live_count of `count` nodes.
+cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,
+                                 const uint32_t* live_count = nullptr);
 
 // Bvh::refit (src/bvh.rs:176-205) bounds, topology kept.
 ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,

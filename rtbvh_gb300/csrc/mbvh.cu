@@ -550,9 +550,16 @@ namespace {
 
 // One axis of a DQNode: grid start lo = the smallest bound of the four
 // slots, step 2^k with 255 * 2^k covering the axis extent, lower bounds
-// rounded down and upper bounds rounded up (checked in double, where
-// lo + q * 2^k is exact for these magnitudes). False if a value is out of
-// range or does not fit.
+// rounded down and upper bounds rounded up. The checks are exact: x - lo is
+// split into hi + lo parts (two-sum, this file is compiled without
+// contraction) and compared with q * 2^k, which is exact in float. False if a
+// value is out of range or does not fit.
+__device__ __forceinline__ void two_diff(float a, float b, float& hi, float& lo) {
+  hi = a - b;
+  const float bb = hi - a;
+  lo = (a - (hi - bb)) + (-b - bb);
+}
+
 __device__ bool quantize_axis(const float* mn, const float* mx, float* lo_out, uint32_t* e_out, uint32_t* qlo,
                               uint32_t* qhi) {
   float lo = mn[0], hi = mn[0];
@@ -562,31 +569,53 @@ __device__ bool quantize_axis(const float* mn, const float* mx, float* lo_out, u
     lo = fminf(lo, fminf(mn[i], mx[i]));
     hi = fmaxf(hi, fmaxf(mn[i], mx[i]));
   }
-  const double ext = (double)hi - (double)lo;
   int k = -126;
-  if (ext > 0.0) {
+  const float ext = hi - lo;
+  if (ext > 0.0f) {
     int ex;
-    const double m = frexp(ext / 255.0, &ex);  // ext / 255 = m 2^ex, m in [0.5, 1)
-    k = (m == 0.5) ? ex - 1 : ex;
+    const float m = frexpf(ext / 255.0f, &ex);  // ext / 255 = m 2^ex, m in [0.5, 1)
+    k = (m == 0.5f) ? ex - 1 : ex;
     if (k < -126) k = -126;
   }
   for (int attempt = 0; attempt < 3; ++attempt, ++k) {
     if (k > 127) return false;
-    const double step = ldexp(1.0, k);
+    const float step = __uint_as_float((uint32_t)(k + 127) << 23);
+    const float inv_step = (k <= 126) ? __uint_as_float((uint32_t)(127 - k) << 23) : 0.0f;
+    if (k > 126 || k < -126) return false;
     uint32_t L = 0, H = 0;
     bool ok = true;
     for (int i = 0; i < 4 && ok; ++i) {
-      double dl = floor(((double)mn[i] - (double)lo) / step);
-      if (dl < 0.0) dl = 0.0;
-      while (dl > 0.0 && (double)lo + dl * step > (double)mn[i]) dl -= 1.0;
-      double dh = ceil(((double)mx[i] - (double)lo) / step);
-      if (dh < 0.0) dh = 0.0;
-      while (dh <= 255.0 && (double)lo + dh * step < (double)mx[i]) dh += 1.0;
-      if (dl > 255.0 || dh > 255.0) {
+      float dh, dl;
+      two_diff(mn[i], lo, dh, dl);  // mn - lo == dh + dl exactly
+      float q = floorf(dh * inv_step);
+      if (q < 0.0f) q = 0.0f;
+      if (q > 255.0f) q = 255.0f;
+      // need q * step <= dh + dl
+      for (int g = 0; g < 4 && q > 0.0f; ++g) {
+        const float v = q * step;
+        if (v < dh || (v == dh && dl >= 0.0f)) break;
+        q -= 1.0f;
+      }
+      {
+        const float v = q * step;
+        if (!(v < dh || (v == dh && dl >= 0.0f))) q = 0.0f;  // 0 is always below: lo is the minimum
+      }
+      const uint32_t ql = (uint32_t)q;
+      two_diff(mx[i], lo, dh, dl);
+      q = ceilf(dh * inv_step);
+      if (q < 0.0f) q = 0.0f;
+      // need q * step >= dh + dl
+      for (int g = 0; g < 4; ++g) {
+        const float v = q * step;
+        if (v > dh || (v == dh && dl <= 0.0f)) break;
+        q += 1.0f;
+      }
+      const float v = q * step;
+      if (q > 255.0f || !(v > dh || (v == dh && dl <= 0.0f))) {
         ok = false;
       } else {
-        L |= (uint32_t)dl << (8 * i);
-        H |= (uint32_t)dh << (8 * i);
+        L |= ql << (8 * i);
+        H |= (uint32_t)q << (8 * i);
       }
     }
     if (ok) {
@@ -601,9 +630,10 @@ __device__ bool quantize_axis(const float* mn, const float* mx, float* lo_out, u
 }
 
 __global__ void __launch_bounds__(kBlock) k_quantize(const DMNode* __restrict__ in, uint32_t count,
+                                                      const uint32_t* __restrict__ live_count,
                                                       DQNode* __restrict__ out) {
   const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-  if (i >= count) return;
+  if (i >= count || (live_count && i >= __ldg(live_count))) return;
   const DMNode m = in[i];
   DQNode q;
   uint32_t ex = 0, ey = 0, ez = 0;
@@ -630,9 +660,10 @@ __global__ void __launch_bounds__(kBlock) k_quantize(const DMNode* __restrict__ 
 
 }  // namespace
 
-cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s) {
+cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,
+                                 const uint32_t* live_count) {
   if (count == 0) return cudaSuccess;
-  k_quantize<<<(count + kBlock - 1) / kBlock, kBlock, 0, s>>>(mnodes, count, qnodes);
+  k_quantize<<<(count + kBlock - 1) / kBlock, kBlock, 0, s>>>(mnodes, count, live_count, qnodes);
   return cudaGetLastError();
 }
 

@@ -17,9 +17,17 @@
 // Kernels are persistent. The stack lives in local memory with a hard bound;
 // a ray that would exceed it stops, reports prim -2 and sets
 // kStatusStackOverflow. A quad node (one 128-byte line) is read with four
-// 256-bit loads: the kernel is bound by L1 wavefronts (each lane reads its
-// own node), and halving the load count per node is worth 13 %. Leaf
-// triangles are 64 bytes ({v0, prim}, {e1}, {e2}, pad): two 256-bit loads.
+// 256-bit loads (each lane reads its own node, so the load count per node
+// sets the L1 wavefronts). Leaf triangles are 64 bytes ({v0, prim}, {e1},
+// {e2}, pad): two 256-bit loads.
+//
+// Closest hit without statistics reads the 64-byte compact copies of the
+// quad nodes (DQNode, two 256-bit loads) when they exist: the boxes contain
+// the exact ones, so the nearest triangle and its t/u/v are unchanged, and
+// only the winner among triangles hit at exactly the same t can differ from
+// the reference's visit order. This halves the node bytes and the L1 fill
+// traffic. Any hit, statistics and rays with a zero, non-finite or huge
+// component use the exact nodes.
 #include <cstdlib>
 
 #include "lib_internal.h"
@@ -171,9 +179,14 @@ __device__ __forceinline__ void quad_intersect_q(const float (&h0)[8], const flo
   const float ax = sx * r.ix, bx = (h0[0] - r.ox) * r.ix;
   const float ay = sy * r.iy, by = (h0[1] - r.oy) * r.iy;
   const float az = sz * r.iz, bz = (h0[2] - r.oz) * r.iz;
+  // with a negative inverse direction the upper plane is the near one; the
+  // fma is monotonic in q, so this selection equals min/max of the two
   const uint32_t xl = __float_as_uint(h0[4]), xh = __float_as_uint(h0[5]);
   const uint32_t yl = __float_as_uint(h0[6]), yh = __float_as_uint(h0[7]);
   const uint32_t zl = __float_as_uint(h1[0]), zh = __float_as_uint(h1[1]);
+  const uint32_t xn = r.ix < 0.0f ? xh : xl, xf = r.ix < 0.0f ? xl : xh;
+  const uint32_t yn = r.iy < 0.0f ? yh : yl, yf = r.iy < 0.0f ? yl : yh;
+  const uint32_t zn = r.iz < 0.0f ? zh : zl, zf = r.iz < 0.0f ? zl : zh;
   children = make_int4(__float_as_int(h1[2]), __float_as_int(h1[3]), __float_as_int(h1[4]), __float_as_int(h1[5]));
   const uint32_t c01 = __float_as_uint(h1[6]), c23 = __float_as_uint(h1[7]);
   counts = make_int4((int)(int16_t)(c01 & 0xffffu), (int)(int16_t)(c01 >> 16), (int)(int16_t)(c23 & 0xffffu),
@@ -182,11 +195,8 @@ __device__ __forceinline__ void quad_intersect_q(const float (&h0)[8], const flo
   uint32_t m = 0;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    const float tx0 = fmaf(qbyte(xl, i), ax, bx), tx1 = fmaf(qbyte(xh, i), ax, bx);
-    const float ty0 = fmaf(qbyte(yl, i), ay, by), ty1 = fmaf(qbyte(yh, i), ay, by);
-    const float tz0 = fmaf(qbyte(zl, i), az, bz), tz1 = fmaf(qbyte(zh, i), az, bz);
-    const float tn = fmaxf(fminf(tx0, tx1), fmaxf(fminf(ty0, ty1), fminf(tz0, tz1)));
-    const float tx = fminf(fmaxf(tx0, tx1), fminf(fmaxf(ty0, ty1), fmaxf(tz0, tz1)));
+    const float tn = fmaxf(fmaf(qbyte(xn, i), ax, bx), fmaxf(fmaf(qbyte(yn, i), ay, by), fmaf(qbyte(zn, i), az, bz)));
+    const float tx = fminf(fmaf(qbyte(xf, i), ax, bx), fminf(fmaf(qbyte(yf, i), ay, by), fmaf(qbyte(zf, i), az, bz)));
     tmin[i] = tn;
     if ((tx >= tn) && (tn < r.t)) m |= 1u << i;
   }
@@ -233,13 +243,14 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   int32_t stack[kStack];
   int sp = -1;
   int32_t next = -1;
-  size_t r = 0;
+  uint32_t r = 0;
   bool active = false, fast = true, compact = false;
-  size_t pool_next = 0, pool_end = 0;  // warp-uniform
+  uint32_t pool_next = 0, pool_end = 0;  // warp-uniform (ray_count < 2^32 - 1024)
   bool exhausted = false;              // warp-uniform
   const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
-  auto start_ray = [&](size_t rr) {
-    r = a.order ? (size_t)__ldg(a.order + rr) : rr;
+  const uint32_t ray_count = (uint32_t)a.ray_count;
+  auto start_ray = [&](uint32_t rr) {
+    r = a.order ? __ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
     fast = finite_ray(ray);
     if (COMPACT)
@@ -252,9 +263,9 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     if (a.node_count == 0) {
       a.hits[r] = make_float4(ray.t, 0.0f, 0.0f, __int_as_float(-1));
       if (STATS) {
-        a.stats[3 * r + 0] = 0;
-        a.stats[3 * r + 1] = 0;
-        a.stats[3 * r + 2] = 0;
+        a.stats[3 * (size_t)r + 0] = 0;
+        a.stats[3 * (size_t)r + 1] = 0;
+        a.stats[3 * (size_t)r + 2] = 0;
       }
     } else {
       sp = -1;
@@ -264,7 +275,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         uint32_t lo = 0, hi = a.seg_count;  // mesh with seg_ray_off[m] <= r < seg_ray_off[m + 1]
         while (hi - lo > 1) {
           const uint32_t mid = (lo + hi) >> 1;
-          if ((size_t)__ldg(a.seg_ray_off + mid) <= r) lo = mid;
+          if (__ldg(a.seg_ray_off + mid) <= r) lo = mid;
           else hi = mid;
         }
         const uint32_t root = __ldg(a.seg_root + lo);
@@ -272,9 +283,9 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
           active = false;
           a.hits[r] = make_float4(ray.t, 0.0f, 0.0f, __int_as_float(-1));
           if (STATS) {
-            a.stats[3 * r + 0] = 0;
-            a.stats[3 * r + 1] = 0;
-            a.stats[3 * r + 2] = 0;
+            a.stats[3 * (size_t)r + 0] = 0;
+            a.stats[3 * (size_t)r + 1] = 0;
+            a.stats[3 * (size_t)r + 2] = 0;
           }
         }
         next = (int32_t)root;
@@ -299,11 +310,11 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
           unsigned int base = 0;
           if (lane == 0) base = atomicAdd(work, batch);
           base = __shfl_sync(0xffffffffu, base, 0);
-          if ((size_t)base >= a.ray_count) {
+          if (base >= ray_count) {
             exhausted = true;
           } else {
             pool_next = base;
-            pool_end = min((size_t)base + batch, a.ray_count);
+            pool_end = (ray_count - base > batch) ? base + batch : ray_count;
             const uint32_t avail2 = (uint32_t)(pool_end - pool_next);
             const bool mine = (need >> lane) & 1u;
             const uint32_t rank = __popc(need & lt_mask);
@@ -387,9 +398,9 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     if (done || (next < 0 && sp < 0)) {
       a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
       if (STATS) {
-        a.stats[3 * r + 0] = visits;
-        a.stats[3 * r + 1] = tests;
-        a.stats[3 * r + 2] = max_depth;
+        a.stats[3 * (size_t)r + 0] = visits;
+        a.stats[3 * (size_t)r + 1] = tests;
+        a.stats[3 * (size_t)r + 2] = max_depth;
       }
       active = false;
     }
@@ -476,9 +487,9 @@ __device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
   }
   a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
   if (STATS) {
-    a.stats[3 * r + 0] = visits;
-    a.stats[3 * r + 1] = tests;
-    a.stats[3 * r + 2] = max_depth;
+    a.stats[3 * (size_t)r + 0] = visits;
+    a.stats[3 * (size_t)r + 1] = tests;
+    a.stats[3 * (size_t)r + 2] = max_depth;
   }
 }
 
@@ -609,7 +620,9 @@ cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
 template <bool MBVH>
 cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
   if (a0.ray_count == 0) return cudaSuccess;
-  if (a0.ray_count > 0xffffffffull - 1024) return cudaErrorInvalidValue;
+  // ray indices and the work counter are 32-bit; after the last batch every
+  // warp adds one more ray_batch (<= 4096) to the counter, which must not wrap
+  if (a0.ray_count > 0xffffffffull - (1ull << 25) || a0.ray_batch > 4096u) return cudaErrorInvalidValue;
   TraceArgs a = a0;
   Scratch<unsigned int> work;
   Scratch<uint32_t> keys, order, acc;
