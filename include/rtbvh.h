@@ -231,6 +231,13 @@ typedef struct RTGpuView {
 } RTGpuView;
 ResultCode rtbvh_gpu_view(uint32_t structure_id, int is_mbvh, RTGpuView *view);
 
+/* The Mbvh's closest-hit traversal tree (no counterpart in the reference):
+ * a 4-wide collapse of the source Bvh with each slot's own box, `count`
+ * nodes with root 0, as exact RTMbvhNode records (`exact`) and as the
+ * 64-byte compact records the kernel reads (`compact`). Device pointers,
+ * valid until the Mbvh is freed or refitted. */
+ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode **exact, const void **compact, uint32_t *count);
+
 /* Bvh::refit (src/bvh.rs:176-205) on the GPU from device triangles or device
  * aabbs (exactly one non-NULL); updates the Bvh and, if mbvh_id != UINT32_MAX,
  * re-collapses that Mbvh from it and re-lays its triangles. */

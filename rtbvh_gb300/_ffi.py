@@ -113,6 +113,7 @@ SIGNATURES = {
     "rtbvh_intersect_mbvh_batch": (_rc, [RTMbvh, _vp, _vp, _sz, _vp, _u32]),
     "rtbvh_gpu_status": (_rc, [_u32, ctypes.c_int]),
     "rtbvh_gpu_view": (_rc, [_u32, ctypes.c_int, ctypes.POINTER(RTGpuView)]),
+    "rtbvh_gpu_traversal_tree": (_rc, [RTMbvh, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_u32)]),
     "rtbvh_gpu_refit": (_rc, [_u32, _vp, _vp, _u32, _vp]),
     "rtbvh_gpu_refit_noalloc": (_rc, [_u32, _vp, _vp]),
     "rtbvh_gpu_intersect_backward": (_rc, [_vp, _sz, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),

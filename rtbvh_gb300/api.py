@@ -253,6 +253,17 @@ class Mbvh:
         return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream, reorder,
                       exact_nodes)
 
+    def traversal_tree(self):
+        """(exact (count, 32) float32 quad records, compact (count, 16) uint32
+        records) of the closest-hit traversal tree, copied to the host."""
+        ex, cp, cnt = _ffi._vp(), _ffi._vp(), _ffi._u32()
+        check(self._lib.rtbvh_gpu_traversal_tree(self._h, ctypes.byref(ex), ctypes.byref(cp), ctypes.byref(cnt)),
+              "traversal_tree")
+        n = cnt.value
+        if n == 0:
+            return np.zeros((0, 32), np.float32), np.zeros((0, 16), np.uint32)
+        return device_copy(ex.value, (n, 32)), device_copy(cp.value, (n, 16), np.uint32)
+
     def intersect_host(self, rays, t_max=None, any_hit=False):
         """Same, with host (numpy) rays and hits, copies included
         (rtbvh_intersect_mbvh_batch)."""

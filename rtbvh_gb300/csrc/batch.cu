@@ -238,7 +238,13 @@ cudaError_t run_trace(Plan& p, cudaStream_t s) {
     a.seg_ray_off = p.ray_off.ptr;
     a.seg_root = p.mbase.ptr;
     a.seg_count = M;
-    a.qnodes = (p.flags & RTBVH_TRACE_EXACT_NODES) ? nullptr : p.qnodes.ptr;
+    if (!(p.flags & RTBVH_TRACE_EXACT_NODES)) {
+      // compact copies of the forest's own quad nodes (sorted near to far)
+      a.qnodes = p.qnodes.ptr;
+      a.qexact = p.mnodes.ptr;
+      a.q_count = p.node_cap;
+      a.seg_qroot = p.mbase.ptr;
+    }
     a.blocks_per_sm = p.trace_blocks_per_sm;
     a.ray_batch = p.trace_ray_batch;
     if ((e = launch_trace_mbvh(a, s))) return e;

@@ -28,7 +28,9 @@ struct Entry {
   uint32_t prim_count = 0;
   DAabb* d_nodes = nullptr;       // Bvh
   DMNode* d_mnodes = nullptr;     // Mbvh
-  DQNode* d_qnodes = nullptr;     // Mbvh: compact copies for closest hit
+  DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
+  DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
+  uint32_t wcount = 0;
   uint32_t* d_indices = nullptr;
   float4* d_tris = nullptr;       // 3 per index slot
   float* d_vertices = nullptr;    // prim-id order, 9 floats each
@@ -42,6 +44,7 @@ struct Entry {
     cudaFree(d_nodes);
     cudaFree(d_mnodes);
     cudaFree(d_qnodes);
+    cudaFree(d_wnodes);
     cudaFree(d_indices);
     cudaFree(d_tris);
     cudaFree(d_vertices);
@@ -49,6 +52,8 @@ struct Entry {
     d_nodes = nullptr;
     d_mnodes = nullptr;
     d_qnodes = nullptr;
+    d_wnodes = nullptr;
+    wcount = 0;
     d_indices = nullptr;
     d_tris = nullptr;
     d_vertices = nullptr;
@@ -601,10 +606,9 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
-  if ((err = dmalloc(&e->d_qnodes, e->node_count)) ||
-      (err = launch_quantize_mbvh(e->d_mnodes, e->node_count, e->d_qnodes, s))) {
+  if ((rc = build_wide(d_nodes, node_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount)) != Ok) {
     e->release();
-    return cuda_rc(err);
+    return rc;
   }
 
   if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
@@ -664,7 +668,11 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
     if (!e) return Error;
     if (!e->d_tris && e->node_count > 0) return InvalidArgument;
     a.mnodes = e->d_mnodes;
-    a.qnodes = (flags & RTBVH_TRACE_EXACT_NODES) ? nullptr : e->d_qnodes;
+    if (!(flags & RTBVH_TRACE_EXACT_NODES) && mbvh) {
+      a.qnodes = e->d_qnodes;
+      a.qexact = e->d_wnodes;
+      a.q_count = e->wcount;
+    }
     a.nodes = e->d_nodes;
     a.node_count = e->node_count;
     a.tris = e->d_tris;
@@ -761,6 +769,17 @@ ResultCode rtbvh_gpu_view(uint32_t structure_id, int is_mbvh, RTGpuView* view) {
   return Ok;
 }
 
+ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode** exact, const void** compact, uint32_t* count) {
+  if (exact == nullptr || compact == nullptr || count == nullptr) return Error;
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* e = lookup(mbvh.id, true);
+  if (!e) return Error;
+  *exact = reinterpret_cast<const RTMbvhNode*>(e->d_wnodes);
+  *compact = e->d_qnodes;
+  *count = e->wcount;
+  return Ok;
+}
+
 ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb* aabbs, uint32_t mbvh_id,
                            rtbvh_stream_t stream) {
   if ((vertices == nullptr) == (aabbs == nullptr)) return Error;
@@ -800,7 +819,12 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     }
     cudaFree(m->d_mnodes);
     m->d_mnodes = fresh;
-    if (m->d_qnodes && (err = launch_quantize_mbvh(m->d_mnodes, m->node_count, m->d_qnodes, s))) return cuda_rc(err);
+    cudaFree(m->d_qnodes);
+    cudaFree(m->d_wnodes);
+    m->d_qnodes = nullptr;
+    m->d_wnodes = nullptr;
+    m->wcount = 0;
+    if ((rc = build_wide(b->d_nodes, b->node_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok) return rc;
     if (vertices) {
       if (!m->d_vertices && (err = dmalloc(&m->d_vertices, 9 * n))) return cuda_rc(err);
       if (!m->d_tris && (err = dmalloc(&m->d_tris, (size_t)kTriFloat4 * n))) return cuda_rc(err);

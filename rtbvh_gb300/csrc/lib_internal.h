@@ -77,6 +77,12 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n,
 // Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here.
 ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes,
                       uint32_t* mnode_count);
+// The closest-hit traversal tree: a 4-wide collapse of the BVH2 with tight
+// slot boxes (largest-area child opened first), as exact nodes and compact
+// copies; *wcount nodes, root 0. No tree (*wcount 0, Ok) when a node's box
+// does not contain its children's (closest hit then reads the exact nodes).
+ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** wnodes, DQNode** wq,
+                      uint32_t* wcount);
 // Compact (64-byte) copies of quad nodes for the closest-hit traversal;
 // with live_count (device) only the first *live_count of `count` nodes.
 cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,
@@ -119,9 +125,14 @@ struct TraceArgs {
   // warp takes from the global ray counter at a time.
   uint32_t blocks_per_sm = 0;
   uint32_t ray_batch = 0;
-  // Optional compact copies of mnodes; closest-hit launches without
-  // statistics read them (any-hit and statistics keep the exact nodes).
+  // Optional closest-hit traversal tree (compact nodes `qnodes`, their
+  // exact copies `qexact`, `q_count` nodes, root 0 or seg_qroot[m] per mesh):
+  // closest-hit launches without statistics trace finite rays through it
+  // (any hit, statistics and other rays use mnodes).
   const DQNode* qnodes = nullptr;
+  const DMNode* qexact = nullptr;
+  uint32_t q_count = 0;
+  const uint32_t* seg_qroot = nullptr;
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);

@@ -668,3 +668,239 @@ cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* q
 }
 
 }  // namespace rtbvh
+
+// ---------------------------------------------------------------- traversal tree (4-wide, tight boxes)
+// A second 4-wide collapse of the BVH2 for the closest-hit traversal: each
+// node takes the two children of its BVH2 node and keeps opening the
+// interior child of largest half area until it has four slots (every slot
+// keeps its own BVH2 box; the reference Mbvh instead gives a leaf slot its
+// parent's box and opens strictly by depth). The tree is an internal
+// acceleration structure: its boxes contain every triangle of their
+// subtrees, so a traversal over it finds the same nearest hit.
+namespace rtbvh {
+
+namespace {
+
+struct WideParams {
+  const DAabb* nodes;
+  uint32_t node_count;
+  DMNode* wnodes;
+  uint32_t capacity;
+  uint32_t* walloc;   // next free traversal-node index
+  uint2* queue[2];
+  uint32_t* qcount;   // 3 rotating counters
+  GridBarrier* bar;
+  uint32_t* status;
+};
+
+__device__ void emit_wide(const WideParams& p, uint32_t c, uint32_t wi, uint2* next, uint32_t* next_count) {
+  uint32_t slot[4];
+  DAabb box[4];
+  int ns = 0;
+  const DAabb cur = load_aabb(p.nodes + c);
+  if (cur.count >= 0 || cur.left_first < 0) {
+    slot[0] = c;
+    box[0] = cur;
+    ns = 1;
+  } else if ((uint32_t)cur.left_first + 1u < p.node_count) {
+    slot[0] = (uint32_t)cur.left_first;
+    slot[1] = slot[0] + 1u;
+    box[0] = load_aabb(p.nodes + slot[0]);
+    box[1] = load_aabb(p.nodes + slot[1]);
+    ns = 2;
+    while (ns < 4) {
+      int best = -1;
+      float best_area = -1.0f;
+      for (int i = 0; i < ns; ++i) {
+        if (box[i].count >= 0 || box[i].left_first < 0) continue;
+        const float a = half_area(box[i].min[0], box[i].min[1], box[i].min[2], box[i].max[0], box[i].max[1],
+                                  box[i].max[2]);
+        if (a > best_area) {
+          best_area = a;
+          best = i;
+        }
+      }
+      if (best < 0) break;
+      const uint32_t lf = (uint32_t)box[best].left_first;
+      if (lf + 1u >= p.node_count) {
+        atomicOr(p.status, kStatusBadIndex);
+        break;
+      }
+      slot[best] = lf;
+      box[best] = load_aabb(p.nodes + lf);
+      slot[ns] = lf + 1u;
+      box[ns] = load_aabb(p.nodes + lf + 1u);
+      ++ns;
+    }
+  } else {
+    atomicOr(p.status, kStatusBadIndex);
+    return;
+  }
+  uint32_t n_int = 0;
+  for (int i = 0; i < ns; ++i) n_int += (box[i].count < 0 && box[i].left_first >= 0) ? 1u : 0u;
+  uint32_t base = 0;
+  if (n_int) {
+    base = atomicAdd(p.walloc, n_int);
+    if (base + n_int > p.capacity) {
+      atomicOr(p.status, kStatusBadIndex);
+      return;
+    }
+  }
+  DMNode m;
+  uint32_t k = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const DAabb& b = box[i < ns ? i : 0];
+    m.min_x[i] = b.min[0]; m.min_y[i] = b.min[1]; m.min_z[i] = b.min[2];
+    m.max_x[i] = b.max[0]; m.max_y[i] = b.max[1]; m.max_z[i] = b.max[2];
+    if (i >= ns) {
+      m.children[i] = -1;
+      m.counts[i] = -1;
+    } else if (b.count >= 0 || b.left_first < 0) {
+      m.children[i] = b.left_first;
+      m.counts[i] = b.count;
+    } else {
+      const uint32_t child = base + k++;
+      m.children[i] = (int32_t)child;
+      m.counts[i] = -1;
+      const uint32_t q = atomicAdd(next_count, 1u);
+      if (q < p.capacity) next[q] = make_uint2(slot[i], child);
+      else atomicOr(p.status, kStatusBadIndex);
+    }
+  }
+  float4* dst = reinterpret_cast<float4*>(p.wnodes + wi);
+  const float4* src = reinterpret_cast<const float4*>(&m);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) dst[j] = src[j];
+}
+
+__global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
+  const uint32_t G = gridDim.x;
+  const uint32_t tid = blockIdx.x * kBlock + threadIdx.x, nthreads = G * kBlock;
+  for (uint32_t level = 0; level < p.capacity + 1; ++level) {
+    uint32_t size = __ldcg(p.qcount + (level % 3));
+    if (size == 0) break;
+    if (size > p.capacity) size = p.capacity;  // only after a kStatusBadIndex
+    const uint2* q = p.queue[level & 1];
+    uint2* next = p.queue[(level + 1) & 1];
+    uint32_t* next_count = p.qcount + ((level + 1) % 3);
+    for (uint32_t k = tid; k < size; k += nthreads) {
+      const uint2 item = __ldcg(q + k);
+      emit_wide(p, item.x, item.y, next, next_count);
+    }
+    if (tid == 0) p.qcount[(level + 2) % 3] = 0;
+    if (!grid_sync(p.bar, G, p.status)) return;
+  }
+}
+
+// Nesting check: every interior node's box contains both children's boxes.
+// The traversal tree finds the nearest hit only if the boxes it reads
+// contain their triangles, which holds for nested trees (leaf boxes are
+// always built from their primitives). A binned-SAH tree can violate it:
+// the reference sizes a left child's box from the bins before
+// best_splits[axis].count, a primitive count, instead of the split bin
+// (src/builders/binned_sah.rs), so the reference's own traversal can miss
+// hits there, and only its exact node order reproduces them.
+__global__ void __launch_bounds__(kBlock) k_check_nested(const DAabb* __restrict__ nodes, uint32_t node_count,
+                                                          uint32_t* __restrict__ not_nested) {
+  const uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  const DAabb n = load_aabb(nodes + c);
+  if (n.count >= 0 || n.left_first < 0) return;
+  const uint32_t lf = (uint32_t)n.left_first;
+  if (lf + 1u >= node_count) {
+    atomicOr(not_nested, 1u);
+    return;
+  }
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const DAabb ch = load_aabb(nodes + lf + k);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ok = ok && ch.min[a] >= n.min[a] && ch.max[a] <= n.max[a];
+  }
+  if (!ok) atomicOr(not_nested, 1u);
+}
+
+__global__ void k_wide_init(uint2* queue0, uint32_t* qcount, uint32_t* walloc) {
+  if (threadIdx.x == 0) {
+    queue0[0] = make_uint2(0u, 0u);
+    qcount[0] = 1;
+    qcount[1] = 0;
+    qcount[2] = 0;
+    *walloc = 1;
+  }
+}
+
+}  // namespace
+
+ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** wnodes_out,
+                      DQNode** wq_out, uint32_t* wcount) {
+  *wnodes_out = nullptr;
+  *wq_out = nullptr;
+  *wcount = 0;
+  if (node_count == 0) return Ok;
+  // one traversal node per BVH2 interior node at most, or the root leaf
+  const uint32_t capacity = node_count < 3u ? 1u : (node_count + 1u) / 2u;
+  cudaError_t e;
+  Scratch<uint32_t> status, qcount, walloc;
+  Scratch<uint2> q0, q1;
+  Scratch<GridBarrier> bar;
+  if ((e = status.alloc(4, s)) || (e = qcount.alloc(4, s)) || (e = walloc.alloc(1, s)) || (e = q0.alloc(capacity, s)) ||
+      (e = q1.alloc(capacity, s)) || (e = bar.alloc(1, s)))
+    return cuda_rc(e);
+  DMNode* wn = nullptr;
+  DQNode* wq = nullptr;
+  auto fail = [&](ResultCode rc) {
+    cudaFree(wn);
+    cudaFree(wq);
+    return rc;
+  };
+  if ((e = cudaMalloc(&wn, (size_t)capacity * sizeof(DMNode)))) return fail(cuda_rc(e));
+  if ((e = cudaMemsetAsync(status.ptr, 0, 16, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
+    return fail(cuda_rc(e));
+  // status[1]: not nested -> no traversal tree (closest hit uses the exact nodes)
+  k_check_nested<<<(node_count + kBlock - 1) / kBlock, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
+  {
+    uint32_t nn = 0;
+    if ((e = cudaMemcpyAsync(&nn, status.ptr + 1, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+      return fail(cuda_rc(e));
+    if (nn) return fail(Ok);
+  }
+  k_wide_init<<<1, 32, 0, s>>>(q0.ptr, qcount.ptr, walloc.ptr);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wide_collapse, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  unsigned grid = (unsigned)(sm_count() * per_sm);
+  const unsigned useful = (capacity + kBlock - 1) / kBlock;
+  if (grid > useful) grid = useful;
+  if (grid < 1) grid = 1;
+  WideParams p;
+  p.nodes = nodes;
+  p.node_count = node_count;
+  p.wnodes = wn;
+  p.capacity = capacity;
+  p.walloc = walloc.ptr;
+  p.queue[0] = q0.ptr;
+  p.queue[1] = q1.ptr;
+  p.qcount = qcount.ptr;
+  p.bar = bar.ptr;
+  p.status = status.ptr;
+  void* args[] = {&p};
+  if ((e = cudaLaunchCooperativeKernel((void*)k_wide_collapse, dim3(grid), dim3(kBlock), args, 0, s)))
+    return fail(cuda_rc(e));
+  uint32_t h[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(h, walloc.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+    return fail(cuda_rc(e));
+  if (h[1] != 0) return fail((h[1] & kStatusTimeout) ? Timeout : Error);
+  if (h[0] == 0 || h[0] > capacity) return fail(Error);
+  if ((e = cudaMalloc(&wq, (size_t)h[0] * sizeof(DQNode)))) return fail(cuda_rc(e));
+  if ((e = launch_quantize_mbvh(wn, h[0], wq, s))) return fail(cuda_rc(e));
+  *wnodes_out = wn;
+  *wq_out = wq;
+  *wcount = h[0];
+  return Ok;
+}
+
+}  // namespace rtbvh

@@ -200,6 +200,8 @@ __device__ __forceinline__ void quad_intersect_q(const float (&h0)[8], const flo
     tmin[i] = tn;
     if ((tx >= tn) && (tn < r.t)) m |= 1u << i;
   }
+  // a full 4-element sorting network (near to far); the reference's last
+  // comparator is (2, 3), which leaves slots 1 and 2 unordered
   uint32_t i0 = 0, i1 = 1, i2 = 2, i3 = 3;
   float t0 = tmin[0], t1 = tmin[1], t2 = tmin[2], t3 = tmin[3], tt;
   uint32_t ti;
@@ -207,7 +209,7 @@ __device__ __forceinline__ void quad_intersect_q(const float (&h0)[8], const flo
   if (t2 > t3) { tt = t2; t2 = t3; t3 = tt; ti = i2; i2 = i3; i3 = ti; }
   if (t0 > t2) { tt = t0; t0 = t2; t2 = tt; ti = i0; i0 = i2; i2 = ti; }
   if (t1 > t3) { tt = t1; t1 = t3; t3 = tt; ti = i1; i1 = i3; i3 = ti; }
-  if (t2 > t3) { ti = i2; i2 = i3; i3 = ti; }
+  if (t1 > t2) { ti = i1; i1 = i2; i2 = ti; }
   mask = m;
   ids = i0 | (i1 << 2) | (i2 << 4) | (i3 << 6);
 }
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     if (COMPACT)
       compact = fast && fabsf(ray.ox) <= kQuantRange && fabsf(ray.oy) <= kQuantRange &&
                 fabsf(ray.oz) <= kQuantRange && fabsf(ray.ix) <= kQuantRange && fabsf(ray.iy) <= kQuantRange &&
-                fabsf(ray.iz) <= kQuantRange;
+                fabsf(ray.iz) <= kQuantRange && a.q_count > 0;
     hu = hv = 0.0f;
     prim = -1;
     visits = tests = max_depth = 0;
@@ -289,6 +291,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
           }
         }
         next = (int32_t)root;
+        if (COMPACT && compact) next = (int32_t)__ldg(a.seg_qroot + lo);
       }
     }
   };
@@ -333,30 +336,64 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     // ---- one quad node
     const int32_t current = next >= 0 ? next : stack[sp--];
     next = -1;
-    if ((uint32_t)current >= a.node_count) {
+    if ((uint32_t)current >= ((COMPACT && compact) ? a.q_count : a.node_count)) {
       atomicOr(a.status, kStatusBadIndex);
       active = false;
       continue;
     }
     uint32_t mask, ids;
     int4 children, counts;
-    bool exact = true;
+    bool done = false;
     if (COMPACT && compact) {
+      // traversal tree: slots sorted near to far; leaves are tested as they
+      // come, the nearest interior child is visited next and the others are
+      // stacked so that they pop near to far
       const float* qn = reinterpret_cast<const float*>(a.qnodes + current);
       float h0[8], h1[8];
       ld8(qn, h0);
       ld8(qn + 8, h1);
       if (!(__float_as_uint(h0[3]) >> 24)) {
         quad_intersect_q(h0, h1, ray, mask, ids, children, counts);
-        exact = false;
+      } else {
+        quad_intersect<true>(a.qexact + current, ray, mask, ids, children, counts);
+        // quad_intersect orders far slots last with the reference's network; any order is valid here
       }
-    }
-    if (exact) {
-      if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
-      else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
-    }
+      const uint32_t inner_mask = mask & ((counts.x <= -1 && children.x > -1) ? 1u : 0u) |
+                                  mask & ((counts.y <= -1 && children.y > -1) ? 2u : 0u) |
+                                  mask & ((counts.z <= -1 && children.z > -1) ? 4u : 0u) |
+                                  mask & ((counts.w <= -1 && children.w > -1) ? 8u : 0u);
+      const int inner = __popc(inner_mask);
+      if (sp + inner > kStack) {
+        atomicOr(a.status, kStatusStackOverflow);
+        prim = -2;
+        done = true;
+      } else {
+        int k = 0;
+#pragma unroll 1
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t id = (ids >> (2 * i)) & 3u;
+          if (!((mask >> id) & 1u)) continue;
+          const int32_t count = sel4(counts, id);
+          const int32_t lf = sel4(children, id);
+          if (count > -1) {
+            if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
+              atomicOr(a.status, kStatusBadIndex);
+              done = true;
+              break;
+            }
+            for (int32_t j = 0; j < count; ++j) mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim);
+          } else if (lf > -1) {
+            if (k == 0) next = lf;
+            else stack[sp + inner - k] = lf;
+            ++k;
+          }
+        }
+        if (inner > 1) sp += inner - 1;
+      }
+    } else {
+    if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
+    else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
     if (STATS) ++visits;
-    bool done = false;
 #pragma unroll 1
     for (int i = 0; i < 4; ++i) {
       const uint32_t id = (ids >> (2 * (3 - i))) & 3u;
@@ -394,6 +431,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         next = lf;
         if (STATS && (uint32_t)(sp + 2) > max_depth) max_depth = (uint32_t)(sp + 2);
       }
+    }
     }
     if (done || (next < 0 && sp < 0)) {
       a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));

@@ -9,7 +9,7 @@ import torch
 import oracle
 import rtbvh_gb300 as rb
 from rtbvh_gb300 import diff, scenes
-from gpu_helpers import to_cuda, u32
+from gpu_helpers import assert_same_nearest, to_cuda, u32
 
 pytestmark = pytest.mark.gpu
 
@@ -183,5 +183,6 @@ def test_vertex_step_then_gpu_refit(setup):
     assert np.array_equal(u32(nodes)[:, cols], u32(ref)[:, cols])
     h2, _ = mbvh.intersect(d_rays)
     oh, _, _ = oracle.trace("mbvh", oracle.mbvh(nodes), bvh.indices(), moved.reshape(-1, 9), rays)
-    assert np.array_equal(u32(h2.cpu().numpy()[:, :3]), u32(oh[:, :3]))
-    assert (rb.hit_prims(h2.cpu().numpy()) == oracle.hit_prims(oh)).mean() > 0.999
+    # the refitted tree is nested, so closest hit runs on the traversal tree:
+    # the same nearest hit as the reference's traversal, ties aside
+    assert_same_nearest(h2.cpu().numpy(), oh, moved, rays)

@@ -10,7 +10,7 @@ import torch
 import oracle
 import rtbvh_gb300 as rb
 from rtbvh_gb300 import _ffi, scenes
-from gpu_helpers import gpu_build, oracle_build, rays_for, scene, to_cuda, u32
+from gpu_helpers import assert_same_nearest, gpu_build, oracle_build, rays_for, scene, to_cuda, u32
 
 pytestmark = pytest.mark.gpu
 
@@ -257,39 +257,6 @@ def test_hit_t_error_against_fp64():
     assert rel.max() < 1e-4
 
 
-def _mt_t(tri, ray):
-    """The reference's triangle test in float32 (no contraction) for one
-    triangle and ray; t or None."""
-    f32 = np.float32
-    v0, v1, v2 = (tri[k].astype(f32) for k in range(3))
-    o, d = ray[:3].astype(f32), ray[3:].astype(f32)
-    e1, e2 = v1 - v0, v2 - v0
-    h = np.array([d[1] * e2[2] - e2[1] * d[2], d[2] * e2[0] - e2[2] * d[0], d[0] * e2[1] - e2[0] * d[1]], f32)
-    det = f32(f32(e1[0] * h[0]) + f32(e1[1] * h[1])) + f32(e1[2] * h[2])
-    if -1e-5 < det < 1e-5:
-        return None
-    f = f32(1.0) / det
-    s = o - v0
-    q = np.array([s[1] * e1[2] - e1[1] * s[2], s[2] * e1[0] - e1[2] * s[0], s[0] * e1[1] - e1[0] * s[1]], f32)
-    return f * (f32(f32(e2[0] * q[0]) + f32(e2[1] * q[1])) + f32(e2[2] * q[2]))
-
-
-def assert_same_nearest(hits, ref, tris, rays, max_tie_frac=1e-4):
-    """Same nearest hit as `ref`: t bit-identical on every ray; the triangle
-    (and its u, v) identical unless the reported one is hit at exactly the
-    same t (a tie, which the compact-node traversal may resolve differently)."""
-    assert np.array_equal(u32(hits[:, 0]), u32(ref[:, 0])), "t differs"
-    p, q = rb.hit_prims(hits), rb.hit_prims(ref)
-    diff = np.nonzero(p != q)[0]
-    for r in diff:
-        assert p[r] >= 0 and q[r] >= 0
-        t = _mt_t(tris[p[r]], rays[r])
-        assert t is not None and np.float32(t).view(np.uint32) == hits[r, 0].view(np.uint32), f"ray {r}: not a tie"
-    same = p == q
-    assert np.array_equal(u32(hits[same]), u32(ref[same]))
-    assert len(diff) <= max(1, int(max_tie_frac * len(hits))), f"{len(diff)} ties"
-
-
 @pytest.mark.parametrize("name", SCENES)
 @pytest.mark.parametrize("kind", ["locb", "sah"])
 def test_compact_nodes_same_nearest_hit(name, kind):
@@ -330,3 +297,65 @@ def test_compact_nodes_out_of_range_values():
     on, oi = oracle_build(tris, "locb")
     oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, stats=False)
     assert_same_nearest(hits, oh, tris, rays)
+
+
+def _decode_axis(lo, e, word):
+    step = np.float64(2.0) ** (int(e) - 127)
+    return np.array([np.float64(lo) + ((int(word) >> (8 * i)) & 0xff) * step for i in range(4)])
+
+
+@pytest.mark.parametrize("name", ["teapot", "incoherent_20k"])
+def test_traversal_tree_boxes_contain_and_cover(name):
+    """The closest-hit traversal tree: each compact slot box contains its
+    exact box, each exact slot box contains its subtree, and every
+    primitive slot is in exactly one leaf."""
+    tris = scene(name)
+    g = gpu_build(tris, "locb")
+    m = rb.Mbvh.construct(g)
+    ex, cp = m.traversal_tree()
+    assert len(ex) > 0 and len(ex) == len(cp)
+    exi = ex.view(np.int32)
+    seen = np.zeros(len(tris), np.int32)
+    for k in range(len(ex)):
+        lo = cp[k, 0:3].view(np.float32)
+        exps = int(cp[k, 3])
+        assert exps >> 24 == 0
+        for ax, (wl, wh) in enumerate(((cp[k, 4], cp[k, 5]), (cp[k, 6], cp[k, 7]), (cp[k, 8], cp[k, 9]))):
+            e = (exps >> (8 * ax)) & 0xff
+            dl, dh = _decode_axis(lo[ax], e, wl), _decode_axis(lo[ax], e, wh)
+            assert (dl <= ex[k, 8 * ax:8 * ax + 4].astype(np.float64)).all()
+            assert (dh >= ex[k, 8 * ax + 4:8 * ax + 8].astype(np.float64)).all()
+        for i in range(4):
+            ch, cnt = exi[k, 24 + i], exi[k, 28 + i]
+            if cnt >= 0:
+                seen[ch:ch + cnt] += 1
+            elif ch >= 0:
+                # child node's slots lie inside this slot's box
+                for ax in range(3):
+                    assert ex[ch, 8 * ax:8 * ax + 4].min() >= ex[k, 8 * ax + i]
+                    assert ex[ch, 8 * ax + 4:8 * ax + 8].max() <= ex[k, 8 * ax + 4 + i]
+    assert (seen == 1).all()
+
+
+def test_non_nested_sah_tree_keeps_exact_nodes():
+    """A binned-SAH tree whose node boxes do not contain their children's
+    (the reference's left-box rule) gets no traversal tree: closest hit then
+    reads the exact nodes and equals the reference's traversal bit for bit."""
+    tris = scenes.sphere()
+    g = gpu_build(tris, "sah")
+    nodes = g.nodes()
+    ints = nodes.view(np.int32)
+    inner = np.nonzero((ints[:, 3] < 0) & (ints[:, 7] >= 0))[0]
+    lf = ints[inner, 7]
+    nested = all(((nodes[lf + k, 0:3] >= nodes[inner, 0:3]) & (nodes[lf + k, 4:7] <= nodes[inner, 4:7])).all()
+                 for k in (0, 1))
+    m = rb.Mbvh.construct(g)
+    ex, _ = m.traversal_tree()
+    assert (len(ex) > 0) == nested
+    rays, _ = rays_for("sphere")
+    hits = m.intersect(to_cuda(rays))[0].cpu().numpy()
+    exact = m.intersect(to_cuda(rays), exact_nodes=True)[0].cpu().numpy()
+    if not nested:
+        assert np.array_equal(u32(hits), u32(exact))
+    else:
+        assert_same_nearest(hits, exact, tris, rays)
