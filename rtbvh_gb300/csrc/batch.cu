@@ -10,8 +10,9 @@
 //      mesh, one block per small mesh, the two sets concurrently;
 //   4. parent pointers and quad-subtree counts over the whole forest, then
 //      one block per mesh for the top-down MBVH collapse (mbvh.cu);
-//   5. leaf-ordered triangles and ONE persistent traversal launch for all
-//      rays, each ray starting at its mesh's root quad node.
+//   5. leaf-ordered triangles, per-mesh closest-hit traversal trees (one
+//      block per mesh, see build_wide) and ONE persistent traversal launch
+//      for all rays, each ray starting at its mesh's root.
 // Every buffer is allocated when the plan is created, and the whole
 // pipeline is captured in a CUDA graph that rtbvh_gpu_batch_run replays.
 // Per mesh, the result equals the single-mesh build's, with node, leaf and
@@ -144,7 +145,8 @@ struct Plan {
   DevBuf<DAabb> aabbs, worlds, lvl0, lvl1, nodes;
   DevBuf<float4> centers, tris;
   DevBuf<DMNode> mnodes;
-  DevBuf<DQNode> qnodes;
+  DevBuf<DMNode> wnodes;  // per-mesh closest-hit traversal trees (exact), mesh m at [off_m, off_m + n_m)
+  DevBuf<DQNode> qnodes;  // the same, compact
   DevBuf<uint2> q0, q1;
   DevBuf<char> sort_temp;
   size_t sort_bytes = 0;
@@ -212,10 +214,10 @@ cudaError_t run_build(Plan& p, cudaStream_t s) {
                                     p.mnodes.ptr, p.node_cap, p.status.ptr, mesh_blocks(M), s)))
     return e;
   if ((e = launch_gather_triangles(p.vertices, p.vals.ptr, N, p.tris.ptr, s))) return e;
-  // compact quad nodes for the closest-hit traversal (the forest's quad
-  // count, mbase[M], is read on the device)
+  // closest-hit traversal trees (LOCB trees are nested, see build_wide)
   if (!(p.flags & (RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_EXACT_NODES)) &&
-      (e = launch_quantize_mbvh(p.mnodes.ptr, p.node_cap, p.qnodes.ptr, s, p.mbase.ptr + M)))
+      (e = launch_wide_segments(p.nodes.ptr, p.node_cap, p.prim_off.ptr, p.order.ptr, M, N, p.wnodes.ptr,
+                                p.qnodes.ptr, p.q0.ptr, p.q1.ptr, p.status.ptr, mesh_blocks(M), s)))
     return e;
   return cudaGetLastError();
 }
@@ -238,12 +240,11 @@ cudaError_t run_trace(Plan& p, cudaStream_t s) {
     a.seg_ray_off = p.ray_off.ptr;
     a.seg_root = p.mbase.ptr;
     a.seg_count = M;
-    if (!(p.flags & RTBVH_TRACE_EXACT_NODES)) {
-      // compact copies of the forest's own quad nodes (sorted near to far)
+    if (!(p.flags & (RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_EXACT_NODES))) {
       a.qnodes = p.qnodes.ptr;
-      a.qexact = p.mnodes.ptr;
-      a.q_count = p.node_cap;
-      a.seg_qroot = p.mbase.ptr;
+      a.qexact = p.wnodes.ptr;
+      a.q_count = N;
+      a.seg_qroot = p.prim_off.ptr;  // mesh m's traversal tree starts at off_m
     }
     a.blocks_per_sm = p.trace_blocks_per_sm;
     a.ray_batch = p.trace_ray_batch;
@@ -365,7 +366,7 @@ ResultCode rtbvh_gpu_batch_create(const float* vertices, const uint32_t* prim_of
       (e = p->status.alloc(4)) || (e = p->aabbs.alloc(N)) || (e = p->worlds.alloc(mesh_count)) ||
       (e = p->lvl0.alloc(p->node_cap)) || (e = p->lvl1.alloc(p->node_cap)) || (e = p->nodes.alloc(p->node_cap)) ||
       (e = p->centers.alloc(N)) || (e = p->tris.alloc((size_t)kTriFloat4 * N)) ||
-      (e = p->mnodes.alloc(p->node_cap)) || (e = p->qnodes.alloc(p->node_cap)) || (e = p->q0.alloc(2 * (size_t)p->node_cap)) ||
+      (e = p->mnodes.alloc(p->node_cap)) || (e = p->qnodes.alloc(N)) || (e = p->wnodes.alloc(N)) || (e = p->q0.alloc(2 * (size_t)p->node_cap)) ||
       (e = p->q1.alloc(2 * (size_t)p->node_cap)) || (e = p->sort_temp.alloc(p->sort_bytes)))
     return cuda_rc(e);
   if ((e = cudaMemcpyAsync(p->prim_off.ptr, prim_offsets, 4 * (size_t)(mesh_count + 1), cudaMemcpyHostToDevice, s)) ||

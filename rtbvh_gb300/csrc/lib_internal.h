@@ -83,6 +83,12 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
 // does not contain its children's (closest hit then reads the exact nodes).
 ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** wnodes, DQNode** wq,
                       uint32_t* wcount);
+// Traversal trees of a concatenated forest (LOCB meshes): mesh m's tree in
+// nodes [off_m, off_m + n_m) of wnodes (exact) and wq (compact), root off_m;
+// q0/q1 hold total_prims entries each.
+cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const uint32_t* prim_off,
+                                 const uint32_t* order, uint32_t mesh_count, uint32_t total_prims, DMNode* wnodes,
+                                 DQNode* wq, uint2* q0, uint2* q1, uint32_t* status, unsigned blocks, cudaStream_t s);
 // Compact (64-byte) copies of quad nodes for the closest-hit traversal;
 // with live_count (device) only the first *live_count of `count` nodes.
 cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,

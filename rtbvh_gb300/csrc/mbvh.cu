@@ -693,7 +693,19 @@ struct WideParams {
   uint32_t* status;
 };
 
-__device__ void emit_wide(const WideParams& p, uint32_t c, uint32_t wi, uint2* next, uint32_t* next_count) {
+// Traversal node wi from BVH2 node c. Interior slots get indices from
+// *alloc (below alloc_end) and are appended to `next` (next_cap entries).
+struct WideCtx {
+  const DAabb* nodes;
+  uint32_t node_count;
+  DMNode* wnodes;
+  uint32_t* alloc;
+  uint32_t alloc_end;
+  uint32_t next_cap;
+  uint32_t* status;
+};
+
+__device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next, uint32_t* next_count) {
   uint32_t slot[4];
   DAabb box[4];
   int ns = 0;
@@ -740,8 +752,8 @@ __device__ void emit_wide(const WideParams& p, uint32_t c, uint32_t wi, uint2* n
   for (int i = 0; i < ns; ++i) n_int += (box[i].count < 0 && box[i].left_first >= 0) ? 1u : 0u;
   uint32_t base = 0;
   if (n_int) {
-    base = atomicAdd(p.walloc, n_int);
-    if (base + n_int > p.capacity) {
+    base = atomicAdd(p.alloc, n_int);
+    if (base + n_int > p.alloc_end) {
       atomicOr(p.status, kStatusBadIndex);
       return;
     }
@@ -764,7 +776,7 @@ __device__ void emit_wide(const WideParams& p, uint32_t c, uint32_t wi, uint2* n
       m.children[i] = (int32_t)child;
       m.counts[i] = -1;
       const uint32_t q = atomicAdd(next_count, 1u);
-      if (q < p.capacity) next[q] = make_uint2(slot[i], child);
+      if (q < p.next_cap) next[q] = make_uint2(slot[i], child);
       else atomicOr(p.status, kStatusBadIndex);
     }
   }
@@ -777,6 +789,14 @@ __device__ void emit_wide(const WideParams& p, uint32_t c, uint32_t wi, uint2* n
 __global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
   const uint32_t G = gridDim.x;
   const uint32_t tid = blockIdx.x * kBlock + threadIdx.x, nthreads = G * kBlock;
+  WideCtx ctx;
+  ctx.nodes = p.nodes;
+  ctx.node_count = p.node_count;
+  ctx.wnodes = p.wnodes;
+  ctx.alloc = p.walloc;
+  ctx.alloc_end = p.capacity;
+  ctx.next_cap = p.capacity;
+  ctx.status = p.status;
   for (uint32_t level = 0; level < p.capacity + 1; ++level) {
     uint32_t size = __ldcg(p.qcount + (level % 3));
     if (size == 0) break;
@@ -786,7 +806,7 @@ __global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
     uint32_t* next_count = p.qcount + ((level + 1) % 3);
     for (uint32_t k = tid; k < size; k += nthreads) {
       const uint2 item = __ldcg(q + k);
-      emit_wide(p, item.x, item.y, next, next_count);
+      emit_wide(ctx, item.x, item.y, next, next_count);
     }
     if (tid == 0) p.qcount[(level + 2) % 3] = 0;
     if (!grid_sync(p.bar, G, p.status)) return;
@@ -832,7 +852,67 @@ __global__ void k_wide_init(uint2* queue0, uint32_t* qcount, uint32_t* walloc) {
   }
 }
 
+// Many meshes: one block per mesh builds the mesh's traversal tree in the
+// node range [off_m, off_m + n_m) (a mesh of n primitives has at most n - 1
+// interior BVH2 nodes), root at off_m, with the frontier in the same range
+// of the two queues.
+__global__ void __launch_bounds__(kBlock)
+    k_wide_segments(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ prim_off,
+                    const uint32_t* __restrict__ order, uint32_t mesh_count, DMNode* wnodes, uint2* q0, uint2* q1,
+                    uint32_t* status) {
+  __shared__ uint32_t s_count[2];
+  __shared__ uint32_t s_alloc;
+  for (uint32_t q = blockIdx.x; q < mesh_count; q += gridDim.x) {
+    const uint32_t m = order[q];
+    const uint32_t off = prim_off[m], n = prim_off[m + 1] - off;
+    if (n == 0) continue;
+    WideCtx ctx;
+    ctx.nodes = nodes;
+    ctx.node_count = node_count;
+    ctx.wnodes = wnodes;
+    ctx.alloc = &s_alloc;
+    ctx.alloc_end = off + n;
+    ctx.next_cap = n;
+    ctx.status = status;
+    if (threadIdx.x == 0) {
+      q0[off] = make_uint2(2u * off - m, off);
+      s_count[0] = 1;
+      s_count[1] = 0;
+      s_alloc = off + 1u;
+    }
+    __syncthreads();
+    int cur = 0;
+    for (uint32_t level = 0; level <= n; ++level) {
+      uint32_t size = s_count[cur];
+      if (size == 0) break;
+      if (size > n) size = n;
+      const uint2* qin = (cur ? q1 : q0) + off;
+      uint2* qout = (cur ? q0 : q1) + off;
+      for (uint32_t k = threadIdx.x; k < size; k += kBlock) {
+        const uint2 item = qin[k];
+        emit_wide(ctx, item.x, item.y, qout, &s_count[cur ^ 1]);
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) s_count[cur] = 0;
+      __syncthreads();
+      cur ^= 1;
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const uint32_t* prim_off,
+                                 const uint32_t* order, uint32_t mesh_count, uint32_t total_prims, DMNode* wnodes,
+                                 DQNode* wq, uint2* q0, uint2* q1, uint32_t* status, unsigned blocks, cudaStream_t s) {
+  if (mesh_count == 0 || total_prims == 0) return cudaSuccess;
+  k_wide_segments<<<blocks, kBlock, 0, s>>>(nodes, node_count, prim_off, order, mesh_count, wnodes, q0, q1, status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // slots of a mesh's range past its own tree are converted too and never read
+  return launch_quantize_mbvh(wnodes, total_prims, wq, s);
+}
 
 ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** wnodes_out,
                       DQNode** wq_out, uint32_t* wcount) {

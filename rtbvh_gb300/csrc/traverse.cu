@@ -345,9 +345,10 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     int4 children, counts;
     bool done = false;
     if (COMPACT && compact) {
-      // traversal tree: slots sorted near to far; leaves are tested as they
-      // come, the nearest interior child is visited next and the others are
-      // stacked so that they pop near to far
+      // traversal tree: slots sorted near to far and visited far to near, as
+      // in the reference's loop (a leaf's triangles at once, interior slots
+      // pushed, the nearest one visited next); this simple loop keeps the
+      // kernel free of spills, which pays more than testing leaves near first
       const float* qn = reinterpret_cast<const float*>(a.qnodes + current);
       float h0[8], h1[8];
       ld8(qn, h0);
@@ -356,39 +357,32 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         quad_intersect_q(h0, h1, ray, mask, ids, children, counts);
       } else {
         quad_intersect<true>(a.qexact + current, ray, mask, ids, children, counts);
-        // quad_intersect orders far slots last with the reference's network; any order is valid here
       }
-      const uint32_t inner_mask = mask & ((counts.x <= -1 && children.x > -1) ? 1u : 0u) |
-                                  mask & ((counts.y <= -1 && children.y > -1) ? 2u : 0u) |
-                                  mask & ((counts.z <= -1 && children.z > -1) ? 4u : 0u) |
-                                  mask & ((counts.w <= -1 && children.w > -1) ? 8u : 0u);
-      const int inner = __popc(inner_mask);
-      if (sp + inner > kStack) {
-        atomicOr(a.status, kStatusStackOverflow);
-        prim = -2;
-        done = true;
-      } else {
-        int k = 0;
 #pragma unroll 1
-        for (int i = 0; i < 4; ++i) {
-          const uint32_t id = (ids >> (2 * i)) & 3u;
-          if (!((mask >> id) & 1u)) continue;
-          const int32_t count = sel4(counts, id);
-          const int32_t lf = sel4(children, id);
-          if (count > -1) {
-            if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
-              atomicOr(a.status, kStatusBadIndex);
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t id = (ids >> (2 * (3 - i))) & 3u;
+        if (!((mask >> id) & 1u)) continue;
+        const int32_t count = sel4(counts, id);
+        const int32_t lf = sel4(children, id);
+        if (count > -1) {
+          if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
+            atomicOr(a.status, kStatusBadIndex);
+            done = true;
+            break;
+          }
+          for (int32_t j = 0; j < count; ++j) mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim);
+        } else if (lf > -1) {
+          if (next >= 0) {
+            if (sp + 1 >= kStack) {
+              atomicOr(a.status, kStatusStackOverflow);
+              prim = -2;
               done = true;
               break;
             }
-            for (int32_t j = 0; j < count; ++j) mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim);
-          } else if (lf > -1) {
-            if (k == 0) next = lf;
-            else stack[sp + inner - k] = lf;
-            ++k;
+            stack[++sp] = next;
           }
+          next = lf;
         }
-        if (inner > 1) sp += inner - 1;
       }
     } else {
     if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
