@@ -345,8 +345,14 @@ def workload_sphere_sah(with_cpu):
     mbvh_ms = _cuda_time(lambda: rb.Mbvh.construct(holder["bvh"], host_mirror=False))
     m = holder["mbvh"]
     trace_ms = _cuda_time(lambda: m.intersect(d_rays), reps=10)
+    # packets of four horizontally adjacent pixels, as examples/benchmark.rs:127-140
+    pk_mbvh_ms = _cuda_time(lambda: m.intersect_packets(d_rays), reps=10)
+    pk_bvh_ms = _cuda_time(lambda: holder["bvh"].intersect_packets(d_rays), reps=10)
     out = {"triangles": len(tris), "rays": len(rays), "sah_build_ms": round(sah_ms, 3),
-           "mbvh_ms": round(mbvh_ms, 3), "closest_hit_mrays": round(len(rays) / (trace_ms * 1e-3) / 1e6, 1)}
+           "mbvh_ms": round(mbvh_ms, 3), "closest_hit_mrays": round(len(rays) / (trace_ms * 1e-3) / 1e6, 1),
+           "packets": {"mbvh_mrays": round(len(rays) / (pk_mbvh_ms * 1e-3) / 1e6, 1),
+                       "bvh_mrays": round(len(rays) / (pk_bvh_ms * 1e-3) / 1e6, 1),
+                       "packet": "4 horizontally adjacent pixels, packet triangle test"}}
     if with_cpu:
         import oracle
         threads = os.cpu_count() or 1
@@ -359,8 +365,11 @@ def workload_sphere_sah(with_cpu):
         t0 = time.perf_counter()
         oracle.trace("mbvh", mn, idx, tris.reshape(-1, 9), rays, threads=threads, stats=False)
         cpu_rays = len(rays) / (time.perf_counter() - t0) / 1e6
+        t0 = time.perf_counter()
+        oracle.trace_packets("mbvh", mn, idx, tris.reshape(-1, 9), rays, threads=threads)
+        cpu_pk = len(rays) / (time.perf_counter() - t0) / 1e6
         out["cpu_baseline"] = {"sah_build_ms": round(cpu_build, 3), "closest_hit_mrays": round(cpu_rays, 2),
-                               "cores": threads, "kind": "port"}
+                               "packets_mbvh_mrays": round(cpu_pk, 2), "cores": threads, "kind": "port"}
     return out
 
 

@@ -210,6 +210,34 @@ ResultCode rtbvh_gpu_intersect_mbvh(RTMbvh mbvh, const float *rays, const float 
 ResultCode rtbvh_gpu_intersect_bvh(RTBvh bvh, const float *rays, const float *t_max, uintptr_t ray_count,
                                    float *hits, uint32_t flags, uint32_t *stats, rtbvh_stream_t stream);
 
+/* Packets of four rays: intersect_mbvh_packet (rtbvh_ffi/src/lib.rs:749-835)
+ * over MbvhPacketIndexIterator (src/iter_indices.rs:316-414) for
+ * packet_count packets at once, on the device, with the reference's packet
+ * triangle test SpatialTriangle::intersect4 (src/builders/spatial_sah.rs:
+ * 165-244, t_min 1e-4) as the candidate callback (examples/benchmark.rs:
+ * 43-68). The six ray arrays and t are device arrays of 4 * packet_count
+ * floats in the FFI's SoA form: lane k of packet p is element 4p + k. t is
+ * in/out like the FFI's t (initial bound in, nearest accepted t out).
+ * hits (R x 4: t, u, v, prim; NULL to skip) and stats (3 uint32 per packet:
+ * node tests, triangle tests, max stack depth; with RTBVH_TRACE_STATS) are
+ * optional. A node is entered when any lane of the packet hits it, so each
+ * lane's nearest hit is the nearest its packet test accepts. RTBVH_TRACE_ANY_HIT
+ * and RTBVH_TRACE_REORDER are not supported here (InvalidArgument); NaN
+ * inputs are traced as the iterator traces them (the FFI's early Nan return
+ * is the caller's check). Asynchronous on `stream`. */
+ResultCode rtbvh_gpu_intersect_mbvh_packets(RTMbvh mbvh, const float *origin_x, const float *origin_y,
+                                            const float *origin_z, const float *direction_x, const float *direction_y,
+                                            const float *direction_z, float *t, uintptr_t packet_count, float *hits,
+                                            uint32_t flags, uint32_t *stats, rtbvh_stream_t stream);
+
+/* intersect_packet (rtbvh_ffi/src/lib.rs:599-686) over BvhPacketIndexIterator
+ * (src/iter_indices.rs:110-200), same arrays and rules as above; a packet
+ * with a NaN origin or direction component walks nothing. */
+ResultCode rtbvh_gpu_intersect_bvh_packets(RTBvh bvh, const float *origin_x, const float *origin_y,
+                                           const float *origin_z, const float *direction_x, const float *direction_y,
+                                           const float *direction_z, float *t, uintptr_t packet_count, float *hits,
+                                           uint32_t flags, uint32_t *stats, rtbvh_stream_t stream);
+
 /* Same as rtbvh_gpu_intersect_mbvh with HOST rays / t_max / hits: copies in,
  * traces and copies out in chunks on two internal streams, and returns when
  * the hits are in host memory. Page-locked host buffers give full speed. */

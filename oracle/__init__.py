@@ -46,6 +46,10 @@ def lib():
         L.ror_trace.argtypes = [ctypes.c_int32, f32p, ctypes.c_size_t, u32p, f32p, f32p, ctypes.c_size_t,
                                 f32p, ctypes.c_float, ctypes.c_int32, f32p, u32p, ctypes.c_uint32]
         L.ror_trace.restype = ctypes.c_int64
+        L.ror_trace_packets.argtypes = [ctypes.c_int32, f32p, ctypes.c_size_t, u32p, f32p,
+                                        ctypes.POINTER(f32p), f32p, ctypes.c_size_t, ctypes.c_float,
+                                        f32p, u32p, ctypes.c_uint32]
+        L.ror_trace_packets.restype = ctypes.c_int64
         _lib = L
     return _lib
 
@@ -163,6 +167,31 @@ def trace(structure: str, nodes, prim_indices, tris, rays, t_max=None, t_min_tri
     bad = lib().ror_trace(st, _f(nd), len(nd), _u(idx), _f(tr), _f(ry), R,
                           _f(tm) if tm is not None else None, float(t_min_tri), int(bool(any_hit)),
                           _f(hits), _u(sts) if sts is not None else None, threads)
+    return hits, sts, int(bad)
+
+
+def trace_packets(structure: str, nodes, prim_indices, tris, rays, t=None, t_min_tri=1e-4, threads: int = 1):
+    """Packet traversal; packet p = rays 4p..4p+3 (len(rays) must be a multiple of 4).
+
+    Returns (hits (R,4) float32 [t,u,v,prim bits], stats (P,3) uint32, overflows).
+    """
+    st = {"mbvh": 0, "bvh": 1}[structure]
+    nd = _c(nodes, np.float32).reshape(-1, 32 if st == 0 else 8)
+    idx = _c(prim_indices, np.uint32)
+    tr = _c(tris, np.float32).reshape(-1, 9)
+    ry = _c(rays, np.float32).reshape(-1, 6)
+    R = len(ry)
+    if R % 4:
+        raise ValueError("packet traversal needs a multiple of 4 rays")
+    P = R // 4
+    soa = [np.ascontiguousarray(ry[:, k]) for k in range(6)]
+    tt = np.full(R, 1e34, np.float32) if t is None else _c(np.broadcast_to(np.asarray(t, np.float32), (R,)),
+                                                            np.float32).copy()
+    arr = (ctypes.POINTER(ctypes.c_float) * 6)(*[_f(a) for a in soa])
+    hits = np.zeros((R, 4), np.float32)
+    sts = np.zeros((P, 3), np.uint32)
+    bad = lib().ror_trace_packets(st, _f(nd), len(nd), _u(idx), _f(tr), arr, _f(tt), P, float(t_min_tri),
+                                  _f(hits), _u(sts), threads)
     return hits, sts, int(bad)
 
 

@@ -909,6 +909,169 @@ void trace_bvh_one(const BvhNode* nodes, size_t ncount, const uint32_t* idx, con
   }
 }
 
+// ---------------------------------------------------------------- packets
+// src/ray.rs:44-61 -- RayPacket4: four rays in SoA form. The inverse
+// directions are 1/d per lane (ray.rs:86-100; rtbvh_ffi/src/lib.rs:673-676).
+struct Packet4 {
+  float ox[4], oy[4], oz[4], dx[4], dy[4], dz[4], ix[4], iy[4], iz[4], t[4];
+};
+
+// src/aabb.rs:217-246 -- Aabb::intersect4: glam Vec4 min/max (SSE rules);
+// Some(per-lane t_min) when any lane has t_max > 0, t_max > t_min and
+// t_min < t.
+inline bool aabb_intersect4(const Aabb& a, const Packet4& p, float tnear[4]) {
+  bool any = false;
+  for (int k = 0; k < 4; ++k) {
+    float t1x = (a.min[0] - p.ox[k]) * p.ix[k], t1y = (a.min[1] - p.oy[k]) * p.iy[k];
+    float t1z = (a.min[2] - p.oz[k]) * p.iz[k];
+    float t2x = (a.max[0] - p.ox[k]) * p.ix[k], t2y = (a.max[1] - p.oy[k]) * p.iy[k];
+    float t2z = (a.max[2] - p.oz[k]) * p.iz[k];
+    float tmin = sse_max(sse_min(t1x, t2x), sse_max(sse_min(t1y, t2y), sse_min(t1z, t2z)));
+    float tmax = sse_min(sse_max(t1x, t2x), sse_min(sse_max(t1y, t2y), sse_max(t1z, t2z)));
+    tnear[k] = tmin;
+    if (tmax > 0.0f && tmax > tmin && tmin < p.t[k]) any = true;
+  }
+  return any;
+}
+
+// src/mbvh_node.rs:242-295 -- MbvhNode::intersect4: slot i is hit when any
+// lane has t_max > t_min and t_min < t. The axes are folded in x, y, z order
+// (t_min = max(max(x, y), z)). ids stay [0, 1, 2, 3].
+inline void mnode_intersect4(const MbvhNode& m, const Packet4& p, bool result[4]) {
+  for (int i = 0; i < 4; ++i) result[i] = false;
+  for (int k = 0; k < 4; ++k) {
+    for (int i = 0; i < 4; ++i) {
+      float x1 = (m.min_x[i] - p.ox[k]) * p.ix[k], x2 = (m.max_x[i] - p.ox[k]) * p.ix[k];
+      float tmin = sse_min(x1, x2), tmax = sse_max(x1, x2);
+      float y1 = (m.min_y[i] - p.oy[k]) * p.iy[k], y2 = (m.max_y[i] - p.oy[k]) * p.iy[k];
+      tmin = sse_max(tmin, sse_min(y1, y2));
+      tmax = sse_min(tmax, sse_max(y1, y2));
+      float z1 = (m.min_z[i] - p.oz[k]) * p.iz[k], z2 = (m.max_z[i] - p.oz[k]) * p.iz[k];
+      tmin = sse_max(tmin, sse_min(z1, z2));
+      tmax = sse_min(tmax, sse_max(z1, z2));
+      if (tmax > tmin && tmin < p.t[k]) result[i] = true;
+    }
+  }
+}
+
+// src/builders/spatial_sah.rs:165-244 -- SpatialTriangle::intersect4, the
+// packet triangle test the reference's packet benchmark calls
+// (examples/benchmark.rs:43-68): |det| >= 1e-6, u and v in [0, 1] with
+// u + v <= 1, t_min <= t < packet t; accepted lanes take the new t.
+inline uint32_t tri_intersect4(const float* tri, Packet4& p, float t_min, float pu[4], float pv[4]) {
+  const float e1x = tri[3] - tri[0], e1y = tri[4] - tri[1], e1z = tri[5] - tri[2];
+  const float e2x = tri[6] - tri[0], e2y = tri[7] - tri[1], e2z = tri[8] - tri[2];
+  uint32_t mask = 0;
+  for (int k = 0; k < 4; ++k) {
+    const float hx = (p.dy[k] * e2z) - (p.dz[k] * e2y);
+    const float hy = (p.dz[k] * e2x) - (p.dx[k] * e2z);
+    const float hz = (p.dx[k] * e2y) - (p.dy[k] * e2x);
+    const float a = ((e1x * hx) + (e1y * hy)) + (e1z * hz);
+    if (!(a <= -1e-6f || a >= 1e-6f)) continue;
+    const float f = 1.0f / a;
+    const float sx = p.ox[k] - tri[0], sy = p.oy[k] - tri[1], sz = p.oz[k] - tri[2];
+    const float u = f * (((sx * hx) + (sy * hy)) + (sz * hz));
+    if (!(u >= 0.0f && u <= 1.0f)) continue;
+    const float qx = sy * e1z - sz * e1y, qy = sz * e1x - sx * e1z, qz = sx * e1y - sy * e1x;
+    const float v = f * (((p.dx[k] * qx) + (p.dy[k] * qy)) + (p.dz[k] * qz));
+    if (!(v >= 0.0f && (u + v) <= 1.0f)) continue;
+    const float t = f * (((e2x * qx) + (e2y * qy)) + (e2z * qz));
+    if (!(t >= t_min && t < p.t[k])) continue;
+    p.t[k] = t;
+    pu[k] = u;
+    pv[k] = v;
+    mask |= 1u << k;
+  }
+  return mask;
+}
+
+struct PacketOut {
+  float u[4], v[4];
+  int32_t prim[4];
+};
+
+inline void packet_test(const float* tris, uint32_t prim, Packet4& p, float t_min, PacketOut& out, Stats& st) {
+  st.tri_tests++;
+  float u[4], v[4];
+  const uint32_t m = tri_intersect4(tris + 9 * (size_t)prim, p, t_min, u, v);
+  for (int k = 0; k < 4; ++k)
+    if ((m >> k) & 1u) { out.u[k] = u[k]; out.v[k] = v[k]; out.prim[k] = (int32_t)prim; }
+}
+
+// src/iter_indices.rs:316-414 (MbvhPacketIndexIterator): slots visited 3..0,
+// a hit leaf's primitives yielded at once, hit interior slots pushed; a popped
+// node's mask is computed with the packet's t at that moment.
+bool trace_mbvh_packet(const MbvhNode* m, size_t mcount, const uint32_t* idx, const float* tris, Packet4& p,
+                       float t_min, PacketOut& out, Stats& st) {
+  if (mcount == 0) return true;
+  int32_t stack[ORACLE_STACK];
+  bool res[4];
+  mnode_intersect4(m[0], p, res);
+  st.node_visits++;
+  int32_t current = 0, sp = -1;
+  for (;;) {
+    const MbvhNode& node = m[current];
+    for (int i = 0; i < 4; ++i) {
+      const int id = 3 - i;
+      if (!res[id]) continue;
+      const int32_t count = node.counts[id], lf = node.children[id];
+      if (count > -1) {
+        for (int32_t j = 0; j < count; ++j) packet_test(tris, idx[lf + j], p, t_min, out, st);
+      } else if (lf > -1) {
+        if (sp + 1 >= ORACLE_STACK) return false;
+        stack[++sp] = lf;
+        if ((uint32_t)(sp + 1) > st.max_stack) st.max_stack = (uint32_t)(sp + 1);
+      }
+    }
+    if (sp < 0) break;
+    current = stack[sp--];
+    mnode_intersect4(m[current], p, res);
+    st.node_visits++;
+  }
+  return true;
+}
+
+// src/iter_indices.rs:110-200 (BvhPacketIndexIterator) with
+// BvhNode::sort_nodes4 (src/bvh_node.rs:180-213): both children hit -> the
+// left one is pushed first (the right one is visited first) when any lane's
+// left t_min is below its right t_min, else the reverse. A packet with a NaN
+// origin or direction component walks nothing.
+bool trace_bvh_packet(const BvhNode* nodes, size_t ncount, const uint32_t* idx, const float* tris, Packet4& p,
+                      float t_min, PacketOut& out, Stats& st) {
+  bool nan = false;
+  for (int k = 0; k < 4; ++k)
+    nan = nan || p.ox[k] != p.ox[k] || p.oy[k] != p.oy[k] || p.oz[k] != p.oz[k] || p.dx[k] != p.dx[k] ||
+          p.dy[k] != p.dy[k] || p.dz[k] != p.dz[k];
+  if (ncount == 0 || nan) return true;
+  int32_t stack[ORACLE_STACK];
+  stack[0] = 0;
+  int32_t sp = 0;
+  while (sp >= 0) {
+    const BvhNode& node = nodes[stack[sp--]];
+    const int32_t count = node.extra1, lf = node.extra2;
+    if (count > -1) {
+      for (int32_t j = 0; j < count; ++j) packet_test(tris, idx[lf + j], p, t_min, out, st);
+    } else if (lf > -1) {
+      st.node_visits++;
+      float lt[4], rt[4];
+      const bool lh = aabb_intersect4(nodes[lf], p, lt), rh = aabb_intersect4(nodes[lf + 1], p, rt);
+      if (sp + 2 >= ORACLE_STACK) return false;
+      if (lh && rh) {
+        bool any_less = false;
+        for (int k = 0; k < 4; ++k) any_less = any_less || (lt[k] < rt[k]);
+        if (any_less) { stack[++sp] = lf; stack[++sp] = lf + 1; }
+        else { stack[++sp] = lf + 1; stack[++sp] = lf; }
+      } else if (lh) {
+        stack[++sp] = lf;
+      } else if (rh) {
+        stack[++sp] = lf + 1;
+      }
+      if ((uint32_t)(sp + 1) > st.max_stack) st.max_stack = (uint32_t)(sp + 1);
+    }
+  }
+  return true;
+}
+
 void load_aabbs(const float* raw, size_t n, std::vector<Aabb>& out) {
   out.resize(n);
   if (n) std::memcpy(out.data(), raw, n * sizeof(Aabb));
@@ -1100,6 +1263,70 @@ int64_t ror_trace(int32_t structure, const float* nodes, size_t node_count, cons
   } else {
     std::vector<std::thread> ts;
     for (uint32_t t = 0; t < threads; ++t) ts.emplace_back(worker);
+    for (auto& th : ts) th.join();
+  }
+  return bad.load();
+}
+
+// Packet traversal of P packets of four rays (closest hit through the
+// packet triangle test). soa = 6 arrays of 4P floats each (origin x, y, z,
+// direction x, y, z; lane k of packet p at 4p + k); t is 4P floats, in/out
+// (the FFI's t). hits_out: 4P x 4 (t, u, v, prim), stats_out: P x 3 (quad /
+// BVH2 node tests, triangle yields, max stack depth). threads > 1 splits the
+// packets into chunks of 1000, as examples/benchmark.rs:43-68. Returns the
+// number of packets whose stack exceeded the oracle's bound.
+int64_t ror_trace_packets(int32_t structure, const float* nodes, size_t node_count, const uint32_t* idx,
+                          const float* tris, const float* const* soa, float* t, size_t npackets, float t_min_tri,
+                          float* hits_out, uint32_t* stats_out, uint32_t threads) {
+  std::atomic<int64_t> bad{0};
+  std::atomic<size_t> next{0};
+  const size_t chunk = 1000;
+  auto worker = [&]() {
+    for (;;) {
+      size_t c0 = next.fetch_add(chunk);
+      if (c0 >= npackets) break;
+      size_t c1 = std::min(npackets, c0 + chunk);
+      for (size_t q = c0; q < c1; ++q) {
+        Packet4 p;
+        PacketOut o;
+        for (int k = 0; k < 4; ++k) {
+          const size_t r = 4 * q + k;
+          p.ox[k] = soa[0][r]; p.oy[k] = soa[1][r]; p.oz[k] = soa[2][r];
+          p.dx[k] = soa[3][r]; p.dy[k] = soa[4][r]; p.dz[k] = soa[5][r];
+          p.ix[k] = 1.0f / p.dx[k]; p.iy[k] = 1.0f / p.dy[k]; p.iz[k] = 1.0f / p.dz[k];
+          p.t[k] = t[r];
+          o.u[k] = o.v[k] = 0.0f;
+          o.prim[k] = -1;
+        }
+        Stats st;
+        const bool ok = structure == 0
+                            ? trace_mbvh_packet(reinterpret_cast<const MbvhNode*>(nodes), node_count, idx, tris, p,
+                                                t_min_tri, o, st)
+                            : trace_bvh_packet(reinterpret_cast<const BvhNode*>(nodes), node_count, idx, tris, p,
+                                               t_min_tri, o, st);
+        if (!ok) bad.fetch_add(1);
+        for (int k = 0; k < 4; ++k) {
+          const size_t r = 4 * q + k;
+          t[r] = p.t[k];
+          if (hits_out) {
+            float* ho = hits_out + 4 * r;
+            ho[0] = p.t[k]; ho[1] = o.u[k]; ho[2] = o.v[k];
+            std::memcpy(ho + 3, &o.prim[k], 4);
+          }
+        }
+        if (stats_out) {
+          stats_out[3 * q + 0] = (uint32_t)st.node_visits;
+          stats_out[3 * q + 1] = (uint32_t)st.tri_tests;
+          stats_out[3 * q + 2] = st.max_stack;
+        }
+      }
+    }
+  };
+  if (threads <= 1) {
+    worker();
+  } else {
+    std::vector<std::thread> ts;
+    for (uint32_t k = 0; k < threads; ++k) ts.emplace_back(worker);
     for (auto& th : ts) th.join();
   }
   return bad.load();

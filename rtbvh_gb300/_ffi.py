@@ -110,6 +110,10 @@ SIGNATURES = {
     "rtbvh_gpu_set_triangles": (_rc, [_u32, ctypes.c_int, _vp, _sz, _vp]),
     "rtbvh_gpu_intersect_mbvh": (_rc, [RTMbvh, _vp, _vp, _sz, _vp, _u32, _vp, _vp]),
     "rtbvh_gpu_intersect_bvh": (_rc, [RTBvh, _vp, _vp, _sz, _vp, _u32, _vp, _vp]),
+    "rtbvh_gpu_intersect_mbvh_packets": (_rc, [RTMbvh, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _u32, _vp,
+                                                _vp]),
+    "rtbvh_gpu_intersect_bvh_packets": (_rc, [RTBvh, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _u32, _vp,
+                                               _vp]),
     "rtbvh_intersect_mbvh_batch": (_rc, [RTMbvh, _vp, _vp, _sz, _vp, _u32]),
     "rtbvh_gpu_status": (_rc, [_u32, ctypes.c_int]),
     "rtbvh_gpu_view": (_rc, [_u32, ctypes.c_int, ctypes.POINTER(RTGpuView)]),

@@ -190,6 +190,15 @@ class Bvh:
         """GPU BvhIndexIterator + triangle test for a batch of rays."""
         return _trace(self._lib.rtbvh_gpu_intersect_bvh, self._h, rays, t_max, any_hit, stats, stream)
 
+    def intersect_packets(self, rays, t=None, stats=False, stream=None):
+        """GPU BvhPacketIndexIterator + packet triangle test; packet p is
+        rays 4p..4p+3. Returns (hits (R,4) CUDA tensor [t, u, v, prim bits],
+        stats (P,3) int32 or None)."""
+        return _trace_packets(self._lib.rtbvh_gpu_intersect_bvh_packets, self._h, rays, t, stats, stream)
+
+    def status(self):
+        return ResultCode(self._lib.rtbvh_gpu_status(self._h.id, 0))
+
     def __del__(self):
         try:
             self._lib.free_bvh(self._h)
@@ -253,6 +262,13 @@ class Mbvh:
         return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream, reorder,
                       exact_nodes)
 
+    def intersect_packets(self, rays, t=None, stats=False, stream=None):
+        """GPU MbvhPacketIndexIterator + packet triangle test (the reference's
+        RayPacket4 path); packet p is rays 4p..4p+3 of the (R, 6) rays, R a
+        multiple of 4. Returns (hits (R,4) CUDA tensor [t, u, v, prim bits],
+        stats (P,3) int32 [node tests, triangle tests, max stack] or None)."""
+        return _trace_packets(self._lib.rtbvh_gpu_intersect_mbvh_packets, self._h, rays, t, stats, stream)
+
     def traversal_tree(self):
         """(exact (count, 32) float32 quad records, compact (count, 16) uint32
         records) of the closest-hit traversal tree, copied to the host."""
@@ -296,6 +312,22 @@ def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False, exact
     flags |= _ffi.TRACE_REORDER if reorder else 0
     flags |= _ffi.TRACE_EXACT_NODES if exact_nodes else 0
     check(fn(handle, _ptr(r), _ptr(tm), n, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect")
+    return hits, st
+
+
+def _trace_packets(fn, handle, rays, t, stats, stream):
+    r = _cuda_f32(rays, 6)
+    n = r.shape[0]
+    if n % 4:
+        raise ValueError("packet traversal needs a multiple of 4 rays")
+    soa = r.t().contiguous()  # (6, R): origin x, y, z, direction x, y, z
+    tt = (torch.full((n,), 1e34, dtype=torch.float32, device=r.device) if t is None
+          else _cuda_f32(t).reshape(-1).expand(n).contiguous().clone())
+    hits = torch.empty((n, 4), dtype=torch.float32, device=r.device)
+    st = torch.empty((n // 4, 3), dtype=torch.int32, device=r.device) if stats else None
+    flags = _ffi.TRACE_STATS if stats else 0
+    ptrs = [ctypes.c_void_p(soa[k].data_ptr()) for k in range(6)]
+    check(fn(handle, *ptrs, _ptr(tt), n // 4, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect_packets")
     return hits, st
 
 

@@ -702,6 +702,56 @@ ResultCode rtbvh_gpu_intersect_bvh(RTBvh bvh, const float* rays, const float* t_
   return trace_common(bvh.id, false, rays, t_max, ray_count, hits, flags, stats, static_cast<cudaStream_t>(stream));
 }
 
+static ResultCode packets_common(uint32_t id, bool mbvh, const float* const origin[3],
+                                 const float* const direction[3], float* t, uintptr_t packet_count, float* hits,
+                                 uint32_t flags, uint32_t* stats, cudaStream_t s) {
+  if (flags & (RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_REORDER)) return InvalidArgument;
+  PacketArgs a;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(id, mbvh);
+    if (!e) return Error;
+    if (!e->d_tris && e->node_count > 0) return InvalidArgument;
+    a.mnodes = e->d_mnodes;
+    a.nodes = e->d_nodes;
+    a.node_count = e->node_count;
+    a.tris = e->d_tris;
+    a.prim_count = e->prim_count;
+    a.status = e->d_status;
+  }
+  if (packet_count == 0) return Ok;
+  for (int k = 0; k < 3; ++k) {
+    if (origin[k] == nullptr || direction[k] == nullptr) return Error;
+    a.origin[k] = origin[k];
+    a.direction[k] = direction[k];
+  }
+  if (t == nullptr) return Error;
+  if ((flags & RTBVH_TRACE_STATS) && stats == nullptr) return Error;
+  a.t = t;
+  a.packet_count = packet_count;
+  a.hits = reinterpret_cast<float4*>(hits);
+  a.stats = (flags & RTBVH_TRACE_STATS) ? stats : nullptr;
+  return cuda_rc(launch_trace_packets(a, mbvh, s));
+}
+
+ResultCode rtbvh_gpu_intersect_mbvh_packets(RTMbvh mbvh, const float* origin_x, const float* origin_y,
+                                            const float* origin_z, const float* direction_x, const float* direction_y,
+                                            const float* direction_z, float* t, uintptr_t packet_count, float* hits,
+                                            uint32_t flags, uint32_t* stats, rtbvh_stream_t stream) {
+  const float* o[3] = {origin_x, origin_y, origin_z};
+  const float* d[3] = {direction_x, direction_y, direction_z};
+  return packets_common(mbvh.id, true, o, d, t, packet_count, hits, flags, stats, static_cast<cudaStream_t>(stream));
+}
+
+ResultCode rtbvh_gpu_intersect_bvh_packets(RTBvh bvh, const float* origin_x, const float* origin_y,
+                                           const float* origin_z, const float* direction_x, const float* direction_y,
+                                           const float* direction_z, float* t, uintptr_t packet_count, float* hits,
+                                           uint32_t flags, uint32_t* stats, rtbvh_stream_t stream) {
+  const float* o[3] = {origin_x, origin_y, origin_z};
+  const float* d[3] = {direction_x, direction_y, direction_z};
+  return packets_common(bvh.id, false, o, d, t, packet_count, hits, flags, stats, static_cast<cudaStream_t>(stream));
+}
+
 ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
                                       float* hits, uint32_t flags) {
   if (ray_count == 0) return Ok;

@@ -143,6 +143,24 @@ struct TraceArgs {
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
 
+// Packets of four rays (see packets.cu). origin/direction: three arrays of
+// 4 * packet_count floats each (lane k of packet p at 4p + k); t: in/out.
+struct PacketArgs {
+  const DMNode* mnodes = nullptr;
+  const DAabb* nodes = nullptr;
+  uint32_t node_count = 0;
+  const float4* tris = nullptr;
+  uint32_t prim_count = 0;
+  const float* origin[3] = {nullptr, nullptr, nullptr};
+  const float* direction[3] = {nullptr, nullptr, nullptr};
+  float* t = nullptr;
+  size_t packet_count = 0;
+  float4* hits = nullptr;     // optional, 4 * packet_count
+  uint32_t* stats = nullptr;  // optional, 3 per packet
+  uint32_t* status = nullptr;
+};
+cudaError_t launch_trace_packets(const PacketArgs& a, bool mbvh, cudaStream_t s);
+
 // ------------------------------------------------------------------ many meshes
 // Per-mesh clustering of a concatenated forest (see locb.cu).
 // Meshes order[0, big_count) (the largest, more than kSegClusterMinPrims

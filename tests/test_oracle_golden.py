@@ -157,3 +157,37 @@ def test_traversal_oracle_matches_brute_force():
     np.testing.assert_array_equal(hits[:, 0], bh[:, 0])
     both = oracle.hit_prims(hits) >= 0
     assert both.sum() > 20
+
+
+@pytest.mark.parametrize("structure,builder", [("mbvh", "locb"), ("bvh", "sah"), ("mbvh", "sah"), ("bvh", "locb")])
+def test_packet_oracle_matches_brute_force(structure, builder):
+    # packets (src/iter_indices.rs:110-414) must find, per lane, the nearest
+    # triangle the packet test (src/builders/spatial_sah.rs:165-244) accepts
+    tris = scenes.incoherent(2000, seed=15)
+    rays, _ = scenes.incoherent_rays(1600, seed=16)
+    a, c = scenes.triangle_aabbs(tris), scenes.triangle_centers(tris)
+    nodes, idx = oracle.build(a, c, builder)
+    st_nodes = oracle.mbvh(nodes) if structure == "mbvh" else nodes
+    hits, st, bad = oracle.trace_packets(structure, st_nodes, idx, tris.reshape(-1, 9), rays)
+    assert bad == 0
+    root = oracle.union_of_list(a).copy()
+    rv = root.view(np.int32)
+    rv[3] = len(tris)
+    rv[7] = 0
+    bh, _, _ = oracle.trace_packets("bvh", root[None, :], np.arange(len(tris), dtype=np.uint32),
+                                    tris.reshape(-1, 9), rays)
+    np.testing.assert_array_equal(hits[:, 0], bh[:, 0])
+    assert (oracle.hit_prims(hits) >= 0).sum() > 20
+    # every packet walks at least the root
+    assert (st[:, 0] >= 1).all() if structure == "mbvh" else True
+
+
+def test_packet_oracle_nan_lane_skips_bvh_packet():
+    # BvhPacketIndexIterator::new (src/iter_indices.rs:122-143): any NaN lane -> no traversal
+    tris = scenes.incoherent(500, seed=17)
+    rays, _ = scenes.incoherent_rays(8, seed=18)
+    rays[1, 4] = np.nan
+    a, c = scenes.triangle_aabbs(tris), scenes.triangle_centers(tris)
+    nodes, idx = oracle.build(a, c, "locb")
+    hits, st, _ = oracle.trace_packets("bvh", nodes, idx, tris.reshape(-1, 9), rays)
+    assert (oracle.hit_prims(hits[:4]) == -1).all() and (st[0] == 0).all()
