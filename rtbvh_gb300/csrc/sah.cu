@@ -104,47 +104,132 @@ struct BinsView {
   __device__ __forceinline__ uint32_t cnt(int a, int i) const { return w[(a * kBins + i) * kBinWords + 6]; }
 };
 
-__device__ __forceinline__ void grow_from_bin(float cmn[3], float cmx[3], const BinsView& B, int a, int i) {
+// One bin (or a union of bins) as floats.
+struct BinVal {
+  float mn[3], mx[3];
+  uint32_t cnt;
+};
+
+__device__ __forceinline__ BinVal load_bin(const BinsView& B, int a, int i) {
+  BinVal v;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    cmn[k] = rs_min(cmn[k], B.mn(a, i, k));
-    cmx[k] = rs_max(cmx[k], B.mx(a, i, k));
+    v.mn[k] = B.mn(a, i, k);
+    v.mx[k] = B.mx(a, i, k);
   }
+  v.cnt = B.cnt(a, i);
+  return v;
+}
+
+// Aabb::grow_bb on bins; Vec3::min/max (rs_min/rs_max) form a commutative,
+// associative operation, and counts are integers, so a union over any
+// grouping of the bins equals the reference's sequential one bit for bit.
+__device__ __forceinline__ void bin_union(BinVal& x, const BinVal& y) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    x.mn[k] = rs_min(x.mn[k], y.mn[k]);
+    x.mx[k] = rs_max(x.mx[k], y.mx[k]);
+  }
+  x.cnt += y.cnt;
+}
+
+__device__ __forceinline__ BinVal shfl_bin(const BinVal& v, int delta, bool up) {
+  BinVal r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.mn[k] = up ? __shfl_up_sync(0xffffffffu, v.mn[k], delta, 16) : __shfl_down_sync(0xffffffffu, v.mn[k], delta, 16);
+    r.mx[k] = up ? __shfl_up_sync(0xffffffffu, v.mx[k], delta, 16) : __shfl_down_sync(0xffffffffu, v.mx[k], delta, 16);
+  }
+  r.cnt = up ? __shfl_up_sync(0xffffffffu, v.cnt, delta, 16) : __shfl_down_sync(0xffffffffu, v.cnt, delta, 16);
+  return r;
+}
+
+// The sweeps of find_split (binned_sah.rs:80-114) for one axis, bin i =
+// lane & 15 of a 16-lane segment: pre = bins [0, i], suf = bins [i, 16).
+struct AxisScan {
+  BinVal pre, suf;
+  float best_cost;
+  uint32_t best_count;
+};
+
+__device__ __forceinline__ AxisScan scan_axis(const BinsView& B, int a, int i) {
+  AxisScan r;
+  const BinVal b = load_bin(B, a, i);
+  r.pre = b;
+  r.suf = b;
+#pragma unroll
+  for (int d = 1; d < kBins; d <<= 1) {
+    const BinVal lo = shfl_bin(r.pre, d, true);
+    const BinVal hi = shfl_bin(r.suf, d, false);
+    if (i >= d) bin_union(r.pre, lo);
+    if (i + d < kBins) bin_union(r.suf, hi);
+  }
+  // both sweeps start from Aabb::empty()
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    r.pre.mn[k] = rs_min(1e34f, r.pre.mn[k]);
+    r.pre.mx[k] = rs_max(-1e34f, r.pre.mx[k]);
+    r.suf.mn[k] = rs_min(1e34f, r.suf.mn[k]);
+    r.suf.mx[k] = rs_max(-1e34f, r.suf.mx[k]);
+  }
+  // right_cost[i] (i >= 1) and the left sweep's cost at i (i <= 14)
+  const float rc = ha6(r.suf.mn, r.suf.mx) * (float)r.suf.cnt;
+  const float rc_next = __shfl_down_sync(0xffffffffu, rc, 1, 16);
+  const float cost = ha6(r.pre.mn, r.pre.mx) * (float)r.pre.cnt + rc_next;
+  // first minimum over i in [0, 15) of the costs below f32::MAX (strict '<'
+  // from f32::MAX in ascending order; NaN costs of empty sides never win)
+  bool valid = i < kBins - 1 && cost < kF32Max;
+  float c = cost;
+  uint32_t idx = valid ? (uint32_t)i : (uint32_t)kBins;
+#pragma unroll
+  for (int d = 8; d > 0; d >>= 1) {
+    const float oc = __shfl_xor_sync(0xffffffffu, c, d, 16);
+    const uint32_t oi = __shfl_xor_sync(0xffffffffu, idx, d, 16);
+    const bool ov = oi < (uint32_t)kBins;
+    if (ov && (!valid || oc < c || (oc == c && oi < idx))) {
+      c = oc;
+      idx = oi;
+      valid = true;
+    }
+  }
+  r.best_cost = valid ? c : kF32Max;
+  r.best_count = valid ? idx + 1u : (uint32_t)kBins;
+  return r;
+}
+
+// Value of field f of the scan of `axis` at bin j, fetched from the lane
+// holding it (A: axes 0 / 1 in lanes 0-15 / 16-31, B: axis 2 in lanes 0-15).
+__device__ __forceinline__ float fetch_f(const AxisScan& A, const AxisScan& Bx, int axis, int j, bool pre, int f) {
+  const BinVal& va = pre ? A.pre : A.suf;
+  const BinVal& vb = pre ? Bx.pre : Bx.suf;
+  const float* fa = f < 3 ? va.mn : va.mx;
+  const float* fb = f < 3 ? vb.mn : vb.mx;
+  const int k = f % 3;
+  const float v = axis == 2 ? fb[k] : fa[k];
+  return __shfl_sync(0xffffffffu, v, axis == 1 ? 16 + j : j);
+}
+__device__ __forceinline__ uint32_t fetch_cnt(const AxisScan& A, const AxisScan& Bx, int axis, int j) {
+  const uint32_t v = axis == 2 ? Bx.pre.cnt : A.pre.cnt;
+  return __shfl_sync(0xffffffffu, v, axis == 1 ? 16 + j : j);
 }
 
 // The split decision of BinnedSahBuildTask::run after binning
-// (binned_sah.rs:174-247, find_split at :80-114). `box` is the node box with
-// its first 1e-4 offset.
-__device__ void sah_decide(const BinsView& B, const float bmn[3], const float bmx[3], uint32_t ws, uint32_t max_leaf,
-                           Decision& d) {
+// (binned_sah.rs:174-247, find_split at :80-114), evaluated by a whole warp
+// (every lane returns the same decision). `box` is the node box with its
+// first 1e-4 offset.
+__device__ void sah_decide_warp(const BinsView& B, const float bmn[3], const float bmx[3], uint32_t ws,
+                                uint32_t max_leaf, Decision& d) {
+  const int lane = threadIdx.x & 31, i = lane & 15;
+  const AxisScan A = scan_axis(B, lane >> 4, i);  // axis 0 (lanes 0-15), axis 1 (lanes 16-31)
+  const AxisScan C = scan_axis(B, 2, i);          // axis 2 (both halves)
   float best_cost[3];
   uint32_t best_count[3];
-  for (int a = 0; a < 3; ++a) {
-    float rc[kBins];
-    float cmn[3] = {1e34f, 1e34f, 1e34f}, cmx[3] = {-1e34f, -1e34f, -1e34f};
-    uint64_t cnt = 0;
-    for (int i = kBins - 1; i > 0; --i) {
-      grow_from_bin(cmn, cmx, B, a, i);
-      cnt += B.cnt(a, i);
-      rc[i] = ha6(cmn, cmx) * (float)cnt;
-    }
-    cmn[0] = cmn[1] = cmn[2] = 1e34f;
-    cmx[0] = cmx[1] = cmx[2] = -1e34f;
-    cnt = 0;
-    float bc = kF32Max;
-    uint32_t bn = kBins;
-    for (int i = 0; i < kBins - 1; ++i) {
-      grow_from_bin(cmn, cmx, B, a, i);
-      cnt += B.cnt(a, i);
-      float cost = ha6(cmn, cmx) * (float)cnt + rc[i + 1];
-      if (cost < bc) {
-        bc = cost;
-        bn = (uint32_t)(i + 1);
-      }
-    }
-    best_cost[a] = bc;
-    best_count[a] = bn;
-  }
+  best_cost[0] = __shfl_sync(0xffffffffu, A.best_cost, 0);
+  best_count[0] = __shfl_sync(0xffffffffu, A.best_count, 0);
+  best_cost[1] = __shfl_sync(0xffffffffu, A.best_cost, 16);
+  best_count[1] = __shfl_sync(0xffffffffu, A.best_count, 16);
+  best_cost[2] = C.best_cost;
+  best_count[2] = C.best_count;
   int axis = 0;
   if (best_cost[0] > best_cost[1]) axis = 1;
   if (best_cost[axis] > best_cost[2]) axis = 2;
@@ -152,43 +237,32 @@ __device__ void sah_decide(const BinsView& B, const float bmn[3], const float bm
   const float max_split_cost = ha6(bmn, bmx) * ((float)ws - kTraversalCost);
   d.split = 0;
   if (best_count[axis] == (uint32_t)kBins || best_cost[axis] >= max_split_cost) {
-    if (ws > max_leaf) {
-      // longest_axis (src/aabb.rs:353-363)
-      int la = 0;
-      if ((bmx[1] - bmn[1]) > (bmx[0] - bmn[0])) la = 1;
-      if ((bmx[2] - bmn[2]) > (bmx[la] - bmn[la])) la = 2;
-      axis = la;
-      uint64_t count = 0;
-      const uint64_t target = (uint64_t)ws * 2 / 5 + 1;
-      for (int i = 0; i < kBins - 1; ++i) {
-        count += B.cnt(axis, i);
-        if (count >= target) {
-          split_index = (uint32_t)(i + 1);
-          break;
-        }
-      }
-    } else {
-      return;  // leaf
-    }
+    if (ws <= max_leaf) return;  // leaf
+    // longest_axis (src/aabb.rs:353-363)
+    int la = 0;
+    if ((bmx[1] - bmn[1]) > (bmx[0] - bmn[0])) la = 1;
+    if ((bmx[2] - bmn[2]) > (bmx[la] - bmn[la])) la = 2;
+    axis = la;
+    // first i < 15 whose cumulative count reaches ws * 2 / 5 + 1
+    const uint64_t target = (uint64_t)ws * 2 / 5 + 1;
+    const uint32_t mine = la == 2 ? C.pre.cnt : A.pre.cnt;
+    const bool in_seg = la == 1 ? lane >= 16 : lane < 16;
+    const uint32_t hit = __ballot_sync(0xffffffffu, in_seg && i < kBins - 1 && (uint64_t)mine >= target);
+    if (hit) split_index = (uint32_t)(__ffs(hit) - 1 - (la == 1 ? 16 : 0)) + 1u;
   }
-  uint32_t n_left = 0;
-  for (uint32_t i = 0; i < split_index && i < (uint32_t)kBins; ++i) n_left += B.cnt(axis, i);
+  const uint32_t n_left = fetch_cnt(A, C, axis, (int)min(split_index, (uint32_t)kBins) - 1);
   if (n_left == 0 || n_left >= ws) return;  // one side empty: leaf
-  float lmn[3] = {1e34f, 1e34f, 1e34f}, lmx[3] = {-1e34f, -1e34f, -1e34f};
-  float rmn[3] = {1e34f, 1e34f, 1e34f}, rmx[3] = {-1e34f, -1e34f, -1e34f};
-  for (uint32_t i = 0; i < best_count[axis]; ++i) grow_from_bin(lmn, lmx, B, axis, (int)i);
-  for (uint32_t i = split_index; i < (uint32_t)kBins; ++i) grow_from_bin(rmn, rmx, B, axis, (int)i);
+  const int lb = (int)best_count[axis] - 1;     // bins [0, best_splits[axis].count)
+  const int rb = (int)min(split_index, (uint32_t)kBins - 1u);  // bins [split_index, 16), split_index <= 15 here
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    d.lbox[f] = fetch_f(A, C, axis, lb, true, f);
+    d.rbox[f] = fetch_f(A, C, axis, rb, false, f);
+  }
   d.split = 1;
   d.axis = (uint32_t)axis;
   d.split_index = split_index;
   d.n_left = n_left;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    d.lbox[k] = lmn[k];
-    d.lbox[3 + k] = lmx[k];
-    d.rbox[k] = rmn[k];
-    d.rbox[3 + k] = rmx[k];
-  }
 }
 
 __device__ __forceinline__ void init_bins(uint32_t* w, int tid, int nthreads) {
@@ -281,7 +355,6 @@ __global__ void __launch_bounds__(1024) k_large_prep(SahParams p) {
       }
       const uint32_t ws = tk.end - tk.begin;
       if (ws > 1 && tk.depth < kMaxDepth) chunks = (ws + kChunk - 1) / kChunk;
-      init_bins(p.bins + (size_t)t * kTaskBinWords, 0, 1);
     }
     uint32_t total;
     uint32_t incl = block_inclusive_scan<1024>(chunks, s_warp, &total);
@@ -293,6 +366,18 @@ __global__ void __launch_bounds__(1024) k_large_prep(SahParams p) {
     p.chunk_base[L] = carry;
     p.cnt->chunks = carry;
     p.cnt->ticket = 0;
+  }
+}
+
+// Empty bins for every large task of the level (one bin per thread).
+__global__ void __launch_bounds__(256) k_bins_init(SahParams p) {
+  const uint32_t L = p.cnt->large;
+  const uint32_t kmin = float_to_ordered(1e34f), kmax = float_to_ordered(-1e34f);
+  const size_t total = (size_t)L * 3 * kBins;
+  for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < total; i += (size_t)gridDim.x * 256) {
+    uint4* b = reinterpret_cast<uint4*>(p.bins + i * kBinWords);
+    b[0] = make_uint4(kmin, kmin, kmin, kmax);
+    b[1] = make_uint4(kmax, kmax, 0u, 0u);
   }
 }
 
@@ -376,8 +461,9 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_bin(SahParams p) {
   }
 }
 
+// One warp per large task.
 __global__ void __launch_bounds__(128) k_large_decide(SahParams p) {
-  const uint32_t t = blockIdx.x * 128 + threadIdx.x;
+  const uint32_t t = (blockIdx.x * 128 + threadIdx.x) >> 5;
   const uint32_t L = p.cnt->large;
   if (t >= L) return;
   const Task tk = p.large[t];
@@ -392,11 +478,13 @@ __global__ void __launch_bounds__(128) k_large_decide(SahParams p) {
   const uint32_t ws = tk.end - tk.begin;
   if (ws > 1 && tk.depth < kMaxDepth) {
     BinsView B{p.bins + (size_t)t * kTaskBinWords};
-    sah_decide(B, mn, mx, ws, p.max_leaf, d);
+    sah_decide_warp(B, mn, mx, ws, p.max_leaf, d);
   }
-  if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
-  else write_leaf(p.nodes, tk, mn, mx);
-  p.dec[t] = d;
+  if ((threadIdx.x & 31) == 0) {
+    if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
+    else write_leaf(p.nodes, tk, mn, mx);
+    p.dec[t] = d;
+  }
 }
 
 // Stable partition of a large task's chunk into idx_b; the number of left
@@ -544,9 +632,11 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(SahParams p) {
       }
     }
     __syncwarp();
-    if (lane == 0) {
+    {
       BinsView B{wb};
-      sah_decide(B, mn, mx, ws, p.max_leaf, d);
+      Decision dl;
+      sah_decide_warp(B, mn, mx, ws, p.max_leaf, dl);
+      if (lane == 0) d = dl;
     }
     __syncwarp();
     if (d.split) {
@@ -817,8 +907,11 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
     return fail(cuda_rc(e));
   for (uint32_t level = 0; level <= kMaxDepth + 1 && (h.large + h.small) > 0; ++level) {
     if (h.large > 0) {
+      const size_t nbins = (size_t)h.large * 3 * kBins;
+      const size_t ib = (nbins + 255) / 256, icap = (size_t)sm_count() * 8;
+      k_bins_init<<<(unsigned)(ib < icap ? ib : icap), 256, 0, s>>>(p);
       k_large_bin<<<h.chunks, kLargeBlock, 0, s>>>(p);
-      k_large_decide<<<(h.large + 127) / 128, 128, 0, s>>>(p);
+      k_large_decide<<<(h.large + 3) / 4, 128, 0, s>>>(p);
       if ((e = cudaMemsetAsync(chunk_status.ptr, 0, (size_t)h.chunks * 4, s))) return fail(cuda_rc(e));
       k_large_partition<<<h.chunks, kLargeBlock, 0, s>>>(p);
       k_large_copyback<<<h.chunks, kLargeBlock, 0, s>>>(p);
