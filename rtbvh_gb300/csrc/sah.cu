@@ -63,7 +63,8 @@ struct Counters {
   uint32_t chunks;      // chunks of the current large list
   uint32_t status;
   uint32_t ticket;      // chunk ticket of the partition kernel
-  uint32_t pad[2];
+  uint32_t mq_count;    // small tasks of more than kThreadMax primitives queued this level
+  uint32_t mq_head;     // next queued task a warp takes
 };
 
 struct BinMap {
@@ -104,37 +105,40 @@ struct BinsView {
   __device__ __forceinline__ uint32_t cnt(int a, int i) const { return w[(a * kBins + i) * kBinWords + 6]; }
 };
 
-// One bin (or a union of bins) as floats.
-struct BinVal {
-  float mn[3], mx[3];
+// One bin (or a union of bins) as ordered keys (float_to_ordered). Bin
+// bounds are never NaN (triangle boxes grow with Vec3::min/max, which ignore
+// NaN, from the empty box), and on non-NaN floats the unsigned min/max of the
+// keys is Vec3::min/max (-0 below +0); it is commutative and associative and
+// counts are integers, so a union over any grouping of the bins equals the
+// reference's sequential Aabb::grow_bb bit for bit.
+struct BinKey {
+  uint32_t mn[3], mx[3];
   uint32_t cnt;
 };
 
-__device__ __forceinline__ BinVal load_bin(const BinsView& B, int a, int i) {
-  BinVal v;
+__device__ __forceinline__ BinKey load_bin(const BinsView& B, int a, int i) {
+  const uint32_t* w = B.w + (a * kBins + i) * kBinWords;
+  BinKey v;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    v.mn[k] = B.mn(a, i, k);
-    v.mx[k] = B.mx(a, i, k);
+    v.mn[k] = w[k];
+    v.mx[k] = w[3 + k];
   }
-  v.cnt = B.cnt(a, i);
+  v.cnt = w[6];
   return v;
 }
 
-// Aabb::grow_bb on bins; Vec3::min/max (rs_min/rs_max) form a commutative,
-// associative operation, and counts are integers, so a union over any
-// grouping of the bins equals the reference's sequential one bit for bit.
-__device__ __forceinline__ void bin_union(BinVal& x, const BinVal& y) {
+__device__ __forceinline__ void bin_union(BinKey& x, const BinKey& y) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    x.mn[k] = rs_min(x.mn[k], y.mn[k]);
-    x.mx[k] = rs_max(x.mx[k], y.mx[k]);
+    x.mn[k] = min(x.mn[k], y.mn[k]);
+    x.mx[k] = max(x.mx[k], y.mx[k]);
   }
   x.cnt += y.cnt;
 }
 
-__device__ __forceinline__ BinVal shfl_bin(const BinVal& v, int delta, bool up) {
-  BinVal r;
+__device__ __forceinline__ BinKey shfl_bin(const BinKey& v, int delta, bool up) {
+  BinKey r;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     r.mn[k] = up ? __shfl_up_sync(0xffffffffu, v.mn[k], delta, 16) : __shfl_down_sync(0xffffffffu, v.mn[k], delta, 16);
@@ -142,6 +146,23 @@ __device__ __forceinline__ BinVal shfl_bin(const BinVal& v, int delta, bool up) 
   }
   r.cnt = up ? __shfl_up_sync(0xffffffffu, v.cnt, delta, 16) : __shfl_down_sync(0xffffffffu, v.cnt, delta, 16);
   return r;
+}
+
+// A union of bins decoded to floats.
+struct BinVal {
+  float mn[3], mx[3];
+  uint32_t cnt;
+};
+
+__device__ __forceinline__ BinVal decode_bin(const BinKey& k) {
+  BinVal v;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    v.mn[q] = ordered_to_float(k.mn[q]);
+    v.mx[q] = ordered_to_float(k.mx[q]);
+  }
+  v.cnt = k.cnt;
+  return v;
 }
 
 // The sweeps of find_split (binned_sah.rs:80-114) for one axis, bin i =
@@ -153,25 +174,27 @@ struct AxisScan {
 };
 
 __device__ __forceinline__ AxisScan scan_axis(const BinsView& B, int a, int i) {
-  AxisScan r;
-  const BinVal b = load_bin(B, a, i);
-  r.pre = b;
-  r.suf = b;
+  const BinKey b = load_bin(B, a, i);
+  BinKey pre = b, suf = b;
 #pragma unroll
   for (int d = 1; d < kBins; d <<= 1) {
-    const BinVal lo = shfl_bin(r.pre, d, true);
-    const BinVal hi = shfl_bin(r.suf, d, false);
-    if (i >= d) bin_union(r.pre, lo);
-    if (i + d < kBins) bin_union(r.suf, hi);
+    const BinKey lo = shfl_bin(pre, d, true);
+    const BinKey hi = shfl_bin(suf, d, false);
+    if (i >= d) bin_union(pre, lo);
+    if (i + d < kBins) bin_union(suf, hi);
   }
   // both sweeps start from Aabb::empty()
+  const uint32_t emn = float_to_ordered(1e34f), emx = float_to_ordered(-1e34f);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    r.pre.mn[k] = rs_min(1e34f, r.pre.mn[k]);
-    r.pre.mx[k] = rs_max(-1e34f, r.pre.mx[k]);
-    r.suf.mn[k] = rs_min(1e34f, r.suf.mn[k]);
-    r.suf.mx[k] = rs_max(-1e34f, r.suf.mx[k]);
+    pre.mn[k] = min(pre.mn[k], emn);
+    pre.mx[k] = max(pre.mx[k], emx);
+    suf.mn[k] = min(suf.mn[k], emn);
+    suf.mx[k] = max(suf.mx[k], emx);
   }
+  AxisScan r;
+  r.pre = decode_bin(pre);
+  r.suf = decode_bin(suf);
   // right_cost[i] (i >= 1) and the left sweep's cost at i (i <= 14)
   const float rc = ha6(r.suf.mn, r.suf.mx) * (float)r.suf.cnt;
   const float rc_next = __shfl_down_sync(0xffffffffu, rc, 1, 16);
@@ -331,6 +354,7 @@ struct SahParams {
   uint32_t* chunk_status;
   uint64_t* scan_vals;  // per task of the level
   uint64_t* scan_sums;
+  uint32_t* mqueue;     // small-task indices for one warp each (small_cap)
   Counters* cnt;
 };
 
@@ -595,23 +619,185 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_copyback(SahParams p) {
 }
 
 // ------------------------------------------------------------------ small tasks
-__global__ void __launch_bounds__(32 * kSmallWarps) k_small(SahParams p) {
-  __shared__ uint32_t s_bins[kSmallWarps][kTaskBinWords];
-  __shared__ uint32_t s_idx[kSmallWarps][kWarpMax];
-  __shared__ Decision s_dec[kSmallWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t S = p.cnt->small, L = p.cnt->large;
-  const uint32_t t = blockIdx.x * kSmallWarps + warp;
-  if (t >= S) return;
+// A task of at most kThreadMax primitives is decided by one thread. Its
+// bins hold at most kThreadMax primitives, and find_split's cost at bin i
+// depends only on which primitives lie left and right of i: it is NaN while
+// a side is empty and constant between two non-empty bins. So the first
+// minimum over i is found by visiting the non-empty bins in ascending order
+// and evaluating the cost at each (the same float expression over the same
+// unions, hence the same bits). Larger small tasks take a warp each.
+constexpr uint32_t kThreadMax = 8;
+
+// Union, from Aabb::empty(), of the primitives in `sel` (keys, decoded).
+__device__ __forceinline__ void union_sel(const uint32_t (&kb)[kThreadMax][6], uint32_t ws, uint32_t sel, float mn[3],
+                                          float mx[3]) {
+  uint32_t umn[3], umx[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    umn[k] = float_to_ordered(1e34f);
+    umx[k] = float_to_ordered(-1e34f);
+  }
+#pragma unroll
+  for (uint32_t j = 0; j < kThreadMax; ++j) {
+    if (j < ws && ((sel >> j) & 1u)) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        umn[k] = min(umn[k], kb[j][k]);
+        umx[k] = max(umx[k], kb[j][3 + k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = ordered_to_float(umn[k]);
+    mx[k] = ordered_to_float(umx[k]);
+  }
+}
+
+__device__ __forceinline__ uint32_t bin_at(uint32_t packed, uint32_t j) { return (packed >> (4 * j)) & 15u; }
+
+// Mask of the primitives whose bin is below `bound`.
+__device__ __forceinline__ uint32_t below(uint32_t packed, uint32_t ws, uint32_t bound) {
+  uint32_t m = 0;
+#pragma unroll
+  for (uint32_t j = 0; j < kThreadMax; ++j)
+    if (j < ws && bin_at(packed, j) < bound) m |= 1u << j;
+  return m;
+}
+
+// Smallest bin above `after` (16: none) -- ascending visit of non-empty bins.
+__device__ __forceinline__ uint32_t next_bin(uint32_t packed, uint32_t ws, int after) {
+  uint32_t nb = (uint32_t)kBins;
+#pragma unroll
+  for (uint32_t j = 0; j < kThreadMax; ++j) {
+    const uint32_t b = bin_at(packed, j);
+    if (j < ws && (int)b > after && b < nb) nb = b;
+  }
+  return nb;
+}
+
+__device__ void small_task_thread(const SahParams& p, uint32_t t, uint32_t L) {
   const Task tk = p.small[t];
   const uint32_t ws = tk.end - tk.begin;
   float mn[3], mx[3];
   task_box(p.nodes, tk.node, mn, mx);
-  Decision& d = s_dec[warp];
+  Decision d;
+  d.split = 0;
+  if (ws > 1 && tk.depth < kMaxDepth) {
+    uint32_t prim[kThreadMax];
+    uint32_t kb[kThreadMax][6];
+    uint32_t packed[3] = {0u, 0u, 0u};
+    const BinMap bm = make_binmap(mn, mx);
+#pragma unroll
+    for (uint32_t j = 0; j < kThreadMax; ++j) {
+      if (j < ws) {
+        prim[j] = __ldg(p.idx_a + tk.begin + j);
+        const float4 c = __ldg(p.centers + prim[j]);
+        const DAabb box = load_aabb(p.aabbs + prim[j]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          kb[j][k] = float_to_ordered(box.min[k]);
+          kb[j][3 + k] = float_to_ordered(box.max[k]);
+        }
+        packed[0] |= bin_of(c.x, bm.c2b[0], bm.off[0]) << (4 * j);
+        packed[1] |= bin_of(c.y, bm.c2b[1], bm.off[1]) << (4 * j);
+        packed[2] |= bin_of(c.z, bm.c2b[2], bm.off[2]) << (4 * j);
+      }
+    }
+    const uint32_t all = (1u << ws) - 1u;
+    float best_cost[3];
+    uint32_t best_count[3];
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+      float bc = kF32Max;
+      uint32_t bn = (uint32_t)kBins;
+      for (int b = -1;;) {
+        b = (int)next_bin(packed[a], ws, b);
+        if (b >= kBins) break;
+        const uint32_t left = below(packed[a], ws, (uint32_t)b + 1u);
+        if (left == all) break;  // right side empty from here on
+        float lmn[3], lmx[3], rmn[3], rmx[3];
+        union_sel(kb, ws, left, lmn, lmx);
+        union_sel(kb, ws, all & ~left, rmn, rmx);
+        const uint32_t nl = (uint32_t)__popc(left);
+        const float cost = ha6(lmn, lmx) * (float)nl + ha6(rmn, rmx) * (float)(ws - nl);
+        if (cost < bc) {
+          bc = cost;
+          bn = (uint32_t)b + 1u;
+        }
+      }
+      best_cost[a] = bc;
+      best_count[a] = bn;
+    }
+    int axis = 0;
+    if (best_cost[0] > best_cost[1]) axis = 1;
+    if (best_cost[axis] > best_cost[2]) axis = 2;
+    uint32_t split_index = best_count[axis];
+    const float max_split_cost = ha6(mn, mx) * ((float)ws - kTraversalCost);
+    bool leaf = false;
+    if (best_count[axis] == (uint32_t)kBins || best_cost[axis] >= max_split_cost) {
+      if (ws <= p.max_leaf) {
+        leaf = true;
+      } else {
+        int la = 0;
+        if ((mx[1] - mn[1]) > (mx[0] - mn[0])) la = 1;
+        if ((mx[2] - mn[2]) > (mx[la] - mn[la])) la = 2;
+        axis = la;
+        const uint32_t target = ws * 2 / 5 + 1;
+        for (int b = -1;;) {
+          b = (int)next_bin(packed[la], ws, b);
+          if (b >= kBins - 1) break;  // the reference's loop stops before bin 15
+          if ((uint32_t)__popc(below(packed[la], ws, (uint32_t)b + 1u)) >= target) {
+            split_index = (uint32_t)b + 1u;
+            break;
+          }
+        }
+      }
+    }
+    if (!leaf) {
+      const uint32_t left = below(packed[axis], ws, split_index);
+      const uint32_t n_left = (uint32_t)__popc(left);
+      if (n_left > 0 && n_left < ws) {
+        d.split = 1;
+        d.axis = (uint32_t)axis;
+        d.split_index = split_index;
+        d.n_left = n_left;
+        float lmn[3], lmx[3], rmn[3], rmx[3];
+        union_sel(kb, ws, below(packed[axis], ws, best_count[axis]), lmn, lmx);
+        union_sel(kb, ws, all & ~left, rmn, rmx);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          d.lbox[k] = lmn[k];
+          d.lbox[3 + k] = lmx[k];
+          d.rbox[k] = rmn[k];
+          d.rbox[3 + k] = rmx[k];
+        }
+        // stable partition (left primitives first, in order)
+        uint32_t tpos = tk.begin, fpos = tk.begin + n_left;
+#pragma unroll
+        for (uint32_t j = 0; j < kThreadMax; ++j) {
+          if (j < ws) p.idx_a[((left >> j) & 1u) ? tpos++ : fpos++] = prim[j];
+        }
+      }
+    }
+  }
+  if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
+  else write_leaf(p.nodes, tk, mn, mx);
+  p.dec[L + t] = d;
+}
+
+// A small task of more than kThreadMax primitives, by one warp: bins in
+// shared memory, the warp-parallel decision, a ballot-based stable partition.
+__device__ void small_task_warp(const SahParams& p, uint32_t t, uint32_t L, uint32_t* wb, uint32_t* sidx,
+                                Decision& d) {
+  const int lane = threadIdx.x & 31;
+  const Task tk = p.small[t];
+  const uint32_t ws = tk.end - tk.begin;
+  float mn[3], mx[3];
+  task_box(p.nodes, tk.node, mn, mx);
   if (lane == 0) d.split = 0;
   __syncwarp();
   if (ws > 1 && tk.depth < kMaxDepth && ws <= kWarpMax) {
-    uint32_t* wb = &s_bins[warp][0];
     init_bins(wb, lane, 32);
     __syncwarp();
     const BinMap bm = make_binmap(mn, mx);
@@ -657,16 +843,16 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(SahParams p) {
         const uint32_t T = __ballot_sync(0xffffffffu, pred);
         const uint32_t V = __ballot_sync(0xffffffffu, valid);
         const uint32_t F = V & ~T;
-        if (pred) s_idx[warp][tb + __popc(T & lt)] = prim;
+        if (pred) sidx[tb + __popc(T & lt)] = prim;
         else if (valid) {
           const uint32_t dst = d.n_left + fb + __popc(F & lt);
-          if (dst < kWarpMax) s_idx[warp][dst] = prim;
+          if (dst < kWarpMax) sidx[dst] = prim;
         }
         tb += __popc(T);
         fb += __popc(F);
       }
       __syncwarp();
-      for (uint32_t i = lane; i < ws; i += 32) p.idx_a[tk.begin + i] = s_idx[warp][i];
+      for (uint32_t i = lane; i < ws; i += 32) p.idx_a[tk.begin + i] = sidx[i];
     }
   }
   __syncwarp();
@@ -674,6 +860,47 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(SahParams p) {
     if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
     else write_leaf(p.nodes, tk, mn, mx);
     p.dec[L + t] = d;
+  }
+  __syncwarp();
+}
+
+// Each thread takes one small task: tasks of at most kThreadMax primitives
+// (and leaves) are done at once; the others are queued for one warp each
+// (k_small_warps). The order in which queued tasks run does not matter: each
+// writes only its own node, index range and decision slot.
+__global__ void __launch_bounds__(128) k_small(SahParams p) {
+  const uint32_t S = p.cnt->small, L = p.cnt->large;
+  const uint32_t t = blockIdx.x * 128 + threadIdx.x;
+  bool big = false;
+  if (t < S) {
+    const Task tk = p.small[t];
+    const uint32_t ws = tk.end - tk.begin;
+    big = ws > kThreadMax && tk.depth < kMaxDepth;
+    if (!big) small_task_thread(p, t, L);
+  }
+  const uint32_t m = __ballot_sync(0xffffffffu, big);
+  if (m) {
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == __ffs(m) - 1) base = atomicAdd(&p.cnt->mq_count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+    if (big) p.mqueue[base + __popc(m & ((1u << lane) - 1u))] = t;
+  }
+}
+
+// Persistent: every warp takes queued small tasks until the queue is empty.
+__global__ void __launch_bounds__(32 * kSmallWarps) k_small_warps(SahParams p) {
+  __shared__ uint32_t s_bins[kSmallWarps][kTaskBinWords];
+  __shared__ uint32_t s_idx[kSmallWarps][kWarpMax];
+  __shared__ Decision s_dec[kSmallWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t Q = p.cnt->mq_count, L = p.cnt->large;
+  for (;;) {
+    uint32_t q = 0;
+    if (lane == 0) q = atomicAdd(&p.cnt->mq_head, 1u);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= Q) break;
+    small_task_warp(p, __ldg(p.mqueue + q), L, &s_bins[warp][0], &s_idx[warp][0], s_dec[warp]);
   }
 }
 
@@ -812,6 +1039,8 @@ __global__ void k_advance(SahParams p, uint32_t nb) {
     p.cnt->node_count += nl + ns;
     p.cnt->large = nl;
     p.cnt->small = ns;
+    p.cnt->mq_count = 0;
+    p.cnt->mq_head = 0;
   }
 }
 
@@ -834,6 +1063,8 @@ __global__ void k_sah_init(SahParams p, const DAabb* world) {
     p.cnt->status = 0;
     p.cnt->chunks = 0;
     p.cnt->ticket = 0;
+    p.cnt->mq_count = 0;
+    p.cnt->mq_head = 0;
   }
 }
 
@@ -869,13 +1100,14 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   Scratch<float> tbox;
   Scratch<uint64_t> scan_vals, scan_sums;
   Scratch<Counters> cnt;
+  Scratch<uint32_t> mqueue;
   const uint32_t scan_blocks_cap = (task_cap + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems) + 1;
   if ((e = world.alloc(1, s)) || (e = acc.alloc(8, s)) || (e = idx_b.alloc(n, s)) ||
       (e = bins.alloc((size_t)large_cap * kTaskBinWords, s)) || (e = chunk_base.alloc(large_cap + 1, s)) ||
       (e = chunk_status.alloc(chunk_cap, s)) || (e = large0.alloc(large_cap, s)) || (e = large1.alloc(large_cap, s)) ||
       (e = small0.alloc(small_cap, s)) || (e = small1.alloc(small_cap, s)) || (e = dec.alloc(task_cap, s)) ||
       (e = tbox.alloc((size_t)large_cap * 6, s)) || (e = scan_vals.alloc(task_cap, s)) ||
-      (e = scan_sums.alloc(scan_blocks_cap + 1, s)) || (e = cnt.alloc(1, s)))
+      (e = scan_sums.alloc(scan_blocks_cap + 1, s)) || (e = cnt.alloc(1, s)) || (e = mqueue.alloc(small_cap, s)))
     return fail(cuda_rc(e));
   if ((e = launch_world_bounds(aabbs, n, world.ptr, acc.ptr, s))) return fail(cuda_rc(e));
 
@@ -898,7 +1130,11 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   p.chunk_status = chunk_status.ptr;
   p.scan_vals = scan_vals.ptr;
   p.scan_sums = scan_sums.ptr;
+  p.mqueue = mqueue.ptr;
   p.cnt = cnt.ptr;
+  int small_warp_blocks = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&small_warp_blocks, k_small_warps, 32 * kSmallWarps, 0);
+  if (small_warp_blocks < 1) small_warp_blocks = 1;
   k_sah_init<<<(n + 255) / 256, 256, 0, s>>>(p, world.ptr);
   k_large_prep<<<1, 1024, 0, s>>>(p);
   Counters h{};
@@ -916,7 +1152,12 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
       k_large_partition<<<h.chunks, kLargeBlock, 0, s>>>(p);
       k_large_copyback<<<h.chunks, kLargeBlock, 0, s>>>(p);
     }
-    if (h.small > 0) k_small<<<(h.small + kSmallWarps - 1) / kSmallWarps, 32 * kSmallWarps, 0, s>>>(p);
+    if (h.small > 0) {
+      k_small<<<(h.small + 127) / 128, 128, 0, s>>>(p);
+      // at most one queued task per 9 primitives of the level's small tasks
+      const size_t wcap = (size_t)sm_count() * small_warp_blocks, wneed = (h.small + kSmallWarps - 1) / kSmallWarps;
+      k_small_warps<<<(unsigned)(wneed < wcap ? wneed : wcap), 32 * kSmallWarps, 0, s>>>(p);
+    }
     const uint32_t N = h.large + h.small;
     const uint32_t nb = (N + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
     k_scan_local<<<nb, kScanBlock, 0, s>>>(p);
