@@ -1,6 +1,9 @@
 // Primitive preparation for the builds: boxes and centres of triangles or
 // points, the world box, 30-bit Morton codes and the leaf-ordered triangle
 // layout used by the traversal kernels.
+#include <mutex>
+#include <vector>
+
 #include "lib_internal.h"
 
 namespace rtbvh {
@@ -213,6 +216,64 @@ cudaError_t launch_gather_triangles(const float* vertices, const uint32_t* indic
   if (n == 0) return cudaSuccess;
   k_gather_triangles<<<grid_for(n, kPrepBlock), kPrepBlock, 0, s>>>(vertices, indices, n, out);
   return cudaGetLastError();
+}
+
+namespace {
+std::mutex g_pool_mu;
+std::vector<cudaMemPool_t> g_pools;
+}  // namespace
+
+// Per-device pool; up to an eighth of the device memory (at most 8 GiB) of
+// freed allocations stays reserved between calls.
+static cudaError_t library_pool(cudaMemPool_t* out) {
+  int dev = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev))) return e;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if ((int)g_pools.size() <= dev) g_pools.resize(dev + 1, nullptr);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    if ((e = cudaMemPoolCreate(&pool, &props))) return e;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    uint64_t keep = (uint64_t)total_b / 8;
+    if (keep > (8ull << 30)) keep = 8ull << 30;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pools[dev] = pool;
+  }
+  *out = g_pools[dev];
+  return cudaSuccess;
+}
+
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s) {
+  *p = nullptr;
+  if (bytes == 0) return cudaSuccess;
+  // under stream capture the allocation becomes a graph memory node of the
+  // default pool
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e;
+  if ((e = cudaStreamIsCapturing(s, &cap))) return e;
+  if (cap != cudaStreamCaptureStatusNone) return cudaMallocAsync(p, bytes, s);
+  cudaMemPool_t pool;
+  if ((e = library_pool(&pool))) return e;
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+void pool_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+void pool_free_now(void* const* ptrs, int count) {
+  bool any = false;
+  for (int i = 0; i < count; ++i) any = any || ptrs[i] != nullptr;
+  if (!any) return;
+  cudaDeviceSynchronize();
+  for (int i = 0; i < count; ++i)
+    if (ptrs[i]) cudaFreeAsync(ptrs[i], 0);
 }
 
 int sm_count() {

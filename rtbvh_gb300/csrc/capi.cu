@@ -41,14 +41,8 @@ struct Entry {
   std::vector<uint32_t> h_indices;
 
   void release() {
-    cudaFree(d_nodes);
-    cudaFree(d_mnodes);
-    cudaFree(d_qnodes);
-    cudaFree(d_wnodes);
-    cudaFree(d_indices);
-    cudaFree(d_tris);
-    cudaFree(d_vertices);
-    cudaFree(d_status);
+    void* const arrays[] = {d_nodes, d_mnodes, d_qnodes, d_wnodes, d_indices, d_tris, d_vertices, d_status};
+    pool_free_now(arrays, 8);
     d_nodes = nullptr;
     d_mnodes = nullptr;
     d_qnodes = nullptr;
@@ -88,13 +82,6 @@ cudaStream_t legacy_stream() {
   static std::once_flag once;
   std::call_once(once, []() { cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking); });
   return s;
-}
-
-template <class T>
-cudaError_t dmalloc(T** p, size_t count) {
-  *p = nullptr;
-  if (count == 0) return cudaSuccess;
-  return cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
 }
 
 RTBvh bvh_handle(uint32_t id, const Entry& e) {
@@ -163,14 +150,14 @@ ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t
   e->d_nodes = out.nodes;
   e->d_indices = out.indices;
   cudaError_t err;
-  if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
+  if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
     e->release();
     return cuda_rc(err);
   }
   if (d_vertices) {
-    if ((err = dmalloc(&e->d_vertices, 9 * n)) ||
+    if ((err = device_alloc(&e->d_vertices, 9 * n, s)) ||
         (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
-        (err = dmalloc(&e->d_tris, (size_t)kTriFloat4 * n)) ||
+        (err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * n, s)) ||
         (err = launch_gather_triangles(e->d_vertices, e->d_indices, n, e->d_tris, s))) {
       e->release();
       return cuda_rc(err);
@@ -611,17 +598,17 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     return rc;
   }
 
-  if ((err = dmalloc(&e->d_status, 4)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
-      (err = dmalloc(&e->d_indices, prim_count)) ||
+  if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
+      (err = device_alloc(&e->d_indices, prim_count, s)) ||
       (err = cudaMemcpyAsync(e->d_indices, d_indices, (size_t)prim_count * 4, cudaMemcpyDeviceToDevice, s))) {
     e->release();
     return cuda_rc(err);
   }
   if (d_tris) {
-    if ((err = dmalloc(&e->d_tris, (size_t)kTriFloat4 * prim_count)) ||
+    if ((err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * prim_count, s)) ||
         (err = cudaMemcpyAsync(e->d_tris, d_tris, 16 * (size_t)kTriFloat4 * prim_count, cudaMemcpyDeviceToDevice,
                                s)) ||
-        (err = dmalloc(&e->d_vertices, 9 * (size_t)prim_count)) ||
+        (err = device_alloc(&e->d_vertices, 9 * (size_t)prim_count, s)) ||
         (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s))) {
       e->release();
       return cuda_rc(err);
@@ -651,8 +638,8 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
   if (!e || vertices == nullptr) return Error;
   if (prim_count != e->prim_count) return InequalAabbsAndPrimitives;
   cudaError_t err;
-  if (!e->d_vertices && (err = dmalloc(&e->d_vertices, 9 * (size_t)prim_count))) return cuda_rc(err);
-  if (!e->d_tris && (err = dmalloc(&e->d_tris, (size_t)kTriFloat4 * prim_count))) return cuda_rc(err);
+  if (!e->d_vertices && (err = device_alloc(&e->d_vertices, 9 * (size_t)prim_count, s))) return cuda_rc(err);
+  if (!e->d_tris && (err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * prim_count, s))) return cuda_rc(err);
   if ((err = cudaMemcpyAsync(e->d_vertices, vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
       (err = launch_gather_triangles(e->d_vertices, e->d_indices, prim_count, e->d_tris, s)))
     return cuda_rc(err);
@@ -864,20 +851,22 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     uint32_t count = 0;
     if ((rc = build_mbvh(b->d_nodes, b->node_count, s, &fresh, &count)) != Ok) return rc;
     if (count != m->node_count) {
-      cudaFree(fresh);
+      pool_free(fresh, s);
       return Error;
     }
-    cudaFree(m->d_mnodes);
+    {
+      // the old arrays may still be read by traversals on other streams
+      void* const old_arrays[] = {m->d_mnodes, m->d_qnodes, m->d_wnodes};
+      pool_free_now(old_arrays, 3);
+    }
     m->d_mnodes = fresh;
-    cudaFree(m->d_qnodes);
-    cudaFree(m->d_wnodes);
     m->d_qnodes = nullptr;
     m->d_wnodes = nullptr;
     m->wcount = 0;
     if ((rc = build_wide(b->d_nodes, b->node_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok) return rc;
     if (vertices) {
-      if (!m->d_vertices && (err = dmalloc(&m->d_vertices, 9 * n))) return cuda_rc(err);
-      if (!m->d_tris && (err = dmalloc(&m->d_tris, (size_t)kTriFloat4 * n))) return cuda_rc(err);
+      if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
+      if (!m->d_tris && (err = device_alloc(&m->d_tris, (size_t)kTriFloat4 * n, s))) return cuda_rc(err);
       if ((err = cudaMemcpyAsync(m->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
           (err = launch_gather_triangles(m->d_vertices, m->d_indices, n, m->d_tris, s)))
         return cuda_rc(err);

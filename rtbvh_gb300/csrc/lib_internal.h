@@ -10,7 +10,24 @@
 
 namespace rtbvh {
 
-// Stream-ordered scratch buffer (cudaMallocAsync / cudaFreeAsync).
+// Device memory of the library comes from one stream-ordered pool per device
+// that keeps freed memory reserved (up to a cap) for the next call, so
+// repeated builds neither map fresh memory nor synchronise in cudaFree.
+cudaError_t pool_alloc(void** p, size_t bytes, cudaStream_t s);
+// Stream-ordered free of a pool allocation.
+void pool_free(void* p, cudaStream_t s);
+// Frees long-lived pool allocations whose last use may be on any stream:
+// waits for the device once, then frees them (NULL entries are skipped).
+void pool_free_now(void* const* ptrs, int count);
+
+template <class T>
+cudaError_t device_alloc(T** p, size_t count, cudaStream_t s) {
+  *p = nullptr;
+  if (count == 0) return cudaSuccess;
+  return pool_alloc(reinterpret_cast<void**>(p), count * sizeof(T), s);
+}
+
+// Stream-ordered scratch buffer from the library pool.
 template <class T>
 struct Scratch {
   T* ptr = nullptr;
@@ -20,10 +37,10 @@ struct Scratch {
     stream = s;
     count = n;
     if (n == 0) return cudaSuccess;
-    return cudaMallocAsync(reinterpret_cast<void**>(&ptr), n * sizeof(T), s);
+    return pool_alloc(reinterpret_cast<void**>(&ptr), n * sizeof(T), s);
   }
   ~Scratch() {
-    if (ptr) cudaFreeAsync(ptr, stream);
+    if (ptr) pool_free(ptr, stream);
   }
   Scratch() = default;
   Scratch(const Scratch&) = delete;
@@ -63,7 +80,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, size_t n, int bits,
 
 // ------------------------------------------------------------------ builds
 struct BuildOutput {
-  DAabb* nodes = nullptr;        // device, node_count entries (cudaMalloc'd, owned by caller)
+  DAabb* nodes = nullptr;        // device, node_count entries (library pool, owned by caller)
   uint32_t* indices = nullptr;   // device, prim_count entries
   uint32_t node_count = 0;
 };

@@ -428,14 +428,14 @@ ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n_, cuda
   cudaError_t e;
   DAabb* nodes = nullptr;
   uint32_t* indices = nullptr;
-  if ((e = cudaMalloc(&nodes, (size_t)node_count * sizeof(DAabb))) != cudaSuccess) return cuda_rc(e);
-  if ((e = cudaMalloc(&indices, (size_t)n * 4)) != cudaSuccess) {
-    cudaFree(nodes);
+  if ((e = device_alloc(&nodes, node_count, s)) != cudaSuccess) return cuda_rc(e);
+  if ((e = device_alloc(&indices, n, s)) != cudaSuccess) {
+    pool_free(nodes, s);
     return cuda_rc(e);
   }
   auto fail = [&](ResultCode rc) {
-    cudaFree(nodes);
-    cudaFree(indices);
+    pool_free(nodes, s);
+    pool_free(indices, s);
     return rc;
   };
   Scratch<DAabb> world;

@@ -375,9 +375,9 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   const uint32_t m_total = h[0];
   if (m_total == 0 || m_total > node_count) return Error;
   DMNode* mnodes = nullptr;
-  if ((e = cudaMalloc(&mnodes, (size_t)m_total * sizeof(DMNode)))) return cuda_rc(e);
+  if ((e = device_alloc(&mnodes, m_total, s))) return cuda_rc(e);
   if ((e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s))) {
-    cudaFree(mnodes);
+    pool_free(mnodes, s);
     return cuda_rc(e);
   }
   int per_sm = 0;
@@ -400,16 +400,16 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   p.status = status.ptr;
   void* args[] = {&p};
   if ((e = cudaLaunchCooperativeKernel((void*)k_collapse, dim3(grid), dim3(kBlock), args, 0, s))) {
-    cudaFree(mnodes);
+    pool_free(mnodes, s);
     return cuda_rc(e);
   }
   uint32_t st = 0;
   if ((e = cudaMemcpyAsync(&st, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
-    cudaFree(mnodes);
+    pool_free(mnodes, s);
     return cuda_rc(e);
   }
   if (st != 0) {
-    cudaFree(mnodes);
+    pool_free(mnodes, s);
     return (st & kStatusTimeout) ? Timeout : Error;
   }
   *mnodes_out = mnodes;
@@ -932,11 +932,11 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   DMNode* wn = nullptr;
   DQNode* wq = nullptr;
   auto fail = [&](ResultCode rc) {
-    cudaFree(wn);
-    cudaFree(wq);
+    pool_free(wn, s);
+    pool_free(wq, s);
     return rc;
   };
-  if ((e = cudaMalloc(&wn, (size_t)capacity * sizeof(DMNode)))) return fail(cuda_rc(e));
+  if ((e = device_alloc(&wn, capacity, s))) return fail(cuda_rc(e));
   if ((e = cudaMemsetAsync(status.ptr, 0, 16, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
     return fail(cuda_rc(e));
   // status[1]: not nested -> no traversal tree (closest hit uses the exact nodes)
@@ -975,7 +975,7 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
     return fail(cuda_rc(e));
   if (h[1] != 0) return fail((h[1] & kStatusTimeout) ? Timeout : Error);
   if (h[0] == 0 || h[0] > capacity) return fail(Error);
-  if ((e = cudaMalloc(&wq, (size_t)h[0] * sizeof(DQNode)))) return fail(cuda_rc(e));
+  if ((e = device_alloc(&wq, h[0], s))) return fail(cuda_rc(e));
   if ((e = launch_quantize_mbvh(wn, h[0], wq, s))) return fail(cuda_rc(e));
   *wnodes_out = wn;
   *wq_out = wq;

@@ -1,16 +1,20 @@
 // Binned SAH build (src/builders/binned_sah.rs) on the GPU, breadth first.
 //
 // The reference runs one task per node (BinnedSahBuildTask::run,
-// binned_sah.rs:132-282) from a depth-first work stack. Here every level of
-// the tree is one round of kernels over all of that level's tasks:
+// binned_sah.rs:132-282) from a depth-first work stack. Here the whole build
+// is one cooperative launch (k_sah_build) that walks the tree level by
+// level; the phases of a level are separated by grid barriers (bounded
+// waits), so no host round trip or relaunch happens between levels:
 //
-//   large tasks (more than kWarpMax primitives): a grid of 2048-primitive
-//     chunks bins into per-task global bins (exact min/max via ordered-int
-//     atomics, counts via atomicAdd), one thread per task decides the split,
-//     and a chunked stable partition (decoupled look-back over the chunks of
-//     a task, bounded waits) scatters the primitive indices;
-//   small tasks: one warp per task bins in shared memory, decides and
-//     partitions in place;
+//   large tasks (more than kWarpMax primitives): the grid bins 2048-primitive
+//     chunks into per-task global bins (runs of primitives in one bin merged
+//     in registers, then ordered-int atomics), one warp per task decides the
+//     split, and a chunked stable partition (decoupled look-back over the
+//     chunks of a task, bounded waits) scatters the primitive indices;
+//   small tasks of at most kThreadMax primitives: one thread each decides
+//     and partitions (exact sweep over the non-empty bins);
+//   other small tasks: one warp each from a queue (bins in shared memory,
+//     the warp-parallel decision, ballot partition);
 //   then a scan over the level's tasks numbers the children (breadth-first,
 //     deterministic) and builds the next level's task lists.
 //
@@ -36,7 +40,8 @@ constexpr float kTraversalCost = 1.0f;
 constexpr int kChunk = 2048;
 constexpr int kLargeBlock = 256;
 constexpr uint32_t kWarpMax = 1024;
-constexpr int kSmallWarps = 4;
+constexpr uint32_t kCoopMaxPrims = 1u << 20;      // larger builds launch the phases separately
+constexpr uint32_t kCoopPrimsPerBlock = 2048;     // cooperative grid: one block per this many primitives
 constexpr int kBinWords = 8;  // ordered min xyz, ordered max xyz, count, pad
 constexpr int kTaskBinWords = 3 * kBins * kBinWords;
 constexpr uint32_t kFlagAgg = 1u << 30;
@@ -95,14 +100,9 @@ __device__ __forceinline__ float ha6(const float mn[3], const float mx[3]) {
   return half_area(mn[0], mn[1], mn[2], mx[0], mx[1], mx[2]);
 }
 
-// Bins stored as ordered keys (global or shared memory).
+// A task's bins as ordered keys (kTaskBinWords words in shared memory).
 struct BinsView {
-  const uint32_t* w;  // kTaskBinWords words
-  __device__ __forceinline__ float mn(int a, int i, int k) const { return ordered_to_float(w[(a * kBins + i) * kBinWords + k]); }
-  __device__ __forceinline__ float mx(int a, int i, int k) const {
-    return ordered_to_float(w[(a * kBins + i) * kBinWords + 3 + k]);
-  }
-  __device__ __forceinline__ uint32_t cnt(int a, int i) const { return w[(a * kBins + i) * kBinWords + 6]; }
+  const uint32_t* w;
 };
 
 // One bin (or a union of bins) as ordered keys (float_to_ordered). Bin
@@ -343,32 +343,82 @@ struct SahParams {
   uint32_t* idx_b;  // partition scratch
   uint32_t n;
   uint32_t max_leaf;
-  Task* large;
-  Task* small;
-  Task* large_next;
-  Task* small_next;
-  Decision* dec;        // [large tasks | small tasks]
+  Task* large[2];       // task lists of even / odd levels
+  Task* small[2];
+  Decision* dec;        // [large tasks | small tasks] of the level
   float* tbox;          // 6 floats per large task (box with first offset)
   uint32_t* bins;       // kTaskBinWords per large task
   uint32_t* chunk_base; // large + 1
   uint32_t* chunk_status;
   uint64_t* scan_vals;  // per task of the level
-  uint64_t* scan_sums;
-  uint32_t* mqueue;     // small-task indices for one warp each (small_cap)
+  uint64_t* scan_sums;  // one per block
+  uint32_t* mqueue;     // small tasks queued for one warp each
   Counters* cnt;
+  GridBarrier* bar;
+};
+
+// The level being built, as every block read it after the level's first
+// barrier.
+struct Level {
+  const Task* large;
+  const Task* small;
+  Task* large_next;
+  Task* small_next;
+  uint32_t L, S, node_base;
+};
+
+// Reads of data written earlier in the same launch (by any block) go to L2:
+// the L1 is not coherent between SMs.
+__device__ __forceinline__ Task ld_task(const Task* t) {
+  const uint4 v = __ldcg(reinterpret_cast<const uint4*>(t));
+  return Task{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ Decision ld_dec(const Decision* d) {
+  Decision r;
+  const uint4* q = reinterpret_cast<const uint4*>(d);
+  uint4* o = reinterpret_cast<uint4*>(&r);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) o[k] = __ldcg(q + k);
+  return r;
+}
+__device__ __forceinline__ void ld_tbox(const float* tb, float mn[3], float mx[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = __ldcg(tb + a);
+    mx[a] = __ldcg(tb + 3 + a);
+  }
+}
+
+__device__ __forceinline__ uint32_t find_task(const uint32_t* chunk_base, uint32_t L, uint32_t chunk) {
+  uint32_t lo = 0, hi = L;  // last t with chunk_base[t] <= chunk
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldcg(chunk_base + mid) <= chunk) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Shared memory of one block, reused by the phases of a level.
+struct alignas(16) SahShared {
+  uint32_t bins[kLargeBlock / 32][kTaskBinWords];  // per-warp bins
+  uint32_t idx[kLargeBlock / 32][kWarpMax];        // per-warp partition buffer
+  Decision dec[kLargeBlock / 32];
+  uint64_t scan[kLargeBlock / 32];
+  uint32_t warp[32];
+  uint32_t chunk, fail, prefix, pad;
 };
 
 // ------------------------------------------------------------------ large tasks
-// Per level, before binning: task boxes, zeroed bins, chunk offsets.
-__global__ void __launch_bounds__(1024) k_large_prep(SahParams p) {
-  __shared__ uint32_t s_warp[32];
-  const uint32_t L = p.cnt->large;
+// Block 0: task boxes (with the first 1e-4 offset) and chunk offsets of the
+// level's large tasks.
+__device__ void large_prep(const SahParams& p, const Level& lv, SahShared& sh) {
   uint32_t carry = 0;
-  for (uint32_t base = 0; base < L || base == 0; base += 1024) {
+  for (uint32_t base = 0; base < lv.L; base += kLargeBlock) {
     const uint32_t t = base + threadIdx.x;
     uint32_t chunks = 0;
-    if (t < L) {
-      const Task tk = p.large[t];
+    if (t < lv.L) {
+      const Task tk = ld_task(lv.large + t);
       float mn[3], mx[3];
       task_box(p.nodes, tk.node, mn, mx);
       float* tb = p.tbox + 6 * (size_t)t;
@@ -381,64 +431,69 @@ __global__ void __launch_bounds__(1024) k_large_prep(SahParams p) {
       if (ws > 1 && tk.depth < kMaxDepth) chunks = (ws + kChunk - 1) / kChunk;
     }
     uint32_t total;
-    uint32_t incl = block_inclusive_scan<1024>(chunks, s_warp, &total);
-    if (t < L) p.chunk_base[t] = carry + incl - chunks;
+    const uint32_t incl = block_inclusive_scan<kLargeBlock>(chunks, sh.warp, &total);
+    if (t < lv.L) p.chunk_base[t] = carry + incl - chunks;
     carry += total;
-    if (base + 1024 >= L) break;
   }
   if (threadIdx.x == 0) {
-    p.chunk_base[L] = carry;
+    p.chunk_base[lv.L] = carry;
     p.cnt->chunks = carry;
     p.cnt->ticket = 0;
   }
 }
 
-// Empty bins for every large task of the level (one bin per thread).
-__global__ void __launch_bounds__(256) k_bins_init(SahParams p) {
-  const uint32_t L = p.cnt->large;
+// Empty bins for every large task (one bin per thread of the grid).
+__device__ void large_bins_init(const SahParams& p, const Level& lv) {
   const uint32_t kmin = float_to_ordered(1e34f), kmax = float_to_ordered(-1e34f);
-  const size_t total = (size_t)L * 3 * kBins;
-  for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < total; i += (size_t)gridDim.x * 256) {
+  const size_t total = (size_t)lv.L * 3 * kBins;
+  for (size_t i = (size_t)blockIdx.x * kLargeBlock + threadIdx.x; i < total; i += (size_t)gridDim.x * kLargeBlock) {
     uint4* b = reinterpret_cast<uint4*>(p.bins + i * kBinWords);
     b[0] = make_uint4(kmin, kmin, kmin, kmax);
     b[1] = make_uint4(kmax, kmax, 0u, 0u);
   }
 }
 
-__device__ __forceinline__ uint32_t find_task(const uint32_t* chunk_base, uint32_t L, uint32_t chunk) {
-  uint32_t lo = 0, hi = L;  // last t with chunk_base[t] <= chunk
-  while (hi - lo > 1) {
-    uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(chunk_base + mid) <= chunk) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-__global__ void __launch_bounds__(kLargeBlock) k_large_bin(SahParams p) {
-  constexpr int NW = kLargeBlock / 32;
-  __shared__ uint32_t s_bins[NW][kTaskBinWords];
+// Bins one 2048-primitive chunk of a large task into the task's global bins.
+__device__ void large_bin_chunk(const SahParams& p, const Level& lv, uint32_t chunk, SahShared& sh) {
   const int warp = threadIdx.x >> 5;
-  const uint32_t L = p.cnt->large;
-  const uint32_t chunk = blockIdx.x;
-  const uint32_t t = find_task(p.chunk_base, L, chunk);
-  const Task tk = p.large[t];
-  const uint32_t k = chunk - p.chunk_base[t];
+  const uint32_t t = find_task(p.chunk_base, lv.L, chunk);
+  const Task tk = ld_task(lv.large + t);
+  const uint32_t k = chunk - __ldcg(p.chunk_base + t);
   const uint32_t c0 = tk.begin + k * kChunk;
   const uint32_t c1 = min(c0 + kChunk, tk.end);
-  init_bins(&s_bins[warp][0], threadIdx.x & 31, 32);
+  init_bins(&sh.bins[warp][0], threadIdx.x & 31, 32);
   __syncthreads();
   float mn[3], mx[3];
-  const float* tb = p.tbox + 6 * (size_t)t;
+  ld_tbox(p.tbox + 6 * (size_t)t, mn, mx);
+  const BinMap bm = make_binmap(mn, mx);
+  uint32_t* wb = &sh.bins[warp][0];
+  // Each thread bins kChunk / kLargeBlock consecutive primitives. Neighbours
+  // in the index array are usually neighbours in space and share bins, so a
+  // run of primitives in one bin is merged in registers and written to the
+  // warp's shared bins once (atomics only when an axis changes bin).
+  constexpr int PER = kChunk / kLargeBlock;
+  uint32_t rbin[3], rmn[3][3], rmx[3][3], rcnt[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    mn[a] = tb[a];
-    mx[a] = tb[3 + a];
+    rbin[a] = 0xffffffffu;
+    rcnt[a] = 0;
   }
-  const BinMap bm = make_binmap(mn, mx);
-  uint32_t* wb = &s_bins[warp][0];
-  for (uint32_t i = c0 + threadIdx.x; i < c1; i += kLargeBlock) {
-    const uint32_t prim = __ldg(p.idx_a + i);
+  auto flush = [&](int a) {
+    if (rcnt[a] == 0) return;
+    uint32_t* b = wb + (a * kBins + rbin[a]) * kBinWords;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      atomicMin(b + q, rmn[a][q]);
+      atomicMax(b + 3 + q, rmx[a][q]);
+    }
+    atomicAdd(b + 6, rcnt[a]);
+  };
+  const uint32_t s0 = c0 + threadIdx.x * PER;
+#pragma unroll 1
+  for (int j = 0; j < PER; ++j) {
+    const uint32_t i = s0 + j;
+    if (i >= c1) break;
+    const uint32_t prim = __ldcg(p.idx_a + i);
     const float4 c = __ldg(p.centers + prim);
     const DAabb box = load_aabb(p.aabbs + prim);
     const float cc[3] = {c.x, c.y, c.z};
@@ -450,22 +505,34 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_bin(SahParams p) {
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      uint32_t* b = wb + (a * kBins + bin_of(cc[a], bm.c2b[a], bm.off[a])) * kBinWords;
+      const uint32_t bin = bin_of(cc[a], bm.c2b[a], bm.off[a]);
+      if (bin != rbin[a]) {
+        flush(a);
+        rbin[a] = bin;
+        rcnt[a] = 0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          rmn[a][q] = kmn[q];
+          rmx[a][q] = kmx[q];
+        }
+      }
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
-        atomicMin(b + q, kmn[q]);
-        atomicMax(b + 3 + q, kmx[q]);
+        rmn[a][q] = min(rmn[a][q], kmn[q]);
+        rmx[a][q] = max(rmx[a][q], kmx[q]);
       }
-      atomicAdd(b + 6, 1u);
+      ++rcnt[a];
     }
   }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) flush(a);
   __syncthreads();
   uint32_t* gb = p.bins + (size_t)t * kTaskBinWords;
   for (int i = threadIdx.x; i < 3 * kBins; i += kLargeBlock) {
     uint32_t cnt = 0;
     uint32_t vmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, vmx[3] = {0u, 0u, 0u};
-    for (int w = 0; w < NW; ++w) {
-      const uint32_t* b = &s_bins[w][i * kBinWords];
+    for (int w = 0; w < kLargeBlock / 32; ++w) {
+      const uint32_t* b = &sh.bins[w][i * kBinWords];
       cnt += b[6];
 #pragma unroll
       for (int q = 0; q < 3; ++q) {
@@ -483,28 +550,28 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_bin(SahParams p) {
       atomicAdd(g + 6, cnt);
     }
   }
+  __syncthreads();  // the shared bins are reused by the block's next chunk
 }
 
-// One warp per large task.
-__global__ void __launch_bounds__(128) k_large_decide(SahParams p) {
-  const uint32_t t = (blockIdx.x * 128 + threadIdx.x) >> 5;
-  const uint32_t L = p.cnt->large;
-  if (t >= L) return;
-  const Task tk = p.large[t];
+// Split decision of large task t by one warp (its global bins are copied to
+// the warp's shared bins first).
+__device__ void large_decide(const SahParams& p, const Level& lv, uint32_t t, SahShared& sh) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const Task tk = ld_task(lv.large + t);
   float mn[3], mx[3];
-  const float* tb = p.tbox + 6 * (size_t)t;
-  for (int a = 0; a < 3; ++a) {
-    mn[a] = tb[a];
-    mx[a] = tb[3 + a];
-  }
+  ld_tbox(p.tbox + 6 * (size_t)t, mn, mx);
   Decision d;
   d.split = 0;
   const uint32_t ws = tk.end - tk.begin;
   if (ws > 1 && tk.depth < kMaxDepth) {
-    BinsView B{p.bins + (size_t)t * kTaskBinWords};
-    sah_decide_warp(B, mn, mx, ws, p.max_leaf, d);
+    uint32_t* wb = &sh.bins[warp][0];
+    const uint32_t* gb = p.bins + (size_t)t * kTaskBinWords;
+    for (int i = lane; i < kTaskBinWords; i += 32) wb[i] = __ldcg(gb + i);
+    __syncwarp();
+    sah_decide_warp(BinsView{wb}, mn, mx, ws, p.max_leaf, d);
+    __syncwarp();
   }
-  if ((threadIdx.x & 31) == 0) {
+  if (lane == 0) {
     if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
     else write_leaf(p.nodes, tk, mn, mx);
     p.dec[t] = d;
@@ -512,34 +579,22 @@ __global__ void __launch_bounds__(128) k_large_decide(SahParams p) {
 }
 
 // Stable partition of a large task's chunk into idx_b; the number of left
-// primitives in the task's earlier chunks comes from a decoupled look-back.
-__global__ void __launch_bounds__(kLargeBlock) k_large_partition(SahParams p) {
-  __shared__ uint32_t s_chunk, s_fail, s_prefix;
-  __shared__ uint32_t s_warp[kLargeBlock / 32];
-  const uint32_t L = p.cnt->large;
-  if (threadIdx.x == 0) {
-    s_chunk = atomicAdd(&p.cnt->ticket, 1u);
-    s_fail = 0;
-  }
-  __syncthreads();
-  const uint32_t chunk = s_chunk;
-  const uint32_t t = find_task(p.chunk_base, L, chunk);
-  const Decision d = p.dec[t];
+// primitives in the task's earlier chunks comes from a decoupled look-back
+// (chunks are taken in ticket order, so every chunk waited on is held by a
+// running block).
+__device__ void large_partition_chunk(const SahParams& p, const Level& lv, uint32_t chunk, SahShared& sh) {
+  const uint32_t t = find_task(p.chunk_base, lv.L, chunk);
+  const Decision d = ld_dec(p.dec + t);
   if (!d.split) return;  // no chunk of this task waits on another
-  const Task tk = p.large[t];
-  const uint32_t first_chunk = p.chunk_base[t];
+  const Task tk = ld_task(lv.large + t);
+  const uint32_t first_chunk = __ldcg(p.chunk_base + t);
   const uint32_t k = chunk - first_chunk;
   const uint32_t c0 = tk.begin + k * kChunk;
   const uint32_t c1 = min(c0 + kChunk, tk.end);
   float mn[3], mx[3];
-  const float* tb = p.tbox + 6 * (size_t)t;
-  for (int a = 0; a < 3; ++a) {
-    mn[a] = tb[a];
-    mx[a] = tb[3 + a];
-  }
+  ld_tbox(p.tbox + 6 * (size_t)t, mn, mx);
   const BinMap bm = make_binmap(mn, mx);
   const int ax = (int)d.axis;
-  // each thread owns kChunk / kLargeBlock consecutive primitives
   constexpr int PER = kChunk / kLargeBlock;
   uint32_t prim[PER];
   uint32_t flags = 0, mine = 0;
@@ -549,7 +604,7 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_partition(SahParams p) {
     const uint32_t i = s + j;
     prim[j] = 0;
     if (i < c1) {
-      prim[j] = __ldg(p.idx_a + i);
+      prim[j] = __ldcg(p.idx_a + i);
       const float4 c = __ldg(p.centers + prim[j]);
       const float cc = ax == 0 ? c.x : (ax == 1 ? c.y : c.z);
       if (bin_of(cc, bm.c2b[ax], bm.off[ax]) < d.split_index) {
@@ -559,11 +614,12 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_partition(SahParams p) {
     }
   }
   uint32_t chunk_true;
-  const uint32_t incl = block_inclusive_scan<kLargeBlock>(mine, s_warp, &chunk_true);
+  const uint32_t incl = block_inclusive_scan<kLargeBlock>(mine, sh.warp, &chunk_true);
   const uint32_t before_me = incl - mine;
   volatile uint32_t* st = p.chunk_status;
   if (threadIdx.x == 0) {
     uint32_t excl = 0;
+    sh.fail = 0;
     if (k == 0) {
       st[chunk] = kFlagInc | chunk_true;
     } else {
@@ -576,7 +632,7 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_partition(SahParams p) {
         if (f == 0u) {
           if (++spins > kSpinLimit) {
             atomicOr(&p.cnt->status, kStatusTimeout);
-            s_fail = 1;
+            sh.fail = 1;
             break;
           }
           __nanosleep(64);
@@ -588,11 +644,13 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_partition(SahParams p) {
       }
       st[chunk] = kFlagInc | (excl + chunk_true);
     }
-    s_prefix = excl;
+    sh.prefix = excl;
   }
   __syncthreads();
-  if (s_fail) return;
-  const uint32_t true_before = s_prefix + before_me;
+  const bool fail = sh.fail != 0;
+  const uint32_t true_before = sh.prefix + before_me;
+  __syncthreads();  // sh.prefix / sh.fail are rewritten by the block's next chunk
+  if (fail) return;
   uint32_t tpos = tk.begin + true_before;
   uint32_t fpos = tk.begin + d.n_left + ((s - tk.begin) - true_before);
 #pragma unroll
@@ -606,16 +664,14 @@ __global__ void __launch_bounds__(kLargeBlock) k_large_partition(SahParams p) {
   }
 }
 
-__global__ void __launch_bounds__(kLargeBlock) k_large_copyback(SahParams p) {
-  const uint32_t L = p.cnt->large;
-  const uint32_t chunk = blockIdx.x;
-  const uint32_t t = find_task(p.chunk_base, L, chunk);
-  if (!p.dec[t].split) return;
-  const Task tk = p.large[t];
-  const uint32_t k = chunk - p.chunk_base[t];
+__device__ void large_copyback_chunk(const SahParams& p, const Level& lv, uint32_t chunk) {
+  const uint32_t t = find_task(p.chunk_base, lv.L, chunk);
+  if (!__ldcg(&p.dec[t].split)) return;
+  const Task tk = ld_task(lv.large + t);
+  const uint32_t k = chunk - __ldcg(p.chunk_base + t);
   const uint32_t c0 = tk.begin + k * kChunk;
   const uint32_t c1 = min(c0 + kChunk, tk.end);
-  for (uint32_t i = c0 + threadIdx.x; i < c1; i += kLargeBlock) p.idx_a[i] = p.idx_b[i];
+  for (uint32_t i = c0 + threadIdx.x; i < c1; i += kLargeBlock) p.idx_a[i] = __ldcg(p.idx_b + i);
 }
 
 // ------------------------------------------------------------------ small tasks
@@ -676,8 +732,7 @@ __device__ __forceinline__ uint32_t next_bin(uint32_t packed, uint32_t ws, int a
   return nb;
 }
 
-__device__ void small_task_thread(const SahParams& p, uint32_t t, uint32_t L) {
-  const Task tk = p.small[t];
+__device__ void small_task_thread(const SahParams& p, const Task& tk, uint32_t slot) {
   const uint32_t ws = tk.end - tk.begin;
   float mn[3], mx[3];
   task_box(p.nodes, tk.node, mn, mx);
@@ -691,7 +746,7 @@ __device__ void small_task_thread(const SahParams& p, uint32_t t, uint32_t L) {
 #pragma unroll
     for (uint32_t j = 0; j < kThreadMax; ++j) {
       if (j < ws) {
-        prim[j] = __ldg(p.idx_a + tk.begin + j);
+        prim[j] = __ldcg(p.idx_a + tk.begin + j);
         const float4 c = __ldg(p.centers + prim[j]);
         const DAabb box = load_aabb(p.aabbs + prim[j]);
 #pragma unroll
@@ -783,15 +838,14 @@ __device__ void small_task_thread(const SahParams& p, uint32_t t, uint32_t L) {
   }
   if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
   else write_leaf(p.nodes, tk, mn, mx);
-  p.dec[L + t] = d;
+  p.dec[slot] = d;
 }
 
 // A small task of more than kThreadMax primitives, by one warp: bins in
 // shared memory, the warp-parallel decision, a ballot-based stable partition.
-__device__ void small_task_warp(const SahParams& p, uint32_t t, uint32_t L, uint32_t* wb, uint32_t* sidx,
+__device__ void small_task_warp(const SahParams& p, const Task& tk, uint32_t slot, uint32_t* wb, uint32_t* sidx,
                                 Decision& d) {
   const int lane = threadIdx.x & 31;
-  const Task tk = p.small[t];
   const uint32_t ws = tk.end - tk.begin;
   float mn[3], mx[3];
   task_box(p.nodes, tk.node, mn, mx);
@@ -799,10 +853,12 @@ __device__ void small_task_warp(const SahParams& p, uint32_t t, uint32_t L, uint
   __syncwarp();
   if (ws > 1 && tk.depth < kMaxDepth && ws <= kWarpMax) {
     init_bins(wb, lane, 32);
+    // stage the task's indices (independent loads, all in flight at once)
+    for (uint32_t i = lane; i < ws; i += 32) sidx[i] = __ldcg(p.idx_a + tk.begin + i);
     __syncwarp();
     const BinMap bm = make_binmap(mn, mx);
     for (uint32_t i = lane; i < ws; i += 32) {
-      const uint32_t prim = __ldg(p.idx_a + tk.begin + i);
+      const uint32_t prim = sidx[i];
       const float4 c = __ldg(p.centers + prim);
       const DAabb box = load_aabb(p.aabbs + prim);
       const float cc[3] = {c.x, c.y, c.z};
@@ -819,15 +875,15 @@ __device__ void small_task_warp(const SahParams& p, uint32_t t, uint32_t L, uint
     }
     __syncwarp();
     {
-      BinsView B{wb};
       Decision dl;
-      sah_decide_warp(B, mn, mx, ws, p.max_leaf, dl);
+      sah_decide_warp(BinsView{wb}, mn, mx, ws, p.max_leaf, dl);
       if (lane == 0) d = dl;
     }
     __syncwarp();
     if (d.split) {
       const int ax = (int)d.axis;
       const uint32_t lt = (1u << lane) - 1u;
+      const uint32_t split_index = d.split_index, n_left = d.n_left;
       uint32_t tb = 0, fb = 0;
       for (uint32_t c0 = 0; c0 < ws; c0 += 32) {
         const uint32_t i = c0 + lane;
@@ -835,73 +891,32 @@ __device__ void small_task_warp(const SahParams& p, uint32_t t, uint32_t L, uint
         uint32_t prim = 0;
         bool pred = false;
         if (valid) {
-          prim = p.idx_a[tk.begin + i];
+          prim = sidx[i];
           const float4 c = __ldg(p.centers + prim);
           const float cc = ax == 0 ? c.x : (ax == 1 ? c.y : c.z);
-          pred = bin_of(cc, bm.c2b[ax], bm.off[ax]) < d.split_index;
+          pred = bin_of(cc, bm.c2b[ax], bm.off[ax]) < split_index;
         }
         const uint32_t T = __ballot_sync(0xffffffffu, pred);
         const uint32_t V = __ballot_sync(0xffffffffu, valid);
         const uint32_t F = V & ~T;
-        if (pred) sidx[tb + __popc(T & lt)] = prim;
+        // written straight to the task's range: the staged copy is the source
+        if (pred) p.idx_a[tk.begin + tb + __popc(T & lt)] = prim;
         else if (valid) {
-          const uint32_t dst = d.n_left + fb + __popc(F & lt);
-          if (dst < kWarpMax) sidx[dst] = prim;
+          const uint32_t dst = n_left + fb + __popc(F & lt);
+          if (dst < ws) p.idx_a[tk.begin + dst] = prim;
         }
         tb += __popc(T);
         fb += __popc(F);
       }
-      __syncwarp();
-      for (uint32_t i = lane; i < ws; i += 32) p.idx_a[tk.begin + i] = sidx[i];
     }
   }
   __syncwarp();
   if (lane == 0) {
     if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
     else write_leaf(p.nodes, tk, mn, mx);
-    p.dec[L + t] = d;
+    p.dec[slot] = d;
   }
   __syncwarp();
-}
-
-// Each thread takes one small task: tasks of at most kThreadMax primitives
-// (and leaves) are done at once; the others are queued for one warp each
-// (k_small_warps). The order in which queued tasks run does not matter: each
-// writes only its own node, index range and decision slot.
-__global__ void __launch_bounds__(128) k_small(SahParams p) {
-  const uint32_t S = p.cnt->small, L = p.cnt->large;
-  const uint32_t t = blockIdx.x * 128 + threadIdx.x;
-  bool big = false;
-  if (t < S) {
-    const Task tk = p.small[t];
-    const uint32_t ws = tk.end - tk.begin;
-    big = ws > kThreadMax && tk.depth < kMaxDepth;
-    if (!big) small_task_thread(p, t, L);
-  }
-  const uint32_t m = __ballot_sync(0xffffffffu, big);
-  if (m) {
-    const int lane = threadIdx.x & 31;
-    uint32_t base = 0;
-    if (lane == __ffs(m) - 1) base = atomicAdd(&p.cnt->mq_count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
-    if (big) p.mqueue[base + __popc(m & ((1u << lane) - 1u))] = t;
-  }
-}
-
-// Persistent: every warp takes queued small tasks until the queue is empty.
-__global__ void __launch_bounds__(32 * kSmallWarps) k_small_warps(SahParams p) {
-  __shared__ uint32_t s_bins[kSmallWarps][kTaskBinWords];
-  __shared__ uint32_t s_idx[kSmallWarps][kWarpMax];
-  __shared__ Decision s_dec[kSmallWarps];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t Q = p.cnt->mq_count, L = p.cnt->large;
-  for (;;) {
-    uint32_t q = 0;
-    if (lane == 0) q = atomicAdd(&p.cnt->mq_head, 1u);
-    q = __shfl_sync(0xffffffffu, q, 0);
-    if (q >= Q) break;
-    small_task_warp(p, __ldg(p.mqueue + q), L, &s_bins[warp][0], &s_idx[warp][0], s_dec[warp]);
-  }
 }
 
 // ------------------------------------------------------------------ level scan + emit
@@ -913,17 +928,14 @@ __device__ __forceinline__ uint64_t children_value(const Decision& d, const Task
   return (large << 32) | (uint64_t)(2u - (uint32_t)large);
 }
 
-__device__ __forceinline__ Task level_task(const SahParams& p, uint32_t t, uint32_t L) {
-  return t < L ? p.large[t] : p.small[t - L];
+__device__ __forceinline__ Task level_task(const Level& lv, uint32_t t) {
+  return t < lv.L ? ld_task(lv.large + t) : ld_task(lv.small + (t - lv.L));
 }
-
-constexpr int kScanBlock = 256;
-constexpr int kScanItems = 4;
 
 template <class T>
 __device__ __forceinline__ T block_scan_incl(T v, T* s_warp, T* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NW = kScanBlock / 32;
+  constexpr int NW = kLargeBlock / 32;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     T n = __shfl_up_sync(0xffffffffu, v, o);
@@ -948,95 +960,249 @@ __device__ __forceinline__ T block_scan_incl(T v, T* s_warp, T* total) {
   return v + prefix;
 }
 
-// Stage 1: values and per-block exclusive scans.
-__global__ void __launch_bounds__(kScanBlock) k_scan_local(SahParams p) {
-  __shared__ uint64_t s_warp[kScanBlock / 32];
-  const uint32_t L = p.cnt->large, N = L + p.cnt->small;
-  const uint32_t base = blockIdx.x * kScanBlock * kScanItems + threadIdx.x * kScanItems;
-  uint64_t v[kScanItems], sum = 0;
-#pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    const uint32_t t = base + j;
-    v[j] = 0;
-    if (t < N) v[j] = children_value(p.dec[t], level_task(p, t, L));
-    sum += v[j];
-  }
-  uint64_t total;
-  uint64_t incl = block_scan_incl<uint64_t>(sum, s_warp, &total);
-  uint64_t run = incl - sum;
-#pragma unroll
-  for (int j = 0; j < kScanItems; ++j) {
-    const uint32_t t = base + j;
-    if (t < N) p.scan_vals[t] = run;
-    run += v[j];
-  }
-  if (threadIdx.x == 0) p.scan_sums[blockIdx.x] = total;
+// Block b's contiguous segment of the level's tasks.
+__device__ __forceinline__ void segment(uint32_t N, uint32_t& lo, uint32_t& hi) {
+  const uint32_t seg = (N + gridDim.x - 1) / gridDim.x;
+  lo = min(N, blockIdx.x * seg);
+  hi = min(N, lo + seg);
 }
 
-// Stage 2: one block scans the block sums (exclusive, total at [nb]).
-__global__ void __launch_bounds__(kScanBlock) k_scan_sums(SahParams p, uint32_t nb) {
-  __shared__ uint64_t s_warp[kScanBlock / 32];
+// Children values of the segment: exclusive scan within the segment
+// (scan_vals) and the segment total (scan_sums[block]).
+__device__ void scan_segment(const SahParams& p, const Level& lv, SahShared& sh) {
+  uint32_t lo, hi;
+  segment(lv.L + lv.S, lo, hi);
   uint64_t carry = 0;
-  for (uint32_t base = 0; base < nb; base += kScanBlock) {
-    const uint32_t i = base + threadIdx.x;
-    uint64_t v = i < nb ? p.scan_sums[i] : 0;
+  for (uint32_t base = lo; base < hi; base += kLargeBlock) {
+    const uint32_t t = base + threadIdx.x;
+    uint64_t v = 0;
+    if (t < hi) v = children_value(ld_dec(p.dec + t), level_task(lv, t));
     uint64_t total;
-    uint64_t incl = block_scan_incl<uint64_t>(v, s_warp, &total);
-    if (i < nb) p.scan_sums[i] = carry + incl - v;
+    const uint64_t incl = block_scan_incl<uint64_t>(v, sh.scan, &total);
+    if (t < hi) p.scan_vals[t] = carry + incl - v;
     carry += total;
   }
-  if (threadIdx.x == 0) p.scan_sums[nb] = carry;
+  if (threadIdx.x == 0) p.scan_sums[blockIdx.x] = carry;
 }
 
-// Stage 3: node numbering and the next level's task lists.
-__global__ void __launch_bounds__(kScanBlock) k_emit(SahParams p, uint32_t nb) {
-  const uint32_t L = p.cnt->large, N = L + p.cnt->small;
-  const uint32_t t = blockIdx.x * kScanBlock + threadIdx.x;
-  const uint64_t total = p.scan_sums[nb];
-  const uint32_t node_base = p.cnt->node_count;
-  if (t < N) {
-    const Decision d = p.dec[t];
-    if (d.split) {
-      const Task tk = level_task(p, t, L);
-      const uint64_t ex = p.scan_vals[t] + p.scan_sums[t / (kScanBlock * kScanItems)];
-      uint32_t li = (uint32_t)(ex >> 32), si = (uint32_t)(ex & 0xffffffffu);
-      const uint32_t child = node_base + li + si;
-      DAabb nd = load_aabb_cg(p.nodes + tk.node);
-      nd.left_first = (int32_t)child;
-      nd.count = -1;
-      store_aabb(p.nodes + tk.node, nd);
-      DAabb lb, rb;
+// Node numbering (breadth first) and the next level's task lists.
+__device__ void emit_segment(const SahParams& p, const Level& lv, SahShared& sh, bool advance) {
+  // prefix of the block totals before this block, and the level total
+  uint64_t before = 0, all = 0;
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += kLargeBlock) {
+    const uint64_t v = __ldcg(p.scan_sums + b);
+    all += v;
+    if (b < blockIdx.x) before += v;
+  }
+  uint64_t t0, t1;
+  block_scan_incl<uint64_t>(before, sh.scan, &t0);
+  block_scan_incl<uint64_t>(all, sh.scan, &t1);
+  before = t0;
+  all = t1;
+  uint32_t lo, hi;
+  segment(lv.L + lv.S, lo, hi);
+  for (uint32_t t = lo + threadIdx.x; t < hi; t += kLargeBlock) {
+    const Decision d = ld_dec(p.dec + t);
+    if (!d.split) continue;
+    const Task tk = level_task(lv, t);
+    const uint64_t ex = __ldcg(p.scan_vals + t) + before;
+    uint32_t li = (uint32_t)(ex >> 32), si = (uint32_t)(ex & 0xffffffffu);
+    const uint32_t child = lv.node_base + li + si;
+    DAabb nd = load_aabb_cg(p.nodes + tk.node);
+    nd.left_first = (int32_t)child;
+    nd.count = -1;
+    store_aabb(p.nodes + tk.node, nd);
+    DAabb lb, rb;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        lb.min[k] = d.lbox[k];
-        lb.max[k] = d.lbox[3 + k];
-        rb.min[k] = d.rbox[k];
-        rb.max[k] = d.rbox[3 + k];
-      }
-      lb.count = rb.count = 0;
-      lb.left_first = rb.left_first = 0;
-      store_aabb(p.nodes + child, lb);
-      store_aabb(p.nodes + child + 1, rb);
-      const Task lt{child, tk.begin, tk.begin + d.n_left, tk.depth + 1};
-      const Task rt{child + 1, tk.begin + d.n_left, tk.end, tk.depth + 1};
-      if (lt.end - lt.begin > kWarpMax) p.large_next[li++] = lt;
-      else p.small_next[si++] = lt;
-      if (rt.end - rt.begin > kWarpMax) p.large_next[li++] = rt;
-      else p.small_next[si++] = rt;
+    for (int k = 0; k < 3; ++k) {
+      lb.min[k] = d.lbox[k];
+      lb.max[k] = d.lbox[3 + k];
+      rb.min[k] = d.rbox[k];
+      rb.max[k] = d.rbox[3 + k];
+    }
+    lb.count = rb.count = 0;
+    lb.left_first = rb.left_first = 0;
+    store_aabb(p.nodes + child, lb);
+    store_aabb(p.nodes + child + 1, rb);
+    const Task lt{child, tk.begin, tk.begin + d.n_left, tk.depth + 1};
+    const Task rt{child + 1, tk.begin + d.n_left, tk.end, tk.depth + 1};
+    if (lt.end - lt.begin > kWarpMax) lv.large_next[li++] = lt;
+    else lv.small_next[si++] = lt;
+    if (rt.end - rt.begin > kWarpMax) lv.large_next[li++] = rt;
+    else lv.small_next[si++] = rt;
+  }
+  if (advance && blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t nl = (uint32_t)(all >> 32), ns = (uint32_t)(all & 0xffffffffu);
+    p.cnt->node_count = lv.node_base + nl + ns;
+    p.cnt->large = nl;
+    p.cnt->small = ns;
+    p.cnt->mq_count = 0;
+    p.cnt->mq_head = 0;
+  }
+}
+
+// Small tasks of the level: up to kThreadMax primitives by one thread each,
+// the rest queued for small_warp_phase. The order in which queued tasks run
+// does not matter: each writes only its own node, index range and decision.
+__device__ void small_thread_phase(const SahParams& p, const Level& lv) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t base = blockIdx.x * kLargeBlock; base < lv.S; base += gridDim.x * kLargeBlock) {
+    const uint32_t t = base + threadIdx.x;
+    bool big = false;
+    if (t < lv.S) {
+      const Task tk = ld_task(lv.small + t);
+      big = (tk.end - tk.begin) > kThreadMax && tk.depth < kMaxDepth;
+      if (!big) small_task_thread(p, tk, lv.L + t);
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, big);
+    if (m) {
+      uint32_t qb = 0;
+      if (lane == __ffs(m) - 1) qb = atomicAdd(&p.cnt->mq_count, (uint32_t)__popc(m));
+      qb = __shfl_sync(0xffffffffu, qb, __ffs(m) - 1);
+      if (big) p.mqueue[qb + __popc(m & ((1u << lane) - 1u))] = t;
     }
   }
-  if (t == 0) {
-    // every block reads cnt before thread 0 of block 0 could change it: the
-    // counters are advanced by k_advance after this kernel.
-    (void)total;
+}
+
+// Every warp takes queued small tasks until the queue is empty.
+__device__ void small_warp_phase(const SahParams& p, const Level& lv, SahShared& sh) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t Q = __ldcg(&p.cnt->mq_count);
+  for (;;) {
+    uint32_t q = 0;
+    if (lane == 0) q = atomicAdd(&p.cnt->mq_head, 1u);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= Q) break;
+    const uint32_t t = __ldcg(p.mqueue + q);
+    small_task_warp(p, ld_task(lv.small + t), lv.L + t, &sh.bins[warp][0], &sh.idx[warp][0], sh.dec[warp]);
   }
 }
 
-__global__ void k_advance(SahParams p, uint32_t nb) {
+// Blocks take partition chunks in ticket order until all are done.
+__device__ void large_partition_phase(const SahParams& p, const Level& lv, uint32_t chunks, SahShared& sh) {
+  for (;;) {
+    if (threadIdx.x == 0) sh.chunk = atomicAdd(&p.cnt->ticket, 1u);
+    __syncthreads();
+    const uint32_t c = sh.chunk;
+    __syncthreads();
+    if (c >= chunks) break;
+    large_partition_chunk(p, lv, c, sh);
+  }
+}
+
+__device__ __forceinline__ Level read_level(const SahParams& p, uint32_t level) {
+  Level lv;
+  lv.L = __ldcg(&p.cnt->large);
+  lv.S = __ldcg(&p.cnt->small);
+  lv.node_base = __ldcg(&p.cnt->node_count);
+  lv.large = p.large[level & 1];
+  lv.small = p.small[level & 1];
+  lv.large_next = p.large[(level + 1) & 1];
+  lv.small_next = p.small[(level + 1) & 1];
+  return lv;
+}
+
+// The whole build: one cooperative launch, the levels of the tree one after
+// another, phases separated by grid barriers. Level l reads task lists
+// large[l & 1] / small[l & 1] and writes the other pair.
+__global__ void __launch_bounds__(kLargeBlock, 2) k_sah_build(SahParams p) {
+  __shared__ SahShared sh;
+  const uint32_t G = gridDim.x;
+  const uint32_t gwarp = (blockIdx.x * kLargeBlock + threadIdx.x) >> 5, nwarps = G * (kLargeBlock / 32);
+  uint32_t* status = &p.cnt->status;
+  for (uint32_t level = 0;; ++level) {
+    const Level lv = read_level(p, level);
+    if (lv.L + lv.S == 0) break;
+    if (level > kMaxDepth + 1) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, kStatusBadIndex);
+      break;
+    }
+    uint32_t chunks = 0;
+    if (lv.L > 0) {
+      if (blockIdx.x == 0) large_prep(p, lv, sh);
+      large_bins_init(p, lv);
+      if (!grid_sync(p.bar, G, status)) return;
+      chunks = __ldcg(&p.cnt->chunks);
+      for (uint32_t c = blockIdx.x; c < chunks; c += G) large_bin_chunk(p, lv, c, sh);
+      if (!grid_sync(p.bar, G, status)) return;
+      for (uint32_t t = gwarp; t < lv.L; t += nwarps) large_decide(p, lv, t, sh);
+    }
+    small_thread_phase(p, lv);
+    if (!grid_sync(p.bar, G, status)) return;
+    // large partitions (chunks in ticket order), then queued small tasks
+    if (lv.L > 0) large_partition_phase(p, lv, chunks, sh);
+    small_warp_phase(p, lv, sh);
+    if (!grid_sync(p.bar, G, status)) return;
+    if (lv.L > 0) {
+      for (uint32_t c = blockIdx.x; c < chunks; c += G) large_copyback_chunk(p, lv, c);
+      for (uint32_t c = blockIdx.x * kLargeBlock + threadIdx.x; c < chunks; c += G * kLargeBlock)
+        p.chunk_status[c] = 0;
+    }
+    scan_segment(p, lv, sh);
+    if (!grid_sync(p.bar, G, status)) return;
+    emit_segment(p, lv, sh, true);
+    if (!grid_sync(p.bar, G, status)) return;
+  }
+}
+
+// ---- the same phases as separate launches (large builds): the level number
+// selects the task lists, counters are read at kernel start.
+__global__ void __launch_bounds__(kLargeBlock) k_ph_prep(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  const Level lv = read_level(p, level);
+  if (blockIdx.x == 0) large_prep(p, lv, sh);
+  large_bins_init(p, lv);
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_bin(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  const Level lv = read_level(p, level);
+  const uint32_t chunks = __ldcg(&p.cnt->chunks);
+  for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) large_bin_chunk(p, lv, c, sh);
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_decide(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  const Level lv = read_level(p, level);
+  const uint32_t gwarp = (blockIdx.x * kLargeBlock + threadIdx.x) >> 5, nwarps = gridDim.x * (kLargeBlock / 32);
+  for (uint32_t t = gwarp; t < lv.L; t += nwarps) large_decide(p, lv, t, sh);
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_small(SahParams p, uint32_t level) {
+  small_thread_phase(p, read_level(p, level));
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_partition(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  const Level lv = read_level(p, level);
+  large_partition_phase(p, lv, __ldcg(&p.cnt->chunks), sh);
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_small_warps(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  small_warp_phase(p, read_level(p, level), sh);
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_copyback_scan(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  const Level lv = read_level(p, level);
+  if (lv.L > 0) {
+    const uint32_t chunks = __ldcg(&p.cnt->chunks);
+    for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) large_copyback_chunk(p, lv, c);
+    for (uint32_t c = blockIdx.x * kLargeBlock + threadIdx.x; c < chunks; c += gridDim.x * kLargeBlock)
+      p.chunk_status[c] = 0;
+  }
+  scan_segment(p, lv, sh);
+}
+__global__ void __launch_bounds__(kLargeBlock) k_ph_emit(SahParams p, uint32_t level) {
+  __shared__ SahShared sh;
+  emit_segment(p, read_level(p, level), sh, false);
+}
+// Counters of the next level (after every block of k_ph_emit read them).
+__global__ void k_ph_advance(SahParams p, uint32_t level, uint32_t blocks) {
+  __shared__ SahShared sh;
+  const Level lv = read_level(p, level);
+  uint64_t all = 0;
+  for (uint32_t b = threadIdx.x; b < blocks; b += kLargeBlock) all += __ldcg(p.scan_sums + b);
+  uint64_t tot;
+  block_scan_incl<uint64_t>(all, sh.scan, &tot);
   if (threadIdx.x == 0) {
-    const uint64_t total = p.scan_sums[nb];
-    const uint32_t nl = (uint32_t)(total >> 32), ns = (uint32_t)(total & 0xffffffffu);
-    p.cnt->node_count += nl + ns;
+    const uint32_t nl = (uint32_t)(tot >> 32), ns = (uint32_t)(tot & 0xffffffffu);
+    p.cnt->node_count = lv.node_base + nl + ns;
     p.cnt->large = nl;
     p.cnt->small = ns;
     p.cnt->mq_count = 0;
@@ -1051,11 +1217,11 @@ __global__ void k_sah_init(SahParams p, const DAabb* world) {
     store_aabb(p.nodes, *world);
     const Task root{0u, 0u, p.n, 0u};
     if (p.n > kWarpMax) {
-      p.large[0] = root;
+      p.large[0][0] = root;
       p.cnt->large = 1;
       p.cnt->small = 0;
     } else {
-      p.small[0] = root;
+      p.small[0][0] = root;
       p.cnt->large = 0;
       p.cnt->small = 1;
     }
@@ -1079,35 +1245,54 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   cudaError_t e;
   DAabb* nodes = nullptr;
   uint32_t* indices = nullptr;
-  if ((e = cudaMalloc(&nodes, (size_t)node_cap * sizeof(DAabb)))) return cuda_rc(e);
-  if ((e = cudaMalloc(&indices, (size_t)n * 4))) {
-    cudaFree(nodes);
+  if ((e = device_alloc(&nodes, node_cap, s))) return cuda_rc(e);
+  if ((e = device_alloc(&indices, n, s))) {
+    pool_free(nodes, s);
     return cuda_rc(e);
   }
   auto fail = [&](ResultCode rc) {
-    cudaFree(nodes);
-    cudaFree(indices);
+    pool_free(nodes, s);
+    pool_free(indices, s);
     return rc;
   };
+  // Small builds run as one cooperative launch with a grid sized to the
+  // problem (fewer blocks make each grid barrier cheaper); large builds
+  // launch the phases separately, which lets each phase run at its own
+  // occupancy, and read the level's counts back between levels.
+  const bool coop = n <= kCoopMaxPrims;
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop ? (const void*)k_sah_build
+                                                                         : (const void*)k_ph_small_warps,
+                                                         kLargeBlock, 0)))
+    return fail(cuda_rc(e));
+  if (per_sm < 1) return fail(DeviceError);
+  uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
+  if (coop) {
+    const uint32_t want = (n + kCoopPrimsPerBlock - 1) / kCoopPrimsPerBlock;
+    if (want < grid) grid = want;
+  }
   const uint32_t large_cap = n / (kWarpMax + 1) + 2;
   const uint32_t small_cap = n + 1;
   const uint32_t task_cap = large_cap + small_cap;
   const uint32_t chunk_cap = n / kChunk + large_cap + 2;
   Scratch<DAabb> world;
-  Scratch<uint32_t> acc, idx_b, bins, chunk_base, chunk_status;
+  Scratch<uint32_t> acc, idx_b, bins, chunk_base, chunk_status, mqueue;
   Scratch<Task> large0, large1, small0, small1;
   Scratch<Decision> dec;
   Scratch<float> tbox;
   Scratch<uint64_t> scan_vals, scan_sums;
   Scratch<Counters> cnt;
-  Scratch<uint32_t> mqueue;
-  const uint32_t scan_blocks_cap = (task_cap + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems) + 1;
+  Scratch<GridBarrier> bar;
   if ((e = world.alloc(1, s)) || (e = acc.alloc(8, s)) || (e = idx_b.alloc(n, s)) ||
       (e = bins.alloc((size_t)large_cap * kTaskBinWords, s)) || (e = chunk_base.alloc(large_cap + 1, s)) ||
       (e = chunk_status.alloc(chunk_cap, s)) || (e = large0.alloc(large_cap, s)) || (e = large1.alloc(large_cap, s)) ||
       (e = small0.alloc(small_cap, s)) || (e = small1.alloc(small_cap, s)) || (e = dec.alloc(task_cap, s)) ||
       (e = tbox.alloc((size_t)large_cap * 6, s)) || (e = scan_vals.alloc(task_cap, s)) ||
-      (e = scan_sums.alloc(scan_blocks_cap + 1, s)) || (e = cnt.alloc(1, s)) || (e = mqueue.alloc(small_cap, s)))
+      (e = scan_sums.alloc(grid, s)) || (e = cnt.alloc(1, s)) || (e = mqueue.alloc(small_cap, s)) ||
+      (e = bar.alloc(1, s)))
+    return fail(cuda_rc(e));
+  if ((e = cudaMemsetAsync(chunk_status.ptr, 0, (size_t)chunk_cap * 4, s)) ||
+      (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
     return fail(cuda_rc(e));
   if ((e = launch_world_bounds(aabbs, n, world.ptr, acc.ptr, s))) return fail(cuda_rc(e));
 
@@ -1119,10 +1304,10 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   p.idx_b = idx_b.ptr;
   p.n = n;
   p.max_leaf = prims_per_leaf == 0 ? 1u : (uint32_t)(prims_per_leaf > 0xffffffffu ? 0xffffffffu : prims_per_leaf);
-  p.large = large0.ptr;
-  p.small = small0.ptr;
-  p.large_next = large1.ptr;
-  p.small_next = small1.ptr;
+  p.large[0] = large0.ptr;
+  p.large[1] = large1.ptr;
+  p.small[0] = small0.ptr;
+  p.small[1] = small1.ptr;
   p.dec = dec.ptr;
   p.tbox = tbox.ptr;
   p.bins = bins.ptr;
@@ -1132,47 +1317,42 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   p.scan_sums = scan_sums.ptr;
   p.mqueue = mqueue.ptr;
   p.cnt = cnt.ptr;
-  int small_warp_blocks = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&small_warp_blocks, k_small_warps, 32 * kSmallWarps, 0);
-  if (small_warp_blocks < 1) small_warp_blocks = 1;
+  p.bar = bar.ptr;
   k_sah_init<<<(n + 255) / 256, 256, 0, s>>>(p, world.ptr);
-  k_large_prep<<<1, 1024, 0, s>>>(p);
   Counters h{};
-  if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaStreamSynchronize(s)))
-    return fail(cuda_rc(e));
-  for (uint32_t level = 0; level <= kMaxDepth + 1 && (h.large + h.small) > 0; ++level) {
-    if (h.large > 0) {
-      const size_t nbins = (size_t)h.large * 3 * kBins;
-      const size_t ib = (nbins + 255) / 256, icap = (size_t)sm_count() * 8;
-      k_bins_init<<<(unsigned)(ib < icap ? ib : icap), 256, 0, s>>>(p);
-      k_large_bin<<<h.chunks, kLargeBlock, 0, s>>>(p);
-      k_large_decide<<<(h.large + 3) / 4, 128, 0, s>>>(p);
-      if ((e = cudaMemsetAsync(chunk_status.ptr, 0, (size_t)h.chunks * 4, s))) return fail(cuda_rc(e));
-      k_large_partition<<<h.chunks, kLargeBlock, 0, s>>>(p);
-      k_large_copyback<<<h.chunks, kLargeBlock, 0, s>>>(p);
-    }
-    if (h.small > 0) {
-      k_small<<<(h.small + 127) / 128, 128, 0, s>>>(p);
-      // at most one queued task per 9 primitives of the level's small tasks
-      const size_t wcap = (size_t)sm_count() * small_warp_blocks, wneed = (h.small + kSmallWarps - 1) / kSmallWarps;
-      k_small_warps<<<(unsigned)(wneed < wcap ? wneed : wcap), 32 * kSmallWarps, 0, s>>>(p);
-    }
-    const uint32_t N = h.large + h.small;
-    const uint32_t nb = (N + kScanBlock * kScanItems - 1) / (kScanBlock * kScanItems);
-    k_scan_local<<<nb, kScanBlock, 0, s>>>(p);
-    k_scan_sums<<<1, kScanBlock, 0, s>>>(p, nb);
-    k_emit<<<(N + kScanBlock - 1) / kScanBlock, kScanBlock, 0, s>>>(p, nb);
-    k_advance<<<1, 32, 0, s>>>(p, nb);
-    std::swap(p.large, p.large_next);
-    std::swap(p.small, p.small_next);
-    k_large_prep<<<1, 1024, 0, s>>>(p);
-    if ((e = cudaGetLastError())) return fail(cuda_rc(e));
+  if (coop) {
+    void* args[] = {&p};
+    if ((e = cudaLaunchCooperativeKernel((void*)k_sah_build, dim3(grid), dim3(kLargeBlock), args, 0, s)))
+      return fail(cuda_rc(e));
     if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
         (e = cudaStreamSynchronize(s)))
       return fail(cuda_rc(e));
-    if (h.status) return fail(h.status & kStatusTimeout ? Timeout : Error);
+  } else {
+    h.large = n > kWarpMax ? 1u : 0u;
+    h.small = 1u - h.large;
+    const size_t cap = (size_t)grid;
+    auto blocks = [cap](size_t need) { return (unsigned)(need < 1 ? 1 : (need < cap ? need : cap)); };
+    for (uint32_t level = 0; h.large + h.small > 0; ++level) {
+      if (level > kMaxDepth + 1) return fail(Error);
+      if (h.large) {
+        k_ph_prep<<<blocks(((size_t)h.large * 3 * kBins + kLargeBlock - 1) / kLargeBlock), kLargeBlock, 0, s>>>(p, level);
+        k_ph_bin<<<grid, kLargeBlock, 0, s>>>(p, level);
+        k_ph_decide<<<blocks((h.large + 7) / 8), kLargeBlock, 0, s>>>(p, level);
+      }
+      if (h.small) k_ph_small<<<(h.small + kLargeBlock - 1) / kLargeBlock, kLargeBlock, 0, s>>>(p, level);
+      if (h.large) k_ph_partition<<<grid, kLargeBlock, 0, s>>>(p, level);
+      if (h.small) k_ph_small_warps<<<grid, kLargeBlock, 0, s>>>(p, level);
+      k_ph_copyback_scan<<<grid, kLargeBlock, 0, s>>>(p, level);
+      k_ph_emit<<<grid, kLargeBlock, 0, s>>>(p, level);
+      k_ph_advance<<<1, kLargeBlock, 0, s>>>(p, level, grid);
+      if ((e = cudaGetLastError())) return fail(cuda_rc(e));
+      if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
+          (e = cudaStreamSynchronize(s)))
+        return fail(cuda_rc(e));
+      if (h.status) break;
+    }
   }
+  if (h.status) return fail(h.status & kStatusTimeout ? Timeout : Error);
   if (h.large + h.small > 0) return fail(Error);
   out->nodes = nodes;
   out->indices = indices;
