@@ -41,7 +41,7 @@ constexpr int kChunk = 2048;
 constexpr int kLargeBlock = 256;
 constexpr uint32_t kWarpMax = 1024;
 constexpr uint32_t kCoopMaxPrims = 1u << 20;      // larger builds launch the phases separately
-constexpr uint32_t kCoopPrimsPerBlock = 2048;     // cooperative grid: one block per this many primitives
+constexpr uint32_t kCoopPrimsPerBlock = 512;      // cooperative grid: one block per this many primitives
 constexpr int kBinWords = 8;  // ordered min xyz, ordered max xyz, count, pad
 constexpr int kTaskBinWords = 3 * kBins * kBinWords;
 constexpr uint32_t kFlagAgg = 1u << 30;
@@ -409,6 +409,66 @@ struct alignas(16) SahShared {
   uint32_t chunk, fail, prefix, pad;
 };
 
+// Bins primitives sidx-ordered positions [i0, i1) into `wb` (one warp's or
+// block's shared bins). Neighbours in the index array are usually neighbours
+// in space and share bins, so a run of primitives in one bin is merged in
+// registers and written with atomics only when an axis changes bin.
+template <class IdxFn>
+__device__ __forceinline__ void bin_run(const SahParams& p, const BinMap& bm, uint32_t i0, uint32_t i1, IdxFn idx,
+                                        uint32_t* wb) {
+  uint32_t rbin[3], rmn[3][3], rmx[3][3], rcnt[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    rbin[a] = 0xffffffffu;
+    rcnt[a] = 0;
+  }
+  auto flush = [&](int a) {
+    if (rcnt[a] == 0) return;
+    uint32_t* b = wb + (a * kBins + rbin[a]) * kBinWords;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      atomicMin(b + q, rmn[a][q]);
+      atomicMax(b + 3 + q, rmx[a][q]);
+    }
+    atomicAdd(b + 6, rcnt[a]);
+  };
+#pragma unroll 1
+  for (uint32_t i = i0; i < i1; ++i) {
+    const uint32_t prim = idx(i);
+    const float4 c = __ldg(p.centers + prim);
+    const DAabb box = load_aabb(p.aabbs + prim);
+    const float cc[3] = {c.x, c.y, c.z};
+    uint32_t kmn[3], kmx[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      kmn[q] = float_to_ordered(box.min[q]);
+      kmx[q] = float_to_ordered(box.max[q]);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const uint32_t bin = bin_of(cc[a], bm.c2b[a], bm.off[a]);
+      if (bin != rbin[a]) {
+        flush(a);
+        rbin[a] = bin;
+        rcnt[a] = 0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          rmn[a][q] = kmn[q];
+          rmx[a][q] = kmx[q];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        rmn[a][q] = min(rmn[a][q], kmn[q]);
+        rmx[a][q] = max(rmx[a][q], kmx[q]);
+      }
+      ++rcnt[a];
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) flush(a);
+}
+
 // ------------------------------------------------------------------ large tasks
 // Block 0: task boxes (with the first 1e-4 offset) and chunk offsets of the
 // level's large tasks.
@@ -467,65 +527,10 @@ __device__ void large_bin_chunk(const SahParams& p, const Level& lv, uint32_t ch
   ld_tbox(p.tbox + 6 * (size_t)t, mn, mx);
   const BinMap bm = make_binmap(mn, mx);
   uint32_t* wb = &sh.bins[warp][0];
-  // Each thread bins kChunk / kLargeBlock consecutive primitives. Neighbours
-  // in the index array are usually neighbours in space and share bins, so a
-  // run of primitives in one bin is merged in registers and written to the
-  // warp's shared bins once (atomics only when an axis changes bin).
-  constexpr int PER = kChunk / kLargeBlock;
-  uint32_t rbin[3], rmn[3][3], rmx[3][3], rcnt[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    rbin[a] = 0xffffffffu;
-    rcnt[a] = 0;
-  }
-  auto flush = [&](int a) {
-    if (rcnt[a] == 0) return;
-    uint32_t* b = wb + (a * kBins + rbin[a]) * kBinWords;
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      atomicMin(b + q, rmn[a][q]);
-      atomicMax(b + 3 + q, rmx[a][q]);
-    }
-    atomicAdd(b + 6, rcnt[a]);
-  };
+  // each thread bins kChunk / kLargeBlock consecutive primitives
+  constexpr uint32_t PER = kChunk / kLargeBlock;
   const uint32_t s0 = c0 + threadIdx.x * PER;
-#pragma unroll 1
-  for (int j = 0; j < PER; ++j) {
-    const uint32_t i = s0 + j;
-    if (i >= c1) break;
-    const uint32_t prim = __ldcg(p.idx_a + i);
-    const float4 c = __ldg(p.centers + prim);
-    const DAabb box = load_aabb(p.aabbs + prim);
-    const float cc[3] = {c.x, c.y, c.z};
-    uint32_t kmn[3], kmx[3];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      kmn[q] = float_to_ordered(box.min[q]);
-      kmx[q] = float_to_ordered(box.max[q]);
-    }
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const uint32_t bin = bin_of(cc[a], bm.c2b[a], bm.off[a]);
-      if (bin != rbin[a]) {
-        flush(a);
-        rbin[a] = bin;
-        rcnt[a] = 0;
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          rmn[a][q] = kmn[q];
-          rmx[a][q] = kmx[q];
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        rmn[a][q] = min(rmn[a][q], kmn[q]);
-        rmx[a][q] = max(rmx[a][q], kmx[q]);
-      }
-      ++rcnt[a];
-    }
-  }
-#pragma unroll
-  for (int a = 0; a < 3; ++a) flush(a);
+  bin_run(p, bm, min(s0, c1), min(s0 + PER, c1), [&](uint32_t i) { return __ldcg(p.idx_a + i); }, wb);
   __syncthreads();
   uint32_t* gb = p.bins + (size_t)t * kTaskBinWords;
   for (int i = threadIdx.x; i < 3 * kBins; i += kLargeBlock) {
