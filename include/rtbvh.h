@@ -238,6 +238,31 @@ ResultCode rtbvh_gpu_intersect_bvh_packets(RTBvh bvh, const float *origin_x, con
                                            const float *direction_z, float *t, uintptr_t packet_count, float *hits,
                                            uint32_t flags, uint32_t *stats, rtbvh_stream_t stream);
 
+/* Candidate lists: the device form of intersect_mbvh with a user callback
+ * (rtbvh_ffi/src/lib.rs:700-731) for primitives whose intersection test the
+ * library does not know (spheres, curves, instances, ...). For each ray, the
+ * primitive ids that MbvhIndexIterator (src/iter_indices.rs:212-313) yields
+ * when the callback leaves t unchanged, in yield order, over the exact quad
+ * nodes; t is t_max[r] (NULL: 1e34). The caller then tests the listed
+ * primitives in its own kernel; its nearest accepted hit is the one the
+ * callback iteration would find, since a callback that shortens t only
+ * removes candidates. Ray r's first max_per_ray ids go to
+ * candidates[r * max_per_ray ...] (candidates may be NULL to count only);
+ * counts[r] (required) is the full number of yields, so a count above
+ * max_per_ray means the list was cut and can be fetched again with a larger
+ * stride (UINT32_MAX: the walk hit the stack bound, see rtbvh_gpu_status).
+ * Asynchronous on `stream`. */
+ResultCode rtbvh_gpu_mbvh_candidates(RTMbvh mbvh, const float *rays, const float *t_max, uintptr_t ray_count,
+                                     uint32_t max_per_ray, uint32_t *candidates, uint32_t *counts,
+                                     rtbvh_stream_t stream);
+
+/* The same over the Bvh with BvhIndexIterator (src/iter_indices.rs:18-107),
+ * i.e. intersect (rtbvh_ffi/src/lib.rs:551-581). A ray with a NaN origin or
+ * direction component yields nothing. */
+ResultCode rtbvh_gpu_bvh_candidates(RTBvh bvh, const float *rays, const float *t_max, uintptr_t ray_count,
+                                    uint32_t max_per_ray, uint32_t *candidates, uint32_t *counts,
+                                    rtbvh_stream_t stream);
+
 /* Same as rtbvh_gpu_intersect_mbvh with HOST rays / t_max / hits: copies in,
  * traces and copies out in chunks on two internal streams, and returns when
  * the hits are in host memory. Page-locked host buffers give full speed. */

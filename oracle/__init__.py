@@ -50,6 +50,9 @@ def lib():
                                         ctypes.POINTER(f32p), f32p, ctypes.c_size_t, ctypes.c_float,
                                         f32p, u32p, ctypes.c_uint32]
         L.ror_trace_packets.restype = ctypes.c_int64
+        L.ror_candidates.argtypes = [ctypes.c_int32, f32p, ctypes.c_size_t, u32p, f32p, ctypes.c_size_t, f32p,
+                                     ctypes.c_uint32, u32p, u32p]
+        L.ror_candidates.restype = ctypes.c_int64
         _lib = L
     return _lib
 
@@ -193,6 +196,27 @@ def trace_packets(structure: str, nodes, prim_indices, tris, rays, t=None, t_min
     bad = lib().ror_trace_packets(st, _f(nd), len(nd), _u(idx), _f(tr), arr, _f(tt), P, float(t_min_tri),
                                   _f(hits), _u(sts), threads)
     return hits, sts, int(bad)
+
+
+def candidates(structure: str, nodes, prim_indices, rays, t_max=None, max_per_ray: int = 64):
+    """Primitive ids the reference's index iterator yields per ray when the
+    callback leaves t unchanged, in yield order.
+
+    Returns (cands (R, max_per_ray) uint32, counts (R,) uint32 full yield counts).
+    """
+    st = {"mbvh": 0, "bvh": 1}[structure]
+    nd = _c(nodes, np.float32).reshape(-1, 32 if st == 0 else 8)
+    idx = _c(prim_indices, np.uint32)
+    ry = _c(rays, np.float32).reshape(-1, 6)
+    R = len(ry)
+    tm = None
+    if t_max is not None:
+        tm = _c(np.broadcast_to(np.asarray(t_max, np.float32), (R,)), np.float32)
+    cands = np.zeros((R, max(int(max_per_ray), 1)), np.uint32)
+    counts = np.zeros(R, np.uint32)
+    lib().ror_candidates(st, _f(nd), len(nd), _u(idx), _f(ry), R, _f(tm) if tm is not None else None,
+                         int(max_per_ray), _u(cands), _u(counts))
+    return cands[:, :max_per_ray], counts
 
 
 def hit_prims(hits):

@@ -1268,6 +1268,74 @@ int64_t ror_trace(int32_t structure, const float* nodes, size_t node_count, cons
   return bad.load();
 }
 
+// Candidate lists: the primitives MbvhIndexIterator (src/iter_indices.rs:
+// 212-313, structure 0) or BvhIndexIterator (:18-107, structure 1) yields for
+// each ray when the callback never changes t (rtbvh_ffi/src/lib.rs:700-731
+// with a callback that returns false and leaves t alone), in yield order.
+// Ray r's first max_per_ray ids go to cand_out[r * max_per_ray ...];
+// counts_out[r] is the full number of yields. Returns the number of rays
+// whose stack exceeded the oracle's bound.
+int64_t ror_candidates(int32_t structure, const float* nodes, size_t node_count, const uint32_t* idx,
+                       const float* rays, size_t nrays, const float* t_max, uint32_t max_per_ray,
+                       uint32_t* cand_out, uint32_t* counts_out) {
+  int64_t bad = 0;
+  for (size_t r = 0; r < nrays; ++r) {
+    const float* rr = rays + 6 * r;
+    Ray ray = ray_new(v3(rr[0], rr[1], rr[2]), v3(rr[3], rr[4], rr[5]));
+    if (t_max) ray.t = t_max[r];
+    uint32_t n = 0;
+    auto yield = [&](uint32_t prim) {
+      if (n < max_per_ray) cand_out[r * (size_t)max_per_ray + n] = prim;
+      ++n;
+    };
+    int32_t stack[ORACLE_STACK];
+    if (structure == 0) {
+      const MbvhNode* m = reinterpret_cast<const MbvhNode*>(nodes);
+      if (node_count > 0) {
+        MbvhHit hit = mnode_intersect(m[0], ray);
+        int32_t current = 0, sp = -1;
+        for (;;) {
+          const MbvhNode& node = m[current];
+          for (int i = 0; i < 4; ++i) {
+            const int id = hit.ids[3 - i];
+            if (!hit.result[id]) continue;
+            const int32_t count = node.counts[id], lf = node.children[id];
+            if (count > -1) {
+              for (int32_t j = 0; j < count; ++j) yield(idx[lf + j]);
+            } else if (lf > -1) {
+              if (sp + 1 >= ORACLE_STACK) { ++bad; sp = -1; break; }
+              stack[++sp] = lf;
+            }
+          }
+          if (sp < 0) break;
+          current = stack[sp--];
+          hit = mnode_intersect(m[current], ray);
+        }
+      }
+    } else {
+      const BvhNode* b = reinterpret_cast<const BvhNode*>(nodes);
+      if (node_count > 0 && !v3_is_nan(ray.origin) && !v3_is_nan(ray.direction)) {
+        stack[0] = 0;
+        int32_t sp = 0;
+        while (sp >= 0) {
+          const BvhNode& node = b[stack[sp--]];
+          const int32_t count = node.extra1, lf = node.extra2;
+          if (count > -1) {
+            for (int32_t j = 0; j < count; ++j) yield(idx[lf + j]);
+          } else if (lf > -1) {
+            float lt = 0.0f, rt = 0.0f;
+            const bool lh = aabb_intersect(b[lf], ray, &lt), rh = aabb_intersect(b[lf + 1], ray, &rt);
+            if (sp + 2 >= ORACLE_STACK) { ++bad; break; }
+            sp = sort_nodes(lh, lt, rh, rt, stack, sp, lf);
+          }
+        }
+      }
+    }
+    counts_out[r] = n;
+  }
+  return bad;
+}
+
 // Packet traversal of P packets of four rays (closest hit through the
 // packet triangle test). soa = 6 arrays of 4P floats each (origin x, y, z,
 // direction x, y, z; lane k of packet p at 4p + k); t is 4P floats, in/out

@@ -114,6 +114,8 @@ SIGNATURES = {
                                                 _vp]),
     "rtbvh_gpu_intersect_bvh_packets": (_rc, [RTBvh, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp, _u32, _vp,
                                                _vp]),
+    "rtbvh_gpu_mbvh_candidates": (_rc, [RTMbvh, _vp, _vp, _sz, _u32, _vp, _vp, _vp]),
+    "rtbvh_gpu_bvh_candidates": (_rc, [RTBvh, _vp, _vp, _sz, _u32, _vp, _vp, _vp]),
     "rtbvh_intersect_mbvh_batch": (_rc, [RTMbvh, _vp, _vp, _sz, _vp, _u32]),
     "rtbvh_gpu_status": (_rc, [_u32, ctypes.c_int]),
     "rtbvh_gpu_view": (_rc, [_u32, ctypes.c_int, ctypes.POINTER(RTGpuView)]),

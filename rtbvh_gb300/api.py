@@ -196,6 +196,12 @@ class Bvh:
         stats (P,3) int32 or None)."""
         return _trace_packets(self._lib.rtbvh_gpu_intersect_bvh_packets, self._h, rays, t, stats, stream)
 
+    def candidates(self, rays, t_max=None, max_per_ray=64, stream=None):
+        """Primitive ids BvhIndexIterator yields per ray (callback leaving t
+        unchanged), in order: (cands (R, max_per_ray) int32 CUDA tensor,
+        counts (R,) int32 -- full yield counts, may exceed max_per_ray)."""
+        return _candidates(self._lib.rtbvh_gpu_bvh_candidates, self._h, rays, t_max, max_per_ray, stream)
+
     def status(self):
         return ResultCode(self._lib.rtbvh_gpu_status(self._h.id, 0))
 
@@ -269,6 +275,13 @@ class Mbvh:
         stats (P,3) int32 [node tests, triangle tests, max stack] or None)."""
         return _trace_packets(self._lib.rtbvh_gpu_intersect_mbvh_packets, self._h, rays, t, stats, stream)
 
+    def candidates(self, rays, t_max=None, max_per_ray=64, stream=None):
+        """Primitive ids MbvhIndexIterator yields per ray when the callback
+        leaves t unchanged, in yield order -- the device form of
+        intersect_mbvh with a user callback, for primitives tested by the
+        caller (see Bvh.candidates for the return values)."""
+        return _candidates(self._lib.rtbvh_gpu_mbvh_candidates, self._h, rays, t_max, max_per_ray, stream)
+
     def traversal_tree(self):
         """(exact (count, 32) float32 quad records, compact (count, 16) uint32
         records) of the closest-hit traversal tree, copied to the host."""
@@ -329,6 +342,17 @@ def _trace_packets(fn, handle, rays, t, stats, stream):
     ptrs = [ctypes.c_void_p(soa[k].data_ptr()) for k in range(6)]
     check(fn(handle, *ptrs, _ptr(tt), n // 4, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect_packets")
     return hits, st
+
+
+def _candidates(fn, handle, rays, t_max, max_per_ray, stream):
+    r = _cuda_f32(rays, 6)
+    n = r.shape[0]
+    tm = _cuda_f32(t_max).reshape(-1) if t_max is not None else None
+    m = int(max_per_ray)
+    cands = torch.empty((n, max(m, 1)), dtype=torch.int32, device=r.device) if m > 0 else None
+    counts = torch.empty((n,), dtype=torch.int32, device=r.device)
+    check(fn(handle, _ptr(r), _ptr(tm), n, m, _ptr(cands), _ptr(counts), _stream(stream)), "candidates")
+    return (cands[:, :m] if cands is not None else None), counts
 
 
 class Builder:

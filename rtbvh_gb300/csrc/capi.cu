@@ -739,6 +739,47 @@ ResultCode rtbvh_gpu_intersect_bvh_packets(RTBvh bvh, const float* origin_x, con
   return packets_common(bvh.id, false, o, d, t, packet_count, hits, flags, stats, static_cast<cudaStream_t>(stream));
 }
 
+static ResultCode candidates_common(uint32_t id, bool mbvh, const float* rays, const float* t_max,
+                                    uintptr_t ray_count, uint32_t max_per_ray, uint32_t* candidates,
+                                    uint32_t* counts, cudaStream_t s) {
+  CandArgs a;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(id, mbvh);
+    if (!e) return Error;
+    a.mnodes = e->d_mnodes;
+    a.nodes = e->d_nodes;
+    a.node_count = e->node_count;
+    a.indices = e->d_indices;
+    a.prim_count = e->prim_count;
+    a.status = e->d_status;
+  }
+  if (ray_count == 0) return Ok;
+  if (rays == nullptr || counts == nullptr) return Error;
+  if (candidates != nullptr && max_per_ray == 0) return InvalidArgument;
+  a.rays = rays;
+  a.t_max = t_max;
+  a.ray_count = ray_count;
+  a.max_per_ray = candidates ? max_per_ray : 0u;
+  a.out = candidates;
+  a.counts = counts;
+  return cuda_rc(launch_candidates(a, mbvh, s));
+}
+
+ResultCode rtbvh_gpu_mbvh_candidates(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
+                                     uint32_t max_per_ray, uint32_t* candidates, uint32_t* counts,
+                                     rtbvh_stream_t stream) {
+  return candidates_common(mbvh.id, true, rays, t_max, ray_count, max_per_ray, candidates, counts,
+                           static_cast<cudaStream_t>(stream));
+}
+
+ResultCode rtbvh_gpu_bvh_candidates(RTBvh bvh, const float* rays, const float* t_max, uintptr_t ray_count,
+                                    uint32_t max_per_ray, uint32_t* candidates, uint32_t* counts,
+                                    rtbvh_stream_t stream) {
+  return candidates_common(bvh.id, false, rays, t_max, ray_count, max_per_ray, candidates, counts,
+                           static_cast<cudaStream_t>(stream));
+}
+
 ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
                                       float* hits, uint32_t flags) {
   if (ray_count == 0) return Ok;

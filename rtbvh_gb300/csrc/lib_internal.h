@@ -160,6 +160,25 @@ struct TraceArgs {
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);
 
+// Candidate lists (see k_candidates in traverse.cu): ray r's first
+// max_per_ray yielded primitive ids go to out[r * max_per_ray ...] (out may
+// be NULL); counts[r] is the number of yields (UINT32_MAX: the walk failed).
+struct CandArgs {
+  const DMNode* mnodes = nullptr;
+  const DAabb* nodes = nullptr;
+  uint32_t node_count = 0;
+  const uint32_t* indices = nullptr;
+  uint32_t prim_count = 0;
+  const float* rays = nullptr;
+  const float* t_max = nullptr;
+  size_t ray_count = 0;
+  uint32_t max_per_ray = 0;
+  uint32_t* out = nullptr;
+  uint32_t* counts = nullptr;
+  uint32_t* status = nullptr;
+};
+cudaError_t launch_candidates(const CandArgs& a, bool mbvh, cudaStream_t s);
+
 // Packets of four rays (see packets.cu). origin/direction: three arrays of
 // 4 * packet_count floats each (lane k of packet p at 4p + k); t: in/out.
 struct PacketArgs {

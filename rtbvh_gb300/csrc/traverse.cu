@@ -538,6 +538,112 @@ __global__ void __launch_bounds__(kBlock) k_trace_bvh(TraceArgs a, unsigned int*
   }
 }
 
+// ------------------------------------------------------------------ candidate lists
+// The primitives the reference's index iterators yield for a ray when the
+// caller's callback leaves t unchanged: MbvhIndexIterator
+// (src/iter_indices.rs:212-313) or BvhIndexIterator (:18-107) over the exact
+// nodes, in yield order. This is the device form of intersect /
+// intersect_mbvh with a user callback (rtbvh_ffi/src/lib.rs:551-581,
+// 700-731) for primitives whose test the library does not know: the caller
+// tests the listed primitives in its own kernel. One ray per thread.
+template <bool MBVH>
+__global__ void __launch_bounds__(kBlock) k_candidates(CandArgs a) {
+  const size_t stride = (size_t)gridDim.x * kBlock;
+  for (size_t r = (size_t)blockIdx.x * kBlock + threadIdx.x; r < a.ray_count; r += stride) {
+    const RayState ray = load_ray(a.rays, r, a.t_max);
+    uint32_t n = 0;
+    bool bad = false;
+    auto yield_range = [&](int32_t lf, int32_t count) {
+      if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
+        atomicOr(a.status, kStatusBadIndex);
+        bad = true;
+        return;
+      }
+      for (int32_t j = 0; j < count; ++j) {
+        if (a.out && n < a.max_per_ray) a.out[r * a.max_per_ray + n] = __ldg(a.indices + lf + j);
+        ++n;
+      }
+    };
+    int32_t stack[kStack];
+    int sp = -1;
+    if (MBVH) {
+      if (a.node_count > 0) {
+        const bool fast = finite_ray(ray);
+        int32_t current = 0;
+        for (;;) {
+          uint32_t mask, ids;
+          int4 children, counts;
+          if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
+          else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
+          for (int i = 0; i < 4 && !bad; ++i) {
+            const uint32_t id = (ids >> (2 * (3 - i))) & 3u;
+            if (!((mask >> id) & 1u)) continue;
+            const int32_t count = sel4(counts, id), lf = sel4(children, id);
+            if (count > -1) {
+              yield_range(lf, count);
+            } else if (lf > -1) {
+              if (sp + 1 >= kStack) {
+                atomicOr(a.status, kStatusStackOverflow);
+                bad = true;
+                break;
+              }
+              stack[++sp] = lf;
+            }
+          }
+          if (bad || sp < 0) break;
+          current = stack[sp--];
+          if ((uint32_t)current >= a.node_count) {
+            atomicOr(a.status, kStatusBadIndex);
+            bad = true;
+            break;
+          }
+        }
+      }
+    } else {
+      const bool nan = (ray.ox != ray.ox) || (ray.oy != ray.oy) || (ray.oz != ray.oz) || (ray.dx != ray.dx) ||
+                       (ray.dy != ray.dy) || (ray.dz != ray.dz);
+      sp = (a.node_count == 0 || nan) ? -1 : 0;
+      stack[0] = 0;
+      while (sp >= 0 && !bad) {
+        const int32_t ni = stack[sp--];
+        if ((uint32_t)ni >= a.node_count) {
+          atomicOr(a.status, kStatusBadIndex);
+          bad = true;
+          break;
+        }
+        const DAabb node = load_aabb(a.nodes + ni);
+        if (node.count > -1) {
+          yield_range(node.left_first, node.count);
+        } else if (node.left_first > -1) {
+          const int32_t lf = node.left_first;
+          if ((uint32_t)lf + 1u >= a.node_count) {
+            atomicOr(a.status, kStatusBadIndex);
+            bad = true;
+            break;
+          }
+          float lt = 0.0f, rt = 0.0f;
+          const bool lh = slab_far(load_aabb(a.nodes + lf), ray, lt);
+          const bool rh = slab_far(load_aabb(a.nodes + lf + 1), ray, rt);
+          if (sp + 2 >= kStack) {
+            atomicOr(a.status, kStatusStackOverflow);
+            bad = true;
+            break;
+          }
+          if (lh && rh) {
+            if (lt < rt) { stack[++sp] = lf; stack[++sp] = lf + 1; }
+            else { stack[++sp] = lf + 1; stack[++sp] = lf; }
+          } else if (lh) {
+            stack[++sp] = lf;
+          } else if (rh) {
+            stack[++sp] = lf + 1;
+          }
+        }
+      }
+    }
+    a.counts[r] = bad ? 0xffffffffu : n;
+  }
+}
+
 // ------------------------------------------------------------------ ray order
 // Incoherent rays are traced in an order that groups rays with nearby
 // origins and similar directions, so that the lanes of a warp walk similar
@@ -687,5 +793,18 @@ cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
 
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s) { return launch_any<true>(a, s); }
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s) { return launch_any<false>(a, s); }
+
+cudaError_t launch_candidates(const CandArgs& a, bool mbvh, cudaStream_t s) {
+  if (a.ray_count == 0) return cudaSuccess;
+  auto kern = mbvh ? k_candidates<true> : k_candidates<false>;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  size_t grid = (size_t)sm_count() * per_sm;
+  const size_t need = (a.ray_count + kBlock - 1) / kBlock;
+  if (grid > need) grid = need;
+  kern<<<(unsigned)grid, kBlock, 0, s>>>(a);
+  return cudaGetLastError();
+}
 
 }  // namespace rtbvh
