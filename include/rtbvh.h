@@ -297,6 +297,36 @@ ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode **exact, const
 ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float *vertices, const RTAabb *aabbs, uint32_t mbvh_id,
                            rtbvh_stream_t stream);
 
+/* An Mbvh refit (the reference refits only the Bvh, src/bvh.rs:176-205): the
+ * Mbvh keeps its own copy of the Bvh's nodes, as the crate's Mbvh does
+ * (src/bvh.rs:318-324); this refits that copy with Bvh::refit's arithmetic
+ * from device triangles or device aabbs (exactly one non-NULL), then
+ * collapses the quad nodes again (Mbvh::construct, same topology) and
+ * re-lays the triangles. The source Bvh is not needed and not changed. */
+ResultCode rtbvh_gpu_refit_mbvh(uint32_t mbvh_id, const float *vertices, const RTAabb *aabbs,
+                                rtbvh_stream_t stream);
+
+/* On-disk form of the crate's serde derives (src/bvh.rs:141-147 Bvh,
+ * :318-324 Mbvh) as bincode 1 writes them with its default options:
+ * little-endian fixed-width integers, a u64 length before each Vec, nodes as
+ * their 32-byte RTAabb / 128-byte RTMbvhNode records, the BuildType as a u32
+ * variant index (None 0, LocallyOrderedClustered 1, BinnedSAH 2, Spatial 3):
+ *   Bvh:  u64 N, N x RTBvhNode, u64 M, M x uint32 index, uint32 build type
+ *   Mbvh: u64 N, N x RTBvhNode, u64 Q, Q x RTMbvhNode, u64 M, M x uint32 index
+ * serialize: buffer NULL (or too small: InvalidArgument) -> *size receives the
+ * byte count. deserialize: validates the layout, the leaf ranges, child
+ * pairs and indices (InvalidArgument otherwise; no primitives:
+ * NoPrimitives) and, for an Mbvh, that the quad nodes are the collapse of
+ * the stored Bvh nodes; creates a library-owned structure (host mirror
+ * unless RTBVH_FLAG_NO_HOST_MIRROR). Triangles are not part of the format:
+ * attach them with rtbvh_gpu_set_triangles before a GPU trace. */
+ResultCode rtbvh_serialize_bvh(RTBvh bvh, uint8_t *buffer, uintptr_t capacity, uintptr_t *size);
+ResultCode rtbvh_deserialize_bvh(const uint8_t *buffer, uintptr_t size, uint32_t flags, rtbvh_stream_t stream,
+                                 RTBvh *result);
+ResultCode rtbvh_serialize_mbvh(RTMbvh mbvh, uint8_t *buffer, uintptr_t capacity, uintptr_t *size);
+ResultCode rtbvh_deserialize_mbvh(const uint8_t *buffer, uintptr_t size, uint32_t flags, rtbvh_stream_t stream,
+                                  RTMbvh *result);
+
 /* Largest tree (in nodes) that rtbvh_gpu_refit_noalloc accepts: 1,048,576
  * nodes, i.e. a BVH over up to 524,288 primitives. */
 #define RTBVH_REFIT_NOALLOC_MAX_NODES 1048576u

@@ -121,6 +121,11 @@ SIGNATURES = {
     "rtbvh_gpu_view": (_rc, [_u32, ctypes.c_int, ctypes.POINTER(RTGpuView)]),
     "rtbvh_gpu_traversal_tree": (_rc, [RTMbvh, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_u32)]),
     "rtbvh_gpu_refit": (_rc, [_u32, _vp, _vp, _u32, _vp]),
+    "rtbvh_gpu_refit_mbvh": (_rc, [_u32, _vp, _vp, _vp]),
+    "rtbvh_serialize_bvh": (_rc, [RTBvh, _vp, _sz, ctypes.POINTER(_sz)]),
+    "rtbvh_deserialize_bvh": (_rc, [_vp, _sz, _u32, _vp, ctypes.POINTER(RTBvh)]),
+    "rtbvh_serialize_mbvh": (_rc, [RTMbvh, _vp, _sz, ctypes.POINTER(_sz)]),
+    "rtbvh_deserialize_mbvh": (_rc, [_vp, _sz, _u32, _vp, ctypes.POINTER(RTMbvh)]),
     "rtbvh_gpu_refit_noalloc": (_rc, [_u32, _vp, _vp]),
     "rtbvh_gpu_intersect_backward": (_rc, [_vp, _sz, _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
     "rtbvh_gpu_batch_create": (_rc, [_vp, _vp, _u32, _vp, _vp, _vp, _vp, _u32, _vp, ctypes.POINTER(RTBatch)]),

@@ -202,6 +202,35 @@ class Bvh:
         counts (R,) int32 -- full yield counts, may exceed max_per_ray)."""
         return _candidates(self._lib.rtbvh_gpu_bvh_candidates, self._h, rays, t_max, max_per_ray, stream)
 
+    def attach_triangles(self, vertices, stream=None):
+        """Device triangles (n, 3, 3) for the GPU traces of a structure that
+        has none (e.g. one loaded with from_bytes)."""
+        v = _cuda_f32(vertices)
+        check(self._lib.rtbvh_gpu_set_triangles(self._h.id, 0, _ptr(v), self._n, _stream(stream)), "set_triangles")
+
+    def to_bytes(self):
+        """The crate's serde form of the Bvh in bincode 1 layout (see rtbvh.h)."""
+        return _serialize(self._lib.rtbvh_serialize_bvh, self._h)
+
+    @classmethod
+    def from_bytes(cls, data, host_mirror=True, stream=None):
+        lib = _ffi.load()
+        out = _ffi.RTBvh()
+        buf = bytes(data)
+        flags = 0 if host_mirror else _ffi.FLAG_NO_HOST_MIRROR
+        check(lib.rtbvh_deserialize_bvh(buf, len(buf), flags, _stream(stream), ctypes.byref(out)), "deserialize_bvh")
+        build_type = BuildType(int.from_bytes(buf[-4:], "little"))
+        return cls(out, build_type, out.index_count)
+
+    def save(self, path):
+        with open(path, "wb") as f:
+            f.write(self.to_bytes())
+
+    @classmethod
+    def load(cls, path, host_mirror=True):
+        with open(path, "rb") as f:
+            return cls.from_bytes(f.read(), host_mirror=host_mirror)
+
     def status(self):
         return ResultCode(self._lib.rtbvh_gpu_status(self._h.id, 0))
 
@@ -282,6 +311,47 @@ class Mbvh:
         caller (see Bvh.candidates for the return values)."""
         return _candidates(self._lib.rtbvh_gpu_mbvh_candidates, self._h, rays, t_max, max_per_ray, stream)
 
+    def refit(self, new_aabbs=None, triangles=None, stream=None):
+        """Refits the Mbvh's own copy of its Bvh nodes (Bvh::refit's
+        arithmetic) and collapses the quad nodes again; the source Bvh is
+        left as it was."""
+        if (new_aabbs is None) == (triangles is None):
+            raise ValueError("give exactly one of new_aabbs / triangles")
+        if triangles is not None:
+            v = triangles.vertices if isinstance(triangles, Triangles) else _cuda_f32(triangles)
+            check(self._lib.rtbvh_gpu_refit_mbvh(self._h.id, _ptr(v), None, _stream(stream)), "refit_mbvh")
+        else:
+            a = _cuda_f32(_aabbs_array(new_aabbs))
+            check(self._lib.rtbvh_gpu_refit_mbvh(self._h.id, None, _ptr(a), _stream(stream)), "refit_mbvh")
+
+    def attach_triangles(self, vertices, stream=None):
+        """Device triangles (n, 3, 3) for the GPU traces (see Bvh.attach_triangles)."""
+        v = _cuda_f32(vertices)
+        check(self._lib.rtbvh_gpu_set_triangles(self._h.id, 1, _ptr(v), self._n, _stream(stream)), "set_triangles")
+
+    def to_bytes(self):
+        """The crate's serde form of the Mbvh in bincode 1 layout (see rtbvh.h)."""
+        return _serialize(self._lib.rtbvh_serialize_mbvh, self._h)
+
+    @classmethod
+    def from_bytes(cls, data, host_mirror=True, stream=None):
+        lib = _ffi.load()
+        out = _ffi.RTMbvh()
+        buf = bytes(data)
+        flags = 0 if host_mirror else _ffi.FLAG_NO_HOST_MIRROR
+        check(lib.rtbvh_deserialize_mbvh(buf, len(buf), flags, _stream(stream), ctypes.byref(out)),
+              "deserialize_mbvh")
+        return cls(out, out.index_count, None)
+
+    def save(self, path):
+        with open(path, "wb") as f:
+            f.write(self.to_bytes())
+
+    @classmethod
+    def load(cls, path, host_mirror=True):
+        with open(path, "rb") as f:
+            return cls.from_bytes(f.read(), host_mirror=host_mirror)
+
     def traversal_tree(self):
         """(exact (count, 32) float32 quad records, compact (count, 16) uint32
         records) of the closest-hit traversal tree, copied to the host."""
@@ -342,6 +412,14 @@ def _trace_packets(fn, handle, rays, t, stats, stream):
     ptrs = [ctypes.c_void_p(soa[k].data_ptr()) for k in range(6)]
     check(fn(handle, *ptrs, _ptr(tt), n // 4, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect_packets")
     return hits, st
+
+
+def _serialize(fn, handle):
+    size = ctypes.c_size_t(0)
+    check(fn(handle, None, 0, ctypes.byref(size)), "serialize")
+    buf = ctypes.create_string_buffer(size.value)
+    check(fn(handle, buf, size.value, ctypes.byref(size)), "serialize")
+    return buf.raw[:size.value]
 
 
 def _candidates(fn, handle, rays, t_max, max_per_ray, stream):

@@ -26,7 +26,9 @@ struct Entry {
   bool mirrored = false;
   uint32_t node_count = 0;
   uint32_t prim_count = 0;
-  DAabb* d_nodes = nullptr;       // Bvh
+  DAabb* d_nodes = nullptr;       // Bvh; Mbvh: its own copy of the source Bvh's nodes
+  uint32_t bvh_node_count = 0;    // Mbvh: entries of d_nodes
+  uint32_t build_type = 0;        // Bvh: the crate's BuildType (1 LOCB, 2 binned SAH)
   DMNode* d_mnodes = nullptr;     // Mbvh
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
@@ -149,6 +151,7 @@ ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t
   e->prim_count = (uint32_t)n;
   e->d_nodes = out.nodes;
   e->d_indices = out.indices;
+  e->build_type = type == LocallyOrderedClustered ? 1u : 2u;
   cudaError_t err;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
     e->release();
@@ -598,9 +601,13 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     return rc;
   }
 
+  e->bvh_node_count = node_count;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
       (err = device_alloc(&e->d_indices, prim_count, s)) ||
-      (err = cudaMemcpyAsync(e->d_indices, d_indices, (size_t)prim_count * 4, cudaMemcpyDeviceToDevice, s))) {
+      (err = cudaMemcpyAsync(e->d_indices, d_indices, (size_t)prim_count * 4, cudaMemcpyDeviceToDevice, s)) ||
+      (err = device_alloc(&e->d_nodes, node_count, s)) ||
+      (err = cudaMemcpyAsync(e->d_nodes, d_nodes, (size_t)node_count * sizeof(DAabb), cudaMemcpyDeviceToDevice,
+                             s))) {
     e->release();
     return cuda_rc(err);
   }
@@ -858,6 +865,71 @@ ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode** exact, const
   return Ok;
 }
 
+// Re-collapses Mbvh entry m from BVH2 nodes after a refit: fresh quad nodes
+// (same count and topology), a fresh traversal tree, triangles re-laid from
+// `vertices` when given, and the host mirror refreshed.
+static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, const float* vertices,
+                             cudaStream_t s) {
+  const size_t n = m->prim_count;
+  DMNode* fresh = nullptr;
+  uint32_t count = 0;
+  ResultCode rc;
+  cudaError_t err;
+  if ((rc = build_mbvh(nodes, node_count, s, &fresh, &count)) != Ok) return rc;
+  if (count != m->node_count) {
+    pool_free(fresh, s);
+    return Error;
+  }
+  {
+    // the old arrays may still be read by traversals on other streams
+    void* const old_arrays[] = {m->d_mnodes, m->d_qnodes, m->d_wnodes};
+    pool_free_now(old_arrays, 3);
+  }
+  m->d_mnodes = fresh;
+  m->d_qnodes = nullptr;
+  m->d_wnodes = nullptr;
+  m->wcount = 0;
+  if ((rc = build_wide(nodes, node_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok) return rc;
+  if (vertices) {
+    if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
+    if (!m->d_tris && (err = device_alloc(&m->d_tris, (size_t)kTriFloat4 * n, s))) return cuda_rc(err);
+    if ((err = cudaMemcpyAsync(m->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
+        (err = launch_gather_triangles(m->d_vertices, m->d_indices, n, m->d_tris, s)))
+      return cuda_rc(err);
+  }
+  if (m->mirrored && (rc = mirror_mbvh(*m, s)) != Ok) return rc;
+  return Ok;
+}
+
+// New primitive boxes from device triangles (written to `boxes`) or taken
+// from device aabbs.
+static cudaError_t refit_boxes(const float* vertices, const RTAabb* aabbs, size_t n, Scratch<DAabb>& d_a,
+                               Scratch<float4>& d_c4, const DAabb** boxes, cudaStream_t s) {
+  *boxes = reinterpret_cast<const DAabb*>(aabbs);
+  if (!vertices) return cudaSuccess;
+  cudaError_t err;
+  if ((err = d_a.alloc(n, s)) || (err = d_c4.alloc(n, s))) return err;
+  if ((err = launch_triangle_prep(vertices, n, d_a.ptr, d_c4.ptr, s))) return err;
+  *boxes = d_a.ptr;
+  return cudaSuccess;
+}
+
+ResultCode rtbvh_gpu_refit_mbvh(uint32_t mbvh_id, const float* vertices, const RTAabb* aabbs, rtbvh_stream_t stream) {
+  if ((vertices == nullptr) == (aabbs == nullptr)) return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* m = lookup(mbvh_id, true);
+  if (!m || !m->d_nodes) return Error;
+  Scratch<DAabb> d_a;
+  Scratch<float4> d_c4;
+  const DAabb* boxes = nullptr;
+  cudaError_t err;
+  if ((err = refit_boxes(vertices, aabbs, m->prim_count, d_a, d_c4, &boxes, s))) return cuda_rc(err);
+  ResultCode rc = refit_bvh(m->d_nodes, m->bvh_node_count, m->d_indices, m->prim_count, boxes, s);
+  if (rc != Ok) return rc;
+  return recollapse(m, m->d_nodes, m->bvh_node_count, vertices, s);
+}
+
 ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb* aabbs, uint32_t mbvh_id,
                            rtbvh_stream_t stream) {
   if ((vertices == nullptr) == (aabbs == nullptr)) return Error;
@@ -888,31 +960,10 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
   ResultCode rc = refit_bvh(b->d_nodes, b->node_count, b->d_indices, b->prim_count, boxes, s);
   if (rc != Ok) return rc;
   if (m) {
-    DMNode* fresh = nullptr;
-    uint32_t count = 0;
-    if ((rc = build_mbvh(b->d_nodes, b->node_count, s, &fresh, &count)) != Ok) return rc;
-    if (count != m->node_count) {
-      pool_free(fresh, s);
-      return Error;
-    }
-    {
-      // the old arrays may still be read by traversals on other streams
-      void* const old_arrays[] = {m->d_mnodes, m->d_qnodes, m->d_wnodes};
-      pool_free_now(old_arrays, 3);
-    }
-    m->d_mnodes = fresh;
-    m->d_qnodes = nullptr;
-    m->d_wnodes = nullptr;
-    m->wcount = 0;
-    if ((rc = build_wide(b->d_nodes, b->node_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok) return rc;
-    if (vertices) {
-      if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
-      if (!m->d_tris && (err = device_alloc(&m->d_tris, (size_t)kTriFloat4 * n, s))) return cuda_rc(err);
-      if ((err = cudaMemcpyAsync(m->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
-          (err = launch_gather_triangles(m->d_vertices, m->d_indices, n, m->d_tris, s)))
-        return cuda_rc(err);
-    }
-    if (m->mirrored && (rc = mirror_mbvh(*m, s)) != Ok) return rc;
+    if (m->d_nodes && (err = cudaMemcpyAsync(m->d_nodes, b->d_nodes, (size_t)b->node_count * sizeof(DAabb),
+                                             cudaMemcpyDeviceToDevice, s)))
+      return cuda_rc(err);
+    if ((rc = recollapse(m, b->d_nodes, b->node_count, vertices, s)) != Ok) return rc;
   }
   if (b->mirrored && (rc = mirror_bvh(*b, s)) != Ok) return rc;
   return Ok;
@@ -949,3 +1000,237 @@ ResultCode rtbvh_gpu_intersect_backward(const float* vertices, uintptr_t prim_co
 const char* rtbvh_gpu_version(void) { return "rtbvh-gb300 0.1.0 (sm_103a)"; }
 
 }  // extern "C"
+
+// ============================================================ on-disk format
+// The serde derives of the crate (src/bvh.rs:141-147, :318-324,
+// src/bvh_node.rs:9-14, src/mbvh_node.rs:26-38, src/aabb.rs:12-20) encoded
+// with bincode 1's default options: little-endian fixed-width integers, a
+// u64 length before every Vec, glam's Vec3 as three f32, enums as a u32
+// variant index. So a BvhNode is the 32-byte RTAabb record, an MbvhNode the
+// 128-byte RTMbvhNode record, and
+//   Bvh  = u64 N, N nodes, u64 M, M u32 indices, u32 BuildType
+//   Mbvh = u64 N, N nodes, u64 Q, Q quad nodes, u64 M, M u32 indices
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ != __ORDER_LITTLE_ENDIAN__
+#error "the serialized layout assumes a little-endian host"
+#endif
+
+namespace {
+
+struct ByteWriter {
+  uint8_t* out;
+  size_t cap, n = 0;
+  void put(const void* src, size_t k) {
+    if (out && n + k <= cap) std::memcpy(out + n, src, k);
+    n += k;
+  }
+  void u64(uint64_t v) { put(&v, 8); }
+  void u32(uint32_t v) { put(&v, 4); }
+};
+
+struct ByteReader {
+  const uint8_t* in;
+  size_t size, n = 0;
+  bool ok = true;
+  const uint8_t* take(size_t k) {
+    if (!ok || k > size - n) {
+      ok = false;
+      return nullptr;
+    }
+    const uint8_t* p = in + n;
+    n += k;
+    return p;
+  }
+  uint64_t u64() {
+    uint64_t v = 0;
+    if (const uint8_t* p = take(8)) std::memcpy(&v, p, 8);
+    return v;
+  }
+  uint32_t u32() {
+    uint32_t v = 0;
+    if (const uint8_t* p = take(4)) std::memcpy(&v, p, 4);
+    return v;
+  }
+};
+
+template <class T>
+ResultCode fetch_device(std::vector<T>& out, const T* d, size_t count) {
+  out.resize(count);
+  if (count == 0) return Ok;
+  cudaError_t e;
+  if ((e = cudaDeviceSynchronize()) || (e = cudaMemcpy(out.data(), d, count * sizeof(T), cudaMemcpyDeviceToHost)))
+    return cuda_rc(e);
+  return Ok;
+}
+
+// Leaf ranges inside [0, prim_count), children pairs inside the node array.
+bool nodes_valid(const RTAabb* nodes, uint64_t count, uint64_t prim_count) {
+  for (uint64_t i = 0; i < count; ++i) {
+    const RTAabb& b = nodes[i];
+    if (b.count >= 0) {
+      if (b.left_first < 0 || (uint64_t)b.left_first + (uint64_t)b.count > prim_count) return false;
+    } else if (b.left_first >= 0 && (uint64_t)b.left_first + 1 >= count) {
+      return false;
+    }
+  }
+  return true;
+}
+
+bool indices_valid(const uint32_t* idx, uint64_t count) {
+  for (uint64_t i = 0; i < count; ++i)
+    if (idx[i] >= count) return false;
+  return true;
+}
+
+// Uploads nodes and indices into a new entry (status word, host mirror).
+ResultCode upload_entry(Entry& e, const RTAabb* nodes, uint64_t node_count, const uint32_t* idx, uint64_t prim_count,
+                        cudaStream_t s) {
+  cudaError_t err;
+  if ((err = device_alloc(&e.d_status, 4, s)) || (err = cudaMemsetAsync(e.d_status, 0, 16, s)) ||
+      (err = device_alloc(&e.d_nodes, node_count, s)) ||
+      (err = cudaMemcpyAsync(e.d_nodes, nodes, node_count * sizeof(DAabb), cudaMemcpyHostToDevice, s)) ||
+      (err = device_alloc(&e.d_indices, prim_count, s)) ||
+      (err = cudaMemcpyAsync(e.d_indices, idx, prim_count * 4, cudaMemcpyHostToDevice, s)) ||
+      (err = cudaStreamSynchronize(s)))
+    return cuda_rc(err);
+  return Ok;
+}
+
+}  // namespace
+
+ResultCode rtbvh_serialize_bvh(RTBvh bvh, uint8_t* buffer, uintptr_t capacity, uintptr_t* size) {
+  if (size == nullptr) return Error;
+  std::vector<DAabb> nodes;
+  std::vector<uint32_t> idx;
+  uint32_t build_type;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(bvh.id, false);
+    if (!e) return Error;
+    build_type = e->build_type;
+    ResultCode rc;
+    if ((rc = fetch_device(nodes, e->d_nodes, e->node_count)) != Ok ||
+        (rc = fetch_device(idx, e->d_indices, e->prim_count)) != Ok)
+      return rc;
+  }
+  ByteWriter w{buffer, buffer ? (size_t)capacity : 0};
+  w.u64(nodes.size());
+  w.put(nodes.data(), nodes.size() * sizeof(DAabb));
+  w.u64(idx.size());
+  w.put(idx.data(), idx.size() * 4);
+  w.u32(build_type);
+  *size = w.n;
+  if (buffer && w.n > capacity) return InvalidArgument;
+  return Ok;
+}
+
+ResultCode rtbvh_deserialize_bvh(const uint8_t* buffer, uintptr_t size, uint32_t flags, rtbvh_stream_t stream,
+                                 RTBvh* result) {
+  if (buffer == nullptr || result == nullptr) return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ByteReader r{buffer, (size_t)size};
+  const uint64_t nn = r.u64();
+  const RTAabb* nodes = nn <= (size - r.n) / 32 ? reinterpret_cast<const RTAabb*>(r.take(nn * 32)) : nullptr;
+  const uint64_t ni = r.ok ? r.u64() : 0;
+  const uint8_t* ip = ni <= (size - r.n) / 4 ? r.take(ni * 4) : nullptr;
+  const uint32_t bt = r.u32();
+  if (!r.ok || !nodes || !ip || r.n != size || bt > 3) return InvalidArgument;
+  if (nn == 0 || ni == 0) return NoPrimitives;
+  if (nn > 0xffffffffull || ni > 0xffffffffull) return InvalidArgument;
+  // the buffer may be unaligned: copy into aligned host arrays
+  std::vector<RTAabb> hn(nn);
+  std::vector<uint32_t> hi(ni);
+  std::memcpy(hn.data(), nodes, nn * 32);
+  std::memcpy(hi.data(), ip, ni * 4);
+  if (!nodes_valid(hn.data(), nn, ni) || !indices_valid(hi.data(), ni)) return InvalidArgument;
+  auto e = std::make_unique<Entry>();
+  e->alive = true;
+  e->node_count = (uint32_t)nn;
+  e->prim_count = (uint32_t)ni;
+  e->build_type = bt;
+  ResultCode rc = upload_entry(*e, hn.data(), nn, hi.data(), ni, s);
+  if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_bvh(*e, s);
+  if (rc != Ok) {
+    e->release();
+    return rc;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* raw = e.get();
+  uint32_t id = store(std::move(e), false);
+  *result = bvh_handle(id, *raw);
+  return Ok;
+}
+
+ResultCode rtbvh_serialize_mbvh(RTMbvh mbvh, uint8_t* buffer, uintptr_t capacity, uintptr_t* size) {
+  if (size == nullptr) return Error;
+  std::vector<DAabb> nodes;
+  std::vector<DMNode> mnodes;
+  std::vector<uint32_t> idx;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    Entry* e = lookup(mbvh.id, true);
+    if (!e || !e->d_nodes) return Error;
+    ResultCode rc;
+    if ((rc = fetch_device(nodes, e->d_nodes, e->bvh_node_count)) != Ok ||
+        (rc = fetch_device(mnodes, e->d_mnodes, e->node_count)) != Ok ||
+        (rc = fetch_device(idx, e->d_indices, e->prim_count)) != Ok)
+      return rc;
+  }
+  ByteWriter w{buffer, buffer ? (size_t)capacity : 0};
+  w.u64(nodes.size());
+  w.put(nodes.data(), nodes.size() * sizeof(DAabb));
+  w.u64(mnodes.size());
+  w.put(mnodes.data(), mnodes.size() * sizeof(DMNode));
+  w.u64(idx.size());
+  w.put(idx.data(), idx.size() * 4);
+  *size = w.n;
+  if (buffer && w.n > capacity) return InvalidArgument;
+  return Ok;
+}
+
+ResultCode rtbvh_deserialize_mbvh(const uint8_t* buffer, uintptr_t size, uint32_t flags, rtbvh_stream_t stream,
+                                  RTMbvh* result) {
+  if (buffer == nullptr || result == nullptr) return Error;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ByteReader r{buffer, (size_t)size};
+  const uint64_t nn = r.u64();
+  const uint8_t* np = nn <= (size - r.n) / 32 ? r.take(nn * 32) : nullptr;
+  const uint64_t nq = r.ok ? r.u64() : 0;
+  const uint8_t* qp = nq <= (size - r.n) / 128 ? r.take(nq * 128) : nullptr;
+  const uint64_t ni = r.ok ? r.u64() : 0;
+  const uint8_t* ip = ni <= (size - r.n) / 4 ? r.take(ni * 4) : nullptr;
+  if (!r.ok || !np || !qp || !ip || r.n != size) return InvalidArgument;
+  if (nn == 0 || ni == 0) return NoPrimitives;
+  if (nn > 0xffffffffull || nq > 0xffffffffull || ni > 0xffffffffull) return InvalidArgument;
+  std::vector<RTAabb> hn(nn);
+  std::vector<RTMbvhNode> hq(nq);
+  std::vector<uint32_t> hi(ni);
+  std::memcpy(hn.data(), np, nn * 32);
+  std::memcpy(hq.data(), qp, nq * 128);
+  std::memcpy(hi.data(), ip, ni * 4);
+  if (!nodes_valid(hn.data(), nn, ni) || !indices_valid(hi.data(), ni)) return InvalidArgument;
+  auto e = std::make_unique<Entry>();
+  e->alive = true;
+  e->prim_count = (uint32_t)ni;
+  e->bvh_node_count = (uint32_t)nn;
+  ResultCode rc = upload_entry(*e, hn.data(), nn, hi.data(), ni, s);
+  // the quad nodes must be the collapse of the BVH2 nodes (Mbvh::construct):
+  // collapse again on the device and compare bit for bit
+  if (rc == Ok) rc = build_mbvh(e->d_nodes, e->bvh_node_count, s, &e->d_mnodes, &e->node_count);
+  if (rc == Ok) {
+    std::vector<DMNode> check;
+    if ((rc = fetch_device(check, e->d_mnodes, e->node_count)) == Ok &&
+        (check.size() != nq || std::memcmp(check.data(), hq.data(), nq * 128) != 0))
+      rc = InvalidArgument;
+  }
+  if (rc == Ok) rc = build_wide(e->d_nodes, e->bvh_node_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount);
+  if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_mbvh(*e, s);
+  if (rc != Ok) {
+    e->release();
+    return rc;
+  }
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* raw = e.get();
+  uint32_t id = store(std::move(e), true);
+  *result = mbvh_handle(id, *raw);
+  return Ok;
+}
