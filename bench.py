@@ -627,6 +627,14 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+ONLY_WORKLOADS = {
+    "sphere_6400_binned_sah": lambda: workload_sphere_sah(False),
+    "differentiable_200k": lambda: workload_differentiable(),
+    "batched_512_meshes": lambda: workload_batched(),
+    "clustered_10M_binned_sah": lambda: workload_clustered(False),
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -639,10 +647,19 @@ def main():
     ap.add_argument("--tris", type=int, default=0, help="profiling only: fewer triangles")
     ap.add_argument("--exact-nodes", action="store_true",
                     help="profiling only: time the closest hit over the exact 128-byte quad nodes")
+    ap.add_argument("--only", default="", choices=["", *ONLY_WORKLOADS],
+                    help="profiling only: run one secondary workload and print its JSON")
     args = ap.parse_args()
     apply_size_overrides(args)
     if args.warmup < 3:
         args.warmup = 3
+    if args.only:
+        import torch
+        from rtbvh_gb300 import build as libbuild
+        torch.cuda.set_device(0)
+        libbuild.build()
+        print(json.dumps({args.only: ONLY_WORKLOADS[args.only]()}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

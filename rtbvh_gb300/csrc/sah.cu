@@ -399,15 +399,19 @@ __device__ __forceinline__ uint32_t find_task(const uint32_t* chunk_base, uint32
   return lo;
 }
 
-// Shared memory of one block, reused by the phases of a level.
+// Shared memory of one block, reused by the phases of a level. The fields
+// are ordered by the phases that need them, so a launch of a single phase
+// allocates only the prefix it uses (kShSmall, kShBins, all).
 struct alignas(16) SahShared {
-  uint32_t bins[kLargeBlock / 32][kTaskBinWords];  // per-warp bins
-  uint32_t idx[kLargeBlock / 32][kWarpMax];        // per-warp partition buffer
-  Decision dec[kLargeBlock / 32];
   uint64_t scan[kLargeBlock / 32];
   uint32_t warp[32];
   uint32_t chunk, fail, prefix, pad;
+  uint32_t bins[kLargeBlock / 32][kTaskBinWords];  // per-warp bins
+  Decision dec[kLargeBlock / 32];
+  uint32_t idx[kLargeBlock / 32][kWarpMax];        // per-warp partition buffer
 };
+constexpr size_t kShSmall = offsetof(SahShared, bins);  // scans, partition scalars
+constexpr size_t kShBins = offsetof(SahShared, dec);    // + per-warp bins
 
 // Bins primitives sidx-ordered positions [i0, i1) into `wb` (one warp's or
 // block's shared bins). Neighbours in the index array are usually neighbours
@@ -1150,22 +1154,29 @@ __global__ void __launch_bounds__(kLargeBlock, 2) k_sah_build(SahParams p) {
   }
 }
 
+// Dynamic shared memory of a per-phase launch, sized to the prefix of
+// SahShared that the phase uses.
+__device__ __forceinline__ SahShared& dyn_shared() {
+  extern __shared__ __align__(16) unsigned char sah_dyn[];
+  return *reinterpret_cast<SahShared*>(sah_dyn);
+}
+
 // ---- the same phases as separate launches (large builds): the level number
 // selects the task lists, counters are read at kernel start.
 __global__ void __launch_bounds__(kLargeBlock) k_ph_prep(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   if (blockIdx.x == 0) large_prep(p, lv, sh);
   large_bins_init(p, lv);
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_bin(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   const uint32_t chunks = __ldcg(&p.cnt->chunks);
   for (uint32_t c = blockIdx.x; c < chunks; c += gridDim.x) large_bin_chunk(p, lv, c, sh);
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_decide(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   const uint32_t gwarp = (blockIdx.x * kLargeBlock + threadIdx.x) >> 5, nwarps = gridDim.x * (kLargeBlock / 32);
   for (uint32_t t = gwarp; t < lv.L; t += nwarps) large_decide(p, lv, t, sh);
@@ -1174,16 +1185,16 @@ __global__ void __launch_bounds__(kLargeBlock) k_ph_small(SahParams p, uint32_t 
   small_thread_phase(p, read_level(p, level));
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_partition(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   large_partition_phase(p, lv, __ldcg(&p.cnt->chunks), sh);
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_small_warps(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   small_warp_phase(p, read_level(p, level), sh);
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_copyback_scan(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   if (lv.L > 0) {
     const uint32_t chunks = __ldcg(&p.cnt->chunks);
@@ -1194,12 +1205,12 @@ __global__ void __launch_bounds__(kLargeBlock) k_ph_copyback_scan(SahParams p, u
   scan_segment(p, lv, sh);
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_emit(SahParams p, uint32_t level) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   emit_segment(p, read_level(p, level), sh, false);
 }
 // Counters of the next level (after every block of k_ph_emit read them).
 __global__ void k_ph_advance(SahParams p, uint32_t level, uint32_t blocks) {
-  __shared__ SahShared sh;
+  SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   uint64_t all = 0;
   for (uint32_t b = threadIdx.x; b < blocks; b += kLargeBlock) all += __ldcg(p.scan_sums + b);
@@ -1268,7 +1279,7 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   int per_sm = 0;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop ? (const void*)k_sah_build
                                                                          : (const void*)k_ph_small_warps,
-                                                         kLargeBlock, 0)))
+                                                         kLargeBlock, coop ? 0 : sizeof(SahShared))))
     return fail(cuda_rc(e));
   if (per_sm < 1) return fail(DeviceError);
   uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
@@ -1340,16 +1351,17 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
     for (uint32_t level = 0; h.large + h.small > 0; ++level) {
       if (level > kMaxDepth + 1) return fail(Error);
       if (h.large) {
-        k_ph_prep<<<blocks(((size_t)h.large * 3 * kBins + kLargeBlock - 1) / kLargeBlock), kLargeBlock, 0, s>>>(p, level);
-        k_ph_bin<<<grid, kLargeBlock, 0, s>>>(p, level);
-        k_ph_decide<<<blocks((h.large + 7) / 8), kLargeBlock, 0, s>>>(p, level);
+        k_ph_prep<<<blocks(((size_t)h.large * 3 * kBins + kLargeBlock - 1) / kLargeBlock), kLargeBlock, kShSmall,
+                    s>>>(p, level);
+        k_ph_bin<<<grid, kLargeBlock, kShBins, s>>>(p, level);
+        k_ph_decide<<<blocks((h.large + 7) / 8), kLargeBlock, kShBins, s>>>(p, level);
       }
       if (h.small) k_ph_small<<<(h.small + kLargeBlock - 1) / kLargeBlock, kLargeBlock, 0, s>>>(p, level);
-      if (h.large) k_ph_partition<<<grid, kLargeBlock, 0, s>>>(p, level);
-      if (h.small) k_ph_small_warps<<<grid, kLargeBlock, 0, s>>>(p, level);
-      k_ph_copyback_scan<<<grid, kLargeBlock, 0, s>>>(p, level);
-      k_ph_emit<<<grid, kLargeBlock, 0, s>>>(p, level);
-      k_ph_advance<<<1, kLargeBlock, 0, s>>>(p, level, grid);
+      if (h.large) k_ph_partition<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
+      if (h.small) k_ph_small_warps<<<grid, kLargeBlock, sizeof(SahShared), s>>>(p, level);
+      k_ph_copyback_scan<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
+      k_ph_emit<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
+      k_ph_advance<<<1, kLargeBlock, kShSmall, s>>>(p, level, grid);
       if ((e = cudaGetLastError())) return fail(cuda_rc(e));
       if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
           (e = cudaStreamSynchronize(s)))
