@@ -88,3 +88,28 @@ def test_sah_trace_matches_oracle(name):
 
 def test_sah_1m_canonical():
     check_tree(scenes.incoherent(1_000_000, seed=21), full=False)
+
+
+def _leaf_sets(mnodes, idx):
+    """(leaf offset, count, sorted primitive ids) of every leaf slot of a
+    quad-node array, as one sortable key array."""
+    mi = np.ascontiguousarray(mnodes).view(np.int32)
+    ch, cnt = mi[:, 24:28].ravel(), mi[:, 28:32].ravel()
+    leaf = cnt >= 0
+    off, c = ch[leaf].astype(np.int64), cnt[leaf].astype(np.int64)
+    rid = np.repeat(np.arange(len(off)), c)
+    pos = np.repeat(off, c) + (np.arange(c.sum()) - np.repeat(np.cumsum(c) - c, c))
+    prims = idx[pos].astype(np.int64)
+    order = np.lexsort((prims, rid))
+    return off, c, prims[order]
+
+
+def test_sah_above_the_cooperative_limit():
+    # builds above 2^20 primitives launch the phases of each level separately
+    tris = scenes.clustered(1_100_000, n_spheres=24, seed=23)
+    assert len(tris) > (1 << 20)
+    g, m, on, oi = check_tree(tris, full=False)
+    om = oracle.mbvh(on)
+    go, gc, gp = _leaf_sets(m.quad_nodes(), g.indices())
+    oo, oc, op = _leaf_sets(om, oi)
+    assert np.array_equal(go, oo) and np.array_equal(gc, oc) and np.array_equal(gp, op)
