@@ -787,6 +787,19 @@ ResultCode rtbvh_gpu_bvh_candidates(RTBvh bvh, const float* rays, const float* t
                            static_cast<cudaStream_t>(stream));
 }
 
+// Chunk schedule of the host-buffer trace: a small first chunk so that the
+// GPU starts after a short upload, large middle chunks (few launch tails),
+// and a small last chunk so that the final download is short (1M, 3M, then
+// 6M rays, the remainder split to end with 1M).
+static size_t next_chunk(size_t done, size_t remaining) {
+  const size_t M = (size_t)1 << 20;
+  if (remaining <= 2 * M) return remaining;
+  if (done == 0) return M;
+  if (done == M) return remaining > 4 * M ? 3 * M : remaining - M;
+  if (remaining > 7 * M) return 6 * M;
+  return remaining - M;
+}
+
 ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
                                       float* hits, uint32_t flags) {
   if (ray_count == 0) return Ok;
@@ -797,8 +810,12 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
     cudaStreamCreateWithFlags(&streams[0], cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&streams[1], cudaStreamNonBlocking);
   });
-  const size_t chunk = (size_t)1 << 21;
-  const size_t per = ray_count < chunk ? ray_count : chunk;
+  size_t per = 0;
+  for (size_t done = 0; done < ray_count;) {
+    const size_t c = next_chunk(done, ray_count - done);
+    per = c > per ? c : per;
+    done += c;
+  }
   Scratch<float> d_rays[2], d_tmax[2];
   Scratch<float4> d_hits[2];
   cudaError_t e;
@@ -807,8 +824,9 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
     if (t_max && (e = d_tmax[k].alloc(per, streams[k]))) return cuda_rc(e);
   }
   ResultCode rc = Ok;
-  for (size_t c0 = 0, k = 0; c0 < ray_count; c0 += per, k ^= 1) {
-    const size_t cnt = (ray_count - c0) < per ? (ray_count - c0) : per;
+  int k = 0;
+  for (size_t c0 = 0; c0 < ray_count; k ^= 1) {
+    const size_t cnt = next_chunk(c0, ray_count - c0);
     cudaStream_t s = streams[k];
     if ((e = cudaMemcpyAsync(d_rays[k].ptr, rays + 6 * c0, 24 * cnt, cudaMemcpyHostToDevice, s))) return cuda_rc(e);
     if (t_max && (e = cudaMemcpyAsync(d_tmax[k].ptr, t_max + c0, 4 * cnt, cudaMemcpyHostToDevice, s)))
@@ -817,6 +835,7 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
                       reinterpret_cast<float*>(d_hits[k].ptr), flags & ~RTBVH_TRACE_STATS, nullptr, s);
     if (rc != Ok) break;
     if ((e = cudaMemcpyAsync(hits + 4 * c0, d_hits[k].ptr, 16 * cnt, cudaMemcpyDeviceToHost, s))) return cuda_rc(e);
+    c0 += cnt;
   }
   if ((e = cudaStreamSynchronize(streams[0])) || (e = cudaStreamSynchronize(streams[1]))) return cuda_rc(e);
   return rc;

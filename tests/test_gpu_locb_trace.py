@@ -109,10 +109,11 @@ def test_trace_bvh2_bit_exact(name):
     assert np.array_equal(st, ost)
 
 
-def test_host_buffer_entry_matches_device_entry():
+@pytest.mark.parametrize("count", [3_000_000, 12_500_000])
+def test_host_buffer_entry_matches_device_entry(count):
     tris = scene("incoherent_20k")
     m = rb.Mbvh.construct(gpu_build(tris, "locb"))
-    rays, tmax = scenes.incoherent_rays(3_000_000, seed=9)  # more than one internal chunk
+    rays, tmax = scenes.incoherent_rays(count, seed=9)  # 2 and 5 internal chunks
     dev, _ = m.intersect(to_cuda(rays))
     host = m.intersect_host(rays)
     assert np.array_equal(u32(host), u32(dev.cpu().numpy()))
