@@ -150,6 +150,18 @@ def t_error_vs_fp64(tris, rays, hits, sample=1 << 20):
             "median_rel": float(f"{np.median(rel):.3g}")}
 
 
+def replica_value(total_ms, rays_per_step, steps, world_size, dist=None, device="cpu"):
+    """Replicas (no exchange between ranks): every rank traces its own copy
+    of the workload. Returns (whole-job Mrays/s = all ranks' rays / the
+    slowest rank's timed total, that total in ms)."""
+    if dist is not None:
+        import torch
+        t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t)
+    return world_size * rays_per_step * steps / (total_ms * 1e-3) / 1e6, total_ms
+
+
 def run_gpu(args):
     import torch
 
@@ -219,13 +231,9 @@ def run_gpu(args):
             times.append(e0.elapsed_time(e1))
         torch.cuda.synchronize()
     ms = statistics.mean(times)
-    total_ms = sum(times)
+    value, total_ms = replica_value(sum(times), N_RAYS, args.steps, ws, dist, "cuda")
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t)
         dist.barrier()
-    value = ws * N_RAYS * args.steps / (total_ms * 1e-3) / 1e6
 
     # any-hit on the same structure (tmax = 0.5 x distance)
     for _ in range(2):
@@ -602,7 +610,7 @@ def run_reference(args):
     nodes, idx = oracle.build(a, c, "locb", threads=threads)
     m = oracle.mbvh(nodes)
     flat = tris.reshape(-1, 9)
-    sample = 500_000
+    sample = min(500_000, N_RAYS // 2)
     times = []
     for s in range(args.warmup + args.steps):
         lo = (s * sample) % (N_RAYS - sample)
