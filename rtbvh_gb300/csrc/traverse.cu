@@ -459,6 +459,12 @@ __device__ __forceinline__ bool slab_far(const DAabb& b, const RayState& r, floa
   return false;
 }
 
+// BvhIndexIterator::next (src/iter_indices.rs:66-107) for one ray: a step
+// is one pop; a leaf's primitives are tested, an interior node's two
+// children are tested with the far-t slab test (which never culls by t) and
+// pushed in sort_nodes order. Stack entries hold the node's (left_first,
+// count), read when its parent loaded both children (two 256-bit loads of
+// the adjacent pair), so a pop needs no node load.
 template <bool ANY_HIT, bool STATS>
 __device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
   RayState ray = load_ray(a.rays, r, a.t_max);
@@ -467,52 +473,64 @@ __device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
   uint32_t visits = 0, tests = 0, max_depth = 0;
   const bool nan = (ray.ox != ray.ox) || (ray.oy != ray.oy) || (ray.oz != ray.oz) || (ray.dx != ray.dx) ||
                    (ray.dy != ray.dy) || (ray.dz != ray.dz);
-  int32_t stack[kStack];
-  int sp = (a.node_count == 0 || nan) ? -1 : 0;
-  stack[0] = 0;
+  int2 stack[kStack];
+  int sp = -1;
+  if (a.node_count > 0 && !nan) {
+    const DAabb root = load_aabb(a.nodes);
+    stack[0] = make_int2(root.left_first, root.count);
+    sp = 0;
+  }
   while (sp >= 0) {
-    const int32_t ni = stack[sp--];
-    if ((uint32_t)ni >= a.node_count) {
-      atomicOr(a.status, kStatusBadIndex);
-      break;
-    }
-    const DAabb node = load_aabb(a.nodes + ni);
-    if (node.count > -1) {
-      if (node.left_first < 0 || (uint32_t)node.left_first + (uint32_t)node.count > a.prim_count) {
+    const int2 e = stack[sp--];
+    const int32_t lf = e.x, count = e.y;
+    if (count > -1) {
+      if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
         atomicOr(a.status, kStatusBadIndex);
         break;
       }
       bool stop = false;
-      for (int32_t j = 0; j < node.count; ++j) {
+      for (int32_t j = 0; j < count; ++j) {
         if (STATS) ++tests;
-        if (mt_test(a.tris + kTriFloat4 * (size_t)(node.left_first + j), ray, hu, hv, prim) && ANY_HIT) {
+        if (mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim) && ANY_HIT) {
           stop = true;
           break;
         }
       }
       if (stop) break;
-    } else if (node.left_first > -1) {
+    } else if (lf > -1) {
       if (STATS) ++visits;
-      const int32_t lf = node.left_first;
       if ((uint32_t)lf + 1u >= a.node_count) {
         atomicOr(a.status, kStatusBadIndex);
         break;
       }
+      float l8[8], r8[8];
+      ld8(reinterpret_cast<const float*>(a.nodes + lf), l8);
+      ld8(reinterpret_cast<const float*>(a.nodes + lf + 1), r8);
+      DAabb lb, rb;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        lb.min[k] = l8[k];
+        lb.max[k] = l8[4 + k];
+        rb.min[k] = r8[k];
+        rb.max[k] = r8[4 + k];
+      }
+      const int2 le = make_int2(__float_as_int(l8[7]), __float_as_int(l8[3]));
+      const int2 re = make_int2(__float_as_int(r8[7]), __float_as_int(r8[3]));
       float lt = 0.0f, rt = 0.0f;
-      const bool lh = slab_far(load_aabb(a.nodes + lf), ray, lt);
-      const bool rh = slab_far(load_aabb(a.nodes + lf + 1), ray, rt);
+      const bool lh = slab_far(lb, ray, lt);
+      const bool rh = slab_far(rb, ray, rt);
       if (sp + 2 >= kStack) {
         atomicOr(a.status, kStatusStackOverflow);
         prim = -2;
         break;
       }
       if (lh && rh) {
-        if (lt < rt) { stack[++sp] = lf; stack[++sp] = lf + 1; }
-        else { stack[++sp] = lf + 1; stack[++sp] = lf; }
+        if (lt < rt) { stack[++sp] = le; stack[++sp] = re; }
+        else { stack[++sp] = re; stack[++sp] = le; }
       } else if (lh) {
-        stack[++sp] = lf;
+        stack[++sp] = le;
       } else if (rh) {
-        stack[++sp] = lf + 1;
+        stack[++sp] = re;
       }
       if (STATS && (uint32_t)(sp + 1) > max_depth) max_depth = (uint32_t)(sp + 1);
     }
@@ -525,6 +543,8 @@ __device__ __forceinline__ void trace_one_bvh(const TraceArgs& a, size_t r) {
   }
 }
 
+// Warps take 32 consecutive rays at a time (adjacent camera rays walk the
+// same nodes in step).
 template <bool ANY_HIT, bool STATS>
 __global__ void __launch_bounds__(kBlock) k_trace_bvh(TraceArgs a, unsigned int* work) {
   const int lane = threadIdx.x & 31;
