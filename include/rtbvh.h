@@ -104,8 +104,20 @@ typedef bool (*RTIntersectFn)(uint32_t, float *, void *);
 
 /* ------------------------------------------------------------------ part 1 */
 
-/* rtbvh_ffi/src/lib.rs:345-389. The spatial-split builder is not part of this
- * library: always returns Error and leaves *result untouched. */
+/* rtbvh_ffi/src/lib.rs:345-389: Builder::construct_spatial_sah
+ * (src/bvh.rs:59-85, src/builders/spatial_sah.rs) over RTTriangleWrapper
+ * primitives, built on the GPU from host inputs. Vertex k of triangle i is
+ * read at float offset (i * triangle_stride / 4) + k * (vertex_stride / 4),
+ * its centre at i * stride / 4; aabbs NULL -> Primitive::aabb of the
+ * wrapper, which reads the vertices at (vertex0 offset * (vertex_stride / 4))
+ * / 4 (the triangle's own vertices when vertex_stride is 16): where that
+ * would read past the triangles' vertices this library returns
+ * InvalidArgument. The result is the reference's as written (no
+ * RTBVH_SPATIAL_FIX_* bits): its index vector has max_reference_count =
+ * n + (n as f32 * 0.75) as usize entries, and on many inputs some
+ * primitives are not referenced by any leaf (see rtbvh_gpu_create_spatial_bvh
+ * for corrected builds). centers/vertices/result NULL or stride % 4 != 0 ->
+ * Error; an input on which the reference panics -> Error. */
 ResultCode create_spatial_Bvh(const RTAabb *aabbs, uintptr_t prim_count, const float *centers, uintptr_t stride,
                               const float *vertices, uintptr_t vertex_stride, uintptr_t triangle_stride,
                               uint32_t prims_per_leaf, RTBvh *result);
@@ -188,6 +200,30 @@ ResultCode rtbvh_gpu_create_bvh_from_triangles(const float *vertices, uintptr_t 
 ResultCode rtbvh_gpu_create_bvh(const RTAabb *aabbs, uintptr_t prim_count, const float *centers,
                                 uintptr_t center_stride, uintptr_t prims_per_leaf, BvhType bvh_type, uint32_t flags,
                                 rtbvh_stream_t stream, RTBvh *result);
+
+/* Corrections of the reference's spatial-split builder
+ * (src/builders/spatial_sah.rs), for rtbvh_gpu_create_spatial_bvh. 0 builds
+ * the reference as written. */
+#define RTBVH_SPATIAL_FIX_CLIP 1u        /* split_edge returns a + t*(b-a), not a*t*(b-a) (:90-93) */
+#define RTBVH_SPATIAL_FIX_EXIT_BIN 2u    /* a reference leaves its last bin, not its first (:545-546) */
+#define RTBVH_SPATIAL_FIX_SWEEP_BOX 4u   /* the sweep's left box is the union of bins 0..i, not of
+                                            their suffix unions (:549-570) */
+#define RTBVH_SPATIAL_FIX_SPLIT_SPACE 8u /* allocate_children gives the freed split space to the left
+                                            child and keeps the right child on its moved references
+                                            (:375-424); without it references are lost */
+#define RTBVH_SPATIAL_FIX_FALLBACK 16u   /* the equal-count fallback counts from the task's begin
+                                            (:643-648) */
+#define RTBVH_SPATIAL_FIX_ALL 31u
+
+/* Builder::construct_spatial_sah (src/bvh.rs:59-85) on device triangles
+ * (n x 9 floats, kept with the structure for traversal). aabbs NULL ->
+ * Triangle::aabb, centers NULL -> Triangle::center (shared/src/lib.rs:27-39);
+ * center_stride 12 or 16 bytes. fixes: RTBVH_SPATIAL_FIX_* bits. The index
+ * vector has max_reference_count entries (RTBvh::index_count); a triangle
+ * split by the builder has several. Error where the reference panics. */
+ResultCode rtbvh_gpu_create_spatial_bvh(const float *vertices, uintptr_t prim_count, const RTAabb *aabbs,
+                                        const float *centers, uintptr_t center_stride, uintptr_t prims_per_leaf,
+                                        uint32_t fixes, uint32_t flags, rtbvh_stream_t stream, RTBvh *result);
 
 /* Mbvh::construct (src/bvh.rs:381-404) on the GPU. */
 ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t stream, RTMbvh *result);

@@ -37,6 +37,11 @@ def lib():
         L.ror_build.argtypes = [f32p, f32p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int32,
                                 ctypes.c_size_t, ctypes.c_uint32, f32p, u32p]
         L.ror_build.restype = ctypes.c_int64
+        L.ror_spatial_max_refs.argtypes = [ctypes.c_size_t]
+        L.ror_spatial_max_refs.restype = ctypes.c_uint64
+        L.ror_build_spatial.argtypes = [f32p, f32p, f32p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32,
+                                        f32p, ctypes.c_size_t, u32p, ctypes.c_size_t]
+        L.ror_build_spatial.restype = ctypes.c_int64
         L.ror_mbvh.argtypes = [f32p, ctypes.c_size_t, f32p]
         L.ror_mbvh.restype = ctypes.c_int64
         L.ror_refit.argtypes = [f32p, ctypes.c_size_t, u32p, f32p, ctypes.c_size_t]
@@ -127,6 +132,45 @@ def build(aabbs, centers, build_type: str, prims_per_leaf: int = 1, spawn_thresh
     idx = np.zeros(n, np.uint32)
     bt = {"locb": 0, "sah": 1}[build_type]
     m = lib().ror_build(_f(a), _f(c), n, prims_per_leaf, bt, spawn_threshold, threads, _f(nodes), _u(idx))
+    if m < 0:
+        raise OracleError(f"build failed ({m})")
+    return nodes[:m].copy(), idx
+
+
+# Corrections of the reference's spatial-split builder (bit flags, 0 = as
+# written); rtbvh_oracle.cpp SpatialFix says what each one changes.
+SPATIAL_FIX_CLIP = 1
+SPATIAL_FIX_EXIT_BIN = 2
+SPATIAL_FIX_SWEEP_BOX = 4
+SPATIAL_FIX_SPLIT_SPACE = 8
+SPATIAL_FIX_FALLBACK = 16
+SPATIAL_FIX_ALL = 31
+
+
+def spatial_max_refs(n: int) -> int:
+    return int(lib().ror_spatial_max_refs(n))
+
+
+def build_spatial(tris, aabbs=None, centers=None, prims_per_leaf: int = 1, fixes: int = 0):
+    """Spatial-split SAH build (src/builders/spatial_sah.rs). Returns (nodes
+    (m,8) float32, prim_indices (max_refs,) uint32, the reference's full
+    index vector). Raises OracleError where the reference panics."""
+    t = _c(tris, np.float32).reshape(-1, 9)
+    n = len(t)
+    if n == 0:
+        raise OracleError("NoPrimitives")
+    if aabbs is None or centers is None:
+        pa, pc = triangle_prep(t)
+        aabbs = pa if aabbs is None else aabbs
+        centers = pc if centers is None else centers
+    a = _c(aabbs, np.float32).reshape(-1, 8)
+    c = _c(centers, np.float32).reshape(-1, 3)
+    mr = spatial_max_refs(n)
+    nodes = np.zeros((2 * mr + 1, 8), np.float32)
+    idx = np.zeros(mr, np.uint32)
+    m = lib().ror_build_spatial(_f(a), _f(c), _f(t), n, prims_per_leaf, fixes, _f(nodes), len(nodes), _u(idx), len(idx))
+    if m == -3:
+        raise OracleError("the reference panics on this input")
     if m < 0:
         raise OracleError(f"build failed ({m})")
     return nodes[:m].copy(), idx

@@ -35,6 +35,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1072,6 +1073,401 @@ bool trace_bvh_packet(const BvhNode* nodes, size_t ncount, const uint32_t* idx, 
   return true;
 }
 
+// ---------------------------------------------------------------- spatial SAH
+// src/builders/spatial_sah.rs, sequential. Tasks run depth first, the child
+// with more references first (ties: the left one): the order of
+// TaskSpawner::run_task (src/utils.rs:246-283) while no task is handed to
+// another thread. The reference hands tasks of more than 1024 references to
+// new threads, after which its node numbering and leaf placement depend on
+// thread timing; this order is the schedule in which each spawned thread
+// runs to completion first.
+//
+// `fixes` selects corrections of reference defects (0 = the reference as
+// written): see SpatialFix.
+
+// spatial_sah.rs:64-78
+struct SRef {
+  Aabb aabb;
+  V3 center;
+  uint32_t prim;
+};
+
+enum SpatialFix : uint32_t {
+  kFixClip = 1,        // split_edge returns a + t*(b-a), not a*t*(b-a) (:90-93)
+  kFixExitBin = 2,     // a reference leaves at its last bin, not its first (:545-546)
+  kFixSweepBox = 4,    // the sweep's left box is the union of bins 0..i, not of their suffix unions (:549-570)
+  kFixSplitSpace = 8,  // allocate_children hands the freed split space to the left child and keeps the right
+                       // child on its moved references (:375-424)
+  kFixFallback = 16,   // the equal-count fallback starts at the task's begin (:643-648)
+};
+
+// src/aabb.rs:288-298
+inline void aabb_shrink(Aabb& a, const Aabb& b) {
+  for (int i = 0; i < 3; ++i) { a.min[i] = rs_max(a.min[i], b.min[i]); a.max[i] = rs_min(a.max[i], b.max[i]); }
+}
+// src/aabb.rs:334-340
+inline float aabb_area(const Aabb& a) {
+  float ex = a.max[0] - a.min[0], ey = a.max[1] - a.min[1], ez = a.max[2] - a.min[2];
+  float v = ((ex * ey) + (ex * ez)) + (ey * ez);
+  return rs_max(0.0f, v);
+}
+// src/aabb.rs:329-332
+inline V3 aabb_center(const Aabb& a) {
+  return v3((a.min[0] + a.max[0]) * 0.5f, (a.min[1] + a.max[1]) * 0.5f, (a.min[2] + a.max[2]) * 0.5f);
+}
+
+// SpatialTriangle::split, spatial_sah.rs:85-129. tri = v0, v1, v2.
+void tri_split(const float* tri, int axis, float position, bool fix_clip, Aabb& left, Aabb& right) {
+  const V3 p[3] = {v3(tri[0], tri[1], tri[2]), v3(tri[3], tri[4], tri[5]), v3(tri[6], tri[7], tri[8])};
+  left = aabb_new();
+  right = aabb_new();
+  auto split_edge = [&](V3 a, V3 b) -> V3 {
+    float t = (position - a[axis]) / (b[axis] - a[axis]);
+    V3 d = sub(b, a);
+    if (fix_clip) return v3(a.x + t * d.x, a.y + t * d.y, a.z + t * d.z);
+    return v3((a.x * t) * d.x, (a.y * t) * d.y, (a.z * t) * d.z);
+  };
+  const bool q0 = p[0][axis] <= position, q1 = p[1][axis] <= position, q2 = p[2][axis] <= position;
+  aabb_grow(q0 ? left : right, p[0]);
+  aabb_grow(q1 ? left : right, p[1]);
+  aabb_grow(q2 ? left : right, p[2]);
+  if (q0 != q1) { V3 m = split_edge(p[0], p[1]); aabb_grow(left, m); aabb_grow(right, m); }
+  if (q1 != q2) { V3 m = split_edge(p[1], p[2]); aabb_grow(left, m); aabb_grow(right, m); }
+  if (q2 != q0) { V3 m = split_edge(p[2], p[0]); aabb_grow(left, m); aabb_grow(right, m); }
+}
+
+struct SWork {  // WorkItem, spatial_sah.rs:247-277
+  size_t node, begin, end, split_end, depth;
+  bool sorted;
+};
+struct ObjSplit {  // spatial_sah.rs:25-44
+  float cost;
+  int64_t index;  // -1: None
+  int axis;
+  Aabb left, right;
+};
+struct SpSplit {  // spatial_sah.rs:46-61
+  float cost, position;
+  int axis;
+};
+
+// Builder defaults, spatial_sah.rs:865-881 (max_leaf_size from primitives_per_leaf).
+constexpr int kSbBins = 16, kSbPasses = 2;
+constexpr size_t kSbMaxDepth = 64;
+constexpr float kSbTraversalCost = 1.0f, kSbAlpha = 1e-5f, kSbSplitFactor = 0.75f;
+
+struct SpatialBuild {
+  const float* tris = nullptr;  // n x 9
+  size_t n = 0, max_ref = 0, max_leaf = 1;
+  uint32_t fixes = 0;
+  float threshold = 0.0f;
+  std::vector<BvhNode> nodes;
+  size_t node_count = 1;
+  std::vector<uint32_t> prim_indices;
+  size_t ref_counter = 0;
+  std::vector<Aabb> acc;
+  std::vector<SRef> refs[3];
+  std::vector<uint8_t> marks;
+  int err = 0;  // 1: the reference panics or writes out of bounds here
+  const float* tri(uint32_t p) const { return tris + 9 * (size_t)p; }
+};
+
+// spatial_sah.rs:314-368
+ObjSplit sb_find_object_split(SpatialBuild& b, size_t begin, size_t end, bool sorted) {
+  if (!sorted) {
+    // sort_by with a comparator that answers Less exactly when a < b: the
+    // standard library's stable sort only asks "is less", so this is a stable
+    // sort on the centre coordinate.
+    for (int axis = 0; axis < 3; ++axis)
+      std::stable_sort(b.refs[axis].begin() + begin, b.refs[axis].begin() + end,
+                       [axis](const SRef& x, const SRef& y) { return x.center[axis] < y.center[axis]; });
+  }
+  ObjSplit best{FLT_MAX, -1, 0, aabb_new(), aabb_new()};
+  for (int axis = 0; axis < 3; ++axis) {
+    const std::vector<SRef>& r = b.refs[axis];
+    Aabb a = aabb_new();
+    for (size_t i = end - 1; i > begin; --i) {
+      aabb_grow_bb(a, r[i].aabb);
+      b.acc[i] = a;
+    }
+    a = aabb_new();
+    for (size_t i = begin; i + 1 < end; ++i) {
+      aabb_grow_bb(a, r[i].aabb);
+      float cost = aabb_half_area(a) * (float)(i + 1 - begin) + aabb_half_area(b.acc[i + 1]) * (float)(end - (i + 1));
+      if (cost < best.cost) best = ObjSplit{cost, (int64_t)(i + 1), axis, a, b.acc[i + 1]};
+    }
+  }
+  return best;
+}
+
+// spatial_sah.rs:491-583. Returns false for None; sets b.err where the
+// reference would panic.
+bool sb_binning_pass(SpatialBuild& b, SpSplit& split, int axis, size_t begin, size_t end, float mn, float mx,
+                     float& next_lo, float& next_hi) {
+  struct Bin {
+    Aabb aabb;
+    size_t entry, exit;
+  } bins[kSbBins];
+  for (auto& bin : bins) bin = Bin{aabb_new(), 0, 0};
+  const float bin_size = (mx - mn) / (float)kSbBins;
+  const float inv_size = 1.0f / bin_size;
+  const bool fix_clip = b.fixes & kFixClip;
+  for (size_t i = begin; i < end; ++i) {
+    const SRef& ref = b.refs[0][i];
+    size_t first = std::min((size_t)(kSbBins - 1), (size_t)rs_f32_to_usize(rs_max(inv_size * (ref.aabb.min[axis] - mn), 0.0f)));
+    size_t last = std::min((size_t)(kSbBins - 1), (size_t)rs_f32_to_usize(rs_max(inv_size * (ref.aabb.max[axis] - mn), 0.0f)));
+    if (!aabb_is_valid(ref.aabb)) break;
+    if (first > last) { b.err = 1; return false; }  // bins[first..last] panics
+    Aabb cur = ref.aabb;
+    for (size_t j = 0; j < last - first; ++j) {
+      Aabb lb, rb;
+      tri_split(b.tri(ref.prim), axis, mn + (float)(j + first + 1) * bin_size, fix_clip, lb, rb);
+      aabb_shrink(lb, cur);
+      aabb_grow_bb(bins[first + j].aabb, lb);
+      aabb_shrink(cur, rb);
+    }
+    aabb_grow_bb(bins[last].aabb, cur);
+    bins[first].entry += 1;
+    bins[(b.fixes & kFixExitBin) ? last : first].exit += 1;
+  }
+  Aabb suffix[kSbBins];
+  Aabb cur = aabb_new();
+  for (int i = kSbBins; i > 0; --i) {
+    aabb_grow_bb(cur, bins[i - 1].aabb);
+    suffix[i - 1] = cur;
+  }
+  size_t left_count = 0, right_count = end - begin;
+  cur = aabb_new();
+  bool found = false;
+  for (int i = 0; i < kSbBins - 1; ++i) {
+    left_count += bins[i].entry;
+    right_count -= bins[i].exit;
+    aabb_grow_bb(cur, (b.fixes & kFixSweepBox) ? bins[i].aabb : suffix[i]);
+    float cost = (float)left_count * aabb_half_area(cur) + (float)right_count * aabb_half_area(suffix[i + 1]);
+    if (cost < split.cost) {
+      split.cost = cost;
+      split.axis = axis;
+      split.position = mn + (float)(i + 1) * bin_size;
+      found = true;
+    }
+  }
+  if (!found) return false;
+  next_lo = split.position - bin_size;
+  next_hi = split.position + bin_size;
+  return true;
+}
+
+// spatial_sah.rs:585-603
+SpSplit sb_find_spatial_split(SpatialBuild& b, const SWork& w) {
+  const Aabb nb = b.nodes[w.node];
+  SpSplit split{FLT_MAX, 0.0f, 0};
+  for (int axis = 0; axis < 3 && !b.err; ++axis) {
+    float mn = nb.min[axis], mx = nb.max[axis];
+    for (int pass = 0; pass < kSbPasses; ++pass) {
+      float lo, hi;
+      if (!sb_binning_pass(b, split, axis, w.begin, w.end, mn, mx, lo, hi)) break;
+      mn = lo;
+      mx = hi;
+    }
+  }
+  return split;
+}
+
+// spatial_sah.rs:370-438
+bool sb_allocate_children(SpatialBuild& b, const SWork& w, size_t right_begin, size_t right_end, const Aabb& left_box,
+                          const Aabb& right_box, bool sorted, SWork& lw, SWork& rw) {
+  if (b.node_count + 1 >= b.nodes.size()) { b.err = 1; return false; }  // AtomicNodeStack::allocate -> None
+  const size_t left = b.node_count;
+  b.node_count += 2;
+  BvhNode& parent = b.nodes[w.node];
+  parent.extra2 = (int32_t)left;
+  parent.extra1 = -1;
+  aabb_offset_by(parent, 0.0001f);
+  b.nodes[left] = left_box;
+  b.nodes[left + 1] = right_box;
+
+  const size_t remaining = w.split_end - right_end;
+  const float left_cost = aabb_half_area(left_box) * (float)(right_begin - w.begin);
+  const float right_cost = aabb_half_area(right_box) * (float)(right_end - right_begin);
+  const size_t lsc = remaining == 0 ? 0 : (size_t)rs_f32_to_usize((float)remaining * (left_cost / (left_cost + right_cost)));
+  if (lsc > 0) {
+    if (right_end + lsc > b.max_ref) { b.err = 1; return false; }
+    for (int axis = 0; axis < 3; ++axis) {  // move_backward, src/utils.rs:59-72
+      SRef* r = b.refs[axis].data();
+      std::memmove(r + right_begin + lsc, r + right_begin, (right_end - right_begin) * sizeof(SRef));
+    }
+  }
+  const bool fix = b.fixes & kFixSplitSpace;
+  lw = SWork{left, w.begin, right_begin, fix ? right_begin + lsc : right_begin, w.depth + 1, sorted};
+  rw = fix ? SWork{left + 1, right_begin + lsc, right_end + lsc, w.split_end, w.depth + 1, sorted}
+           : SWork{left + 1, right_begin, right_end, w.split_end, w.depth + 1, sorted};
+  return true;
+}
+
+// spatial_sah.rs:440-489
+bool sb_apply_object_split(SpatialBuild& b, const SWork& w, const ObjSplit& split, SWork& lw, SWork& rw) {
+  const size_t s = (size_t)split.index;
+  if (split.index < (int64_t)w.begin || s >= w.end) { b.err = 1; return false; }  // assert!
+  std::vector<SRef>& r = b.refs[split.axis];
+  for (size_t i = w.begin; i < s; ++i) b.marks[r[i].prim] = 1;
+  for (size_t i = s; i < w.end; ++i) b.marks[r[i].prim] = 0;
+  // sort_by with "Less exactly when a is marked and b is not": a stable
+  // partition, marked references first.
+  for (int o = 1; o <= 2; ++o) {
+    std::vector<SRef>& q = b.refs[(split.axis + o) % 3];
+    std::stable_partition(q.begin() + w.begin, q.begin() + w.end, [&b](const SRef& x) { return b.marks[x.prim] != 0; });
+  }
+  for (int axis = 0; axis < 3; ++axis)  // the reference allocates fresh marks per call
+    for (size_t i = w.begin; i < w.end; ++i) b.marks[b.refs[axis][i].prim] = 0;
+  return sb_allocate_children(b, w, s, w.end, split.left, split.right, true, lw, rw);
+}
+
+// spatial_sah.rs:605-724
+bool sb_apply_spatial_split(SpatialBuild& b, const SWork& w, const SpSplit& split, SWork& lw, SWork& rw) {
+  const int ax = split.axis;
+  const float pos = split.position;
+  std::vector<SRef>& r = b.refs[ax];
+  size_t left_end = w.begin, right_begin = w.end, right_end = w.end;
+  Aabb left_box = aabb_new(), right_box = aabb_new();
+  size_t i = w.begin;
+  while (i < right_begin) {
+    const Aabb a = r[i].aabb;
+    if (a.max[ax] <= pos) {
+      aabb_grow_bb(left_box, a);
+      std::swap(r[i], r[left_end]);
+      i += 1;
+      left_end += 1;
+    } else if (a.min[ax] >= pos) {
+      aabb_grow_bb(right_box, a);
+      right_begin -= 1;
+      std::swap(r[i], r[right_begin]);
+    } else {
+      i += 1;
+    }
+  }
+  size_t left_count = left_end - w.begin, right_count = right_end - right_begin;
+  if ((left_count == 0 || right_count == 0) && left_end == right_begin) {
+    if (left_count > 0) left_end = (b.fixes & kFixFallback) ? w.begin + left_count / 2 : left_count / 2;
+    else left_end += right_count / 2;
+    right_begin = left_end;
+    if (left_end < w.begin || left_end > w.end) { b.err = 1; return false; }  // slice range panics
+    left_box = aabb_new();
+    right_box = aabb_new();
+    for (size_t k = w.begin; k < left_end; ++k) aabb_grow_bb(left_box, r[k].aabb);
+    for (size_t k = left_end; k < w.end; ++k) aabb_grow_bb(right_box, r[k].aabb);
+  }
+  const bool fix_clip = b.fixes & kFixClip;
+  while (left_end < right_begin) {
+    const SRef ref = r[left_end];
+    Aabb lp, rp;
+    tri_split(b.tri(ref.prim), ax, pos, fix_clip, lp, rp);
+    aabb_shrink(lp, ref.aabb);
+    aabb_shrink(rp, ref.aabb);
+    if (w.split_end - right_end > 0) {
+      aabb_grow_bb(left_box, lp);
+      aabb_grow_bb(right_box, rp);
+      r[right_end] = SRef{rp, aabb_center(rp), ref.prim};
+      r[left_end] = SRef{lp, aabb_center(lp), ref.prim};
+      right_end += 1;
+      left_end += 1;
+      left_count += 1;
+      right_count += 1;
+    } else if (left_count < right_count) {
+      aabb_grow_bb(left_box, ref.aabb);
+      left_end += 1;
+      left_count += 1;
+    } else {
+      aabb_grow_bb(right_box, ref.aabb);
+      right_begin -= 1;
+      std::swap(r[right_begin], r[left_end]);
+      right_count += 1;
+    }
+  }
+  for (int o = 1; o <= 2; ++o)
+    std::copy(r.begin() + w.begin, r.begin() + right_end, b.refs[(ax + o) % 3].begin() + w.begin);
+  return sb_allocate_children(b, w, right_begin, right_end, left_box, right_box, false, lw, rw);
+}
+
+// make_leaf, spatial_sah.rs:733-744
+void sb_make_leaf(SpatialBuild& b, const SWork& w) {
+  const size_t count = w.end - w.begin;
+  const size_t first = b.ref_counter;
+  b.ref_counter += count;
+  if (first + count > b.max_ref) { b.err = 1; return; }
+  for (size_t i = 0; i < count; ++i) b.prim_indices[first + i] = b.refs[0][w.begin + i].prim;
+  b.nodes[w.node].extra2 = (int32_t)first;
+  b.nodes[w.node].extra1 = (int32_t)count;
+}
+
+// Task::run, spatial_sah.rs:726-838. Returns true with two child tasks.
+bool sb_run(SpatialBuild& b, const SWork& w, SWork& lw, SWork& rw) {
+  const size_t work = w.end - w.begin;
+  if (work <= 1 || w.depth >= kSbMaxDepth) {
+    sb_make_leaf(b, w);
+    return false;
+  }
+  ObjSplit obj = sb_find_object_split(b, w.begin, w.end, w.sorted);
+  SpSplit sp{FLT_MAX, 0.0f, 0};
+  Aabb ov = obj.left;
+  aabb_shrink(ov, obj.right);
+  const float overlap = aabb_area(ov);
+  if (overlap > b.threshold && (w.split_end - w.end) > 0) sp = sb_find_spatial_split(b, w);
+  if (b.err) return false;
+  const float best = rs_min(sp.cost, obj.cost);
+  bool use_spatial = best < obj.cost;
+  const Aabb nb = b.nodes[w.node];
+  const float max_split_cost = aabb_half_area(nb) * ((float)work - kSbTraversalCost);
+  if (best >= max_split_cost) {
+    if (work > b.max_leaf) {
+      use_spatial = false;
+      obj.index = (int64_t)((w.begin + w.end) / 2);
+      obj.axis = aabb_longest_axis(nb);
+      obj.left = aabb_new();
+      obj.right = aabb_new();
+      for (size_t i = w.begin; i < (size_t)obj.index; ++i) aabb_grow_bb(obj.left, b.refs[obj.axis][i].aabb);
+      for (size_t i = (size_t)obj.index; i < w.end; ++i) aabb_grow_bb(obj.right, b.refs[obj.axis][i].aabb);
+    } else {
+      sb_make_leaf(b, w);
+      return false;
+    }
+  }
+  if (use_spatial) return sb_apply_spatial_split(b, w, sp, lw, rw);
+  if (obj.index >= 0) return sb_apply_object_split(b, w, obj, lw, rw);
+  sb_make_leaf(b, w);
+  return false;
+}
+
+// SpatialSahBuilder::build, spatial_sah.rs:926-1034. aabbs: n boxes (with
+// their extras), centers: Primitive::center of each triangle.
+void build_spatial(SpatialBuild& b, const Aabb* aabbs, const V3* centers) {
+  const size_t n = b.n;
+  b.max_ref = n + (size_t)rs_f32_to_usize((float)n * kSbSplitFactor);
+  b.nodes.assign(2 * b.max_ref + 1, node_new());
+  b.prim_indices.assign(b.max_ref, 0u);
+  b.acc.assign(b.max_ref, aabb_new());
+  b.marks.assign(b.max_ref, 0);
+  for (int axis = 0; axis < 3; ++axis) {
+    b.refs[axis].assign(b.max_ref, SRef{aabb_new(), v3(0.0f, 0.0f, 0.0f), 0u});
+    for (size_t i = 0; i < n; ++i) b.refs[axis][i] = SRef{aabbs[i], centers[i], (uint32_t)i};
+  }
+  const Aabb root = aabb_union_of_list(aabbs, n);
+  b.threshold = kSbAlpha * 2.0f * aabb_half_area(root);
+  b.node_count = 1;
+  b.nodes[0] = root;
+  std::vector<SWork> stack{SWork{0, 0, n, b.max_ref, 0, false}};
+  while (!stack.empty() && !b.err) {
+    SWork w = stack.back();
+    stack.pop_back();
+    SWork a, c;
+    if (sb_run(b, w, a, c)) {
+      if (a.end - a.begin < c.end - c.begin) std::swap(a, c);
+      stack.push_back(c);
+      stack.push_back(a);
+    }
+  }
+  b.nodes.resize(b.node_count);
+}
+
 void load_aabbs(const float* raw, size_t n, std::vector<Aabb>& out) {
   out.resize(n);
   if (n) std::memcpy(out.data(), raw, n * sizeof(Aabb));
@@ -1176,6 +1572,34 @@ int64_t ror_build(const float* aabbs, const float* centers, size_t n, size_t pri
   } else {
     b = build_binned_sah(a.data(), c.data(), n, prims_per_leaf, spawn_threshold == 0 ? SIZE_MAX : spawn_threshold);
   }
+  std::memcpy(nodes_out, b.nodes.data(), b.nodes.size() * sizeof(BvhNode));
+  std::memcpy(idx_out, b.prim_indices.data(), b.prim_indices.size() * 4);
+  return (int64_t)b.nodes.size();
+}
+
+// Spatial-split SAH (src/builders/spatial_sah.rs; see build_spatial for the
+// task order). tris: n x 9 vertices, aabbs: n x 8, centers: n x 3. nodes_out
+// holds nodes_cap nodes (2 * max_refs + 1 suffice), idx_out idx_cap entries
+// (max_refs: the reference returns all of them, unused ones 0). Returns the
+// node count, -2 no primitives, -3 an input on which the reference panics or
+// writes out of bounds, -4 output too small.
+uint64_t ror_spatial_max_refs(size_t n) { return n + rs_f32_to_usize((float)n * kSbSplitFactor); }
+
+int64_t ror_build_spatial(const float* aabbs, const float* centers, const float* tris, size_t n, size_t prims_per_leaf,
+                          uint32_t fixes, float* nodes_out, size_t nodes_cap, uint32_t* idx_out, size_t idx_cap) {
+  if (n == 0) return -2;
+  std::vector<Aabb> a;
+  std::vector<V3> c;
+  load_aabbs(aabbs, n, a);
+  load_centers(centers, n, c);
+  SpatialBuild b;
+  b.tris = tris;
+  b.n = n;
+  b.max_leaf = prims_per_leaf == 0 ? 1 : prims_per_leaf;
+  b.fixes = fixes;
+  build_spatial(b, a.data(), c.data());
+  if (b.err) return -3;
+  if (b.nodes.size() > nodes_cap || b.prim_indices.size() > idx_cap) return -4;
   std::memcpy(nodes_out, b.nodes.data(), b.nodes.size() * sizeof(BvhNode));
   std::memcpy(idx_out, b.prim_indices.data(), b.prim_indices.size() * 4);
   return (int64_t)b.nodes.size();

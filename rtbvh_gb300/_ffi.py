@@ -38,6 +38,14 @@ TRACE_STATS = 2
 TRACE_REORDER = 4
 TRACE_EXACT_NODES = 8
 
+# RTBVH_SPATIAL_FIX_*: corrections of the reference's spatial-split builder.
+SPATIAL_FIX_CLIP = 1
+SPATIAL_FIX_EXIT_BIN = 2
+SPATIAL_FIX_SWEEP_BOX = 4
+SPATIAL_FIX_SPLIT_SPACE = 8
+SPATIAL_FIX_FALLBACK = 16
+SPATIAL_FIX_ALL = 31
+
 
 class RTAabb(ctypes.Structure):
     _fields_ = [("min", ctypes.c_float * 3), ("count", ctypes.c_int32), ("max", ctypes.c_float * 3),
@@ -105,6 +113,7 @@ SIGNATURES = {
     "free_bvh": (None, [RTBvh]),
     "free_mbvh": (None, [RTMbvh]),
     "rtbvh_gpu_create_bvh_from_triangles": (_rc, [_vp, _sz, _sz, _u32, _u32, _vp, ctypes.POINTER(RTBvh)]),
+    "rtbvh_gpu_create_spatial_bvh": (_rc, [_vp, _sz, _vp, _vp, _sz, _sz, _u32, _u32, _vp, ctypes.POINTER(RTBvh)]),
     "rtbvh_gpu_create_bvh": (_rc, [_vp, _sz, _vp, _sz, _sz, _u32, _u32, _vp, ctypes.POINTER(RTBvh)]),
     "rtbvh_gpu_create_mbvh": (_rc, [RTBvh, _u32, _vp, ctypes.POINTER(RTMbvh)]),
     "rtbvh_gpu_set_triangles": (_rc, [_u32, ctypes.c_int, _vp, _sz, _vp]),

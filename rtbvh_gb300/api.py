@@ -206,7 +206,8 @@ class Bvh:
         """Device triangles (n, 3, 3) for the GPU traces of a structure that
         has none (e.g. one loaded with from_bytes)."""
         v = _cuda_f32(vertices)
-        check(self._lib.rtbvh_gpu_set_triangles(self._h.id, 0, _ptr(v), self._n, _stream(stream)), "set_triangles")
+        check(self._lib.rtbvh_gpu_set_triangles(self._h.id, 0, _ptr(v), v.numel() // 9, _stream(stream)),
+              "set_triangles")
 
     def to_bytes(self):
         """The crate's serde form of the Bvh in bincode 1 layout (see rtbvh.h)."""
@@ -327,7 +328,8 @@ class Mbvh:
     def attach_triangles(self, vertices, stream=None):
         """Device triangles (n, 3, 3) for the GPU traces (see Bvh.attach_triangles)."""
         v = _cuda_f32(vertices)
-        check(self._lib.rtbvh_gpu_set_triangles(self._h.id, 1, _ptr(v), self._n, _stream(stream)), "set_triangles")
+        check(self._lib.rtbvh_gpu_set_triangles(self._h.id, 1, _ptr(v), v.numel() // 9, _stream(stream)),
+              "set_triangles")
 
     def to_bytes(self):
         """The crate's serde form of the Mbvh in bincode 1 layout (see rtbvh.h)."""
@@ -447,8 +449,29 @@ class Builder:
     def construct_locally_ordered_clustered(self, stream=None, host_mirror=True) -> Bvh:
         return self._construct(BvhType.LocallyOrderedClustered, stream, host_mirror)
 
-    def construct_spatial_sah(self):
-        raise NotImplementedError("the spatial-split SAH builder is not part of this library")
+    def construct_spatial_sah(self, stream=None, host_mirror=True, fixes=0) -> Bvh:
+        """Builder::construct_spatial_sah (src/bvh.rs:59-85) on the GPU;
+        primitives must be Triangles. ``fixes`` (SPATIAL_FIX_* bits of
+        ``rtbvh_gb300._ffi``) corrects defects of the reference builder;
+        0 reproduces it as written, which on many inputs leaves some
+        primitives out of every leaf."""
+        prims = self.primitives
+        n = 0 if prims is None else len(prims)
+        if n == 0:
+            raise BuildError.NoPrimitives()
+        if not isinstance(prims, Triangles):
+            raise TypeError("the spatial-split builder needs Triangles (SpatialTriangle)")
+        aabbs = None if self.aabbs is None else _aabbs_array(self.aabbs)
+        if aabbs is not None and len(aabbs) != n:
+            raise BuildError.InequalAabbsAndPrimitives(len(aabbs), n)
+        a = _cuda_f32(aabbs) if aabbs is not None else None
+        lib = _ffi.load()
+        out = _ffi.RTBvh()
+        flags = 0 if host_mirror else _ffi.FLAG_NO_HOST_MIRROR
+        check(lib.rtbvh_gpu_create_spatial_bvh(_ptr(prims.vertices), n, _ptr(a), None, 0,
+                                               int(self.primitives_per_leaf or 0), int(fixes), flags,
+                                               _stream(stream), ctypes.byref(out)), "create_spatial_bvh")
+        return Bvh(out, BuildType.Spatial, n)
 
     def _construct(self, bvh_type, stream, host_mirror):
         prims = self.primitives

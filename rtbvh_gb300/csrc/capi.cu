@@ -6,6 +6,7 @@
 // ids are never reused; free_* empties a slot. Each entry holds the device
 // arrays (nodes, indices, leaf-ordered triangles) and, unless asked not to,
 // a host mirror of nodes and indices that the handle pointers refer to.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -25,10 +26,12 @@ struct Entry {
   bool alive = false;
   bool mirrored = false;
   uint32_t node_count = 0;
-  uint32_t prim_count = 0;
+  uint32_t prim_count = 0;        // index slots (prim_indices entries)
+  uint32_t vertex_count = 0;      // primitives: boxes and triangles (a spatial tree has more slots)
+  bool vertex_lower_bound = false;  // loaded from bytes: vertex_count is the largest index + 1
   DAabb* d_nodes = nullptr;       // Bvh; Mbvh: its own copy of the source Bvh's nodes
   uint32_t bvh_node_count = 0;    // Mbvh: entries of d_nodes
-  uint32_t build_type = 0;        // Bvh: the crate's BuildType (1 LOCB, 2 binned SAH)
+  uint32_t build_type = 0;        // Bvh: the crate's BuildType (1 LOCB, 2 binned SAH, 3 spatial)
   DMNode* d_mnodes = nullptr;     // Mbvh
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
@@ -57,7 +60,7 @@ struct Entry {
     std::vector<DAabb>().swap(h_nodes);
     std::vector<DMNode>().swap(h_mnodes);
     std::vector<uint32_t>().swap(h_indices);
-    node_count = prim_count = 0;
+    node_count = prim_count = vertex_count = 0;
     alive = false;
     mirrored = false;
   }
@@ -137,21 +140,20 @@ ResultCode mirror_mbvh(Entry& e, cudaStream_t s) {
   return Ok;
 }
 
-// Builds a Bvh entry from device boxes + float4 centres (+ optional device
-// triangles, prim-id order) and stores it.
-ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t n, size_t ppl, BvhType type,
-                           const float* d_vertices, uint32_t flags, cudaStream_t s, RTBvh* result) {
-  BuildOutput out;
-  ResultCode rc = (type == LocallyOrderedClustered) ? build_locb(d_aabbs, d_centers, n, s, &out)
-                                                     : build_binned_sah(d_aabbs, d_centers, n, ppl, s, &out);
-  if (rc != Ok) return rc;
+// Stores a built Bvh (`slots` index entries over n primitives, BuildType
+// `build_type`) with its status word, optional device triangles (prim-id
+// order, re-laid per index slot) and host mirror.
+ResultCode store_bvh(const BuildOutput& out, uint32_t slots, size_t n, uint32_t build_type, const float* d_vertices,
+                     uint32_t flags, cudaStream_t s, RTBvh* result) {
   auto e = std::make_unique<Entry>();
   e->alive = true;
   e->node_count = out.node_count;
-  e->prim_count = (uint32_t)n;
+  e->prim_count = slots;
+  e->vertex_count = (uint32_t)n;
   e->d_nodes = out.nodes;
   e->d_indices = out.indices;
-  e->build_type = type == LocallyOrderedClustered ? 1u : 2u;
+  e->build_type = build_type;
+  ResultCode rc;
   cudaError_t err;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
     e->release();
@@ -160,8 +162,8 @@ ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t
   if (d_vertices) {
     if ((err = device_alloc(&e->d_vertices, 9 * n, s)) ||
         (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
-        (err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * n, s)) ||
-        (err = launch_gather_triangles(e->d_vertices, e->d_indices, n, e->d_tris, s))) {
+        (err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * slots, s)) ||
+        (err = launch_gather_triangles(e->d_vertices, e->d_indices, slots, e->d_tris, s))) {
       e->release();
       return cuda_rc(err);
     }
@@ -180,6 +182,28 @@ ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t
   uint32_t id = store(std::move(e), false);
   *result = bvh_handle(id, *raw);
   return Ok;
+}
+
+// Builds a Bvh entry from device boxes + float4 centres (+ optional device
+// triangles, prim-id order) and stores it.
+ResultCode build_and_store(const DAabb* d_aabbs, const float4* d_centers, size_t n, size_t ppl, BvhType type,
+                           const float* d_vertices, uint32_t flags, cudaStream_t s, RTBvh* result) {
+  BuildOutput out;
+  ResultCode rc = (type == LocallyOrderedClustered) ? build_locb(d_aabbs, d_centers, n, s, &out)
+                                                     : build_binned_sah(d_aabbs, d_centers, n, ppl, s, &out);
+  if (rc != Ok) return rc;
+  return store_bvh(out, (uint32_t)n, n, type == LocallyOrderedClustered ? 1u : 2u, d_vertices, flags, s, result);
+}
+
+// The spatial-split build of device boxes, float4 centres and triangles
+// (prim-id order), stored with the triangles (BuildType::Spatial, 3).
+ResultCode spatial_and_store(const DAabb* d_aabbs, const float4* d_centers, const float* d_vertices, size_t n,
+                             size_t ppl, uint32_t fixes, uint32_t flags, cudaStream_t s, RTBvh* result) {
+  BuildOutput out;
+  uint32_t slots = 0;
+  ResultCode rc = build_spatial_sah(d_aabbs, d_centers, d_vertices, n, ppl, fixes, s, &out, &slots);
+  if (rc != Ok) return rc;
+  return store_bvh(out, slots, n, 3u, d_vertices, flags, s, result);
 }
 
 // ------------------------------------------------------------- host iterators
@@ -302,9 +326,66 @@ bool finite3(const float* v) { return !(v[0] != v[0] || v[1] != v[1] || v[2] != 
 // =================================================================== part 1
 extern "C" {
 
-ResultCode create_spatial_Bvh(const RTAabb*, uintptr_t, const float*, uintptr_t, const float*, uintptr_t,
-                              uintptr_t, uint32_t, RTBvh*) {
-  return Error;
+// RTTriangleWrapper (rtbvh_ffi/src/lib.rs:258-336) gathered on the host,
+// then the build on the GPU with no corrections.
+ResultCode create_spatial_Bvh(const RTAabb* aabbs, uintptr_t prim_count, const float* centers, uintptr_t stride,
+                              const float* vertices, uintptr_t vertex_stride, uintptr_t triangle_stride,
+                              uint32_t prims_per_leaf, RTBvh* result) {
+  if (result == nullptr || centers == nullptr || vertices == nullptr) return Error;
+  if (stride % 4 != 0) return Error;  // assert_eq!(stride % 4, 0)
+  if (prim_count == 0) return NoPrimitives;
+  const size_t n = prim_count;
+  const uint32_t vs = (uint32_t)(vertex_stride / 4), cs = (uint32_t)stride;
+  std::vector<float> tris(9 * n);
+  std::vector<float4> c4(n);
+  size_t extent = 0;  // floats the triangles' own vertex reads cover
+  for (size_t i = 0; i < n; ++i) {
+    const uint32_t off = (uint32_t)(i * triangle_stride / 4);  // vertex0_offset
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t at = off + (uint32_t)k * vs;
+      for (int a = 0; a < 3; ++a) tris[9 * i + 3 * k + a] = vertices[at + a];
+      extent = std::max(extent, (size_t)at + 3);
+    }
+    const float* c = centers + (uint32_t)((uint32_t)i * cs / 4);  // center_i * center_stride / 4 (u32)
+    c4[i] = make_float4(c[0], c[1], c[2], 0.0f);
+  }
+  std::vector<RTAabb> boxes;
+  if (aabbs == nullptr) {  // Primitive::aabb of the wrapper (:281-296)
+    boxes.resize(n);
+    auto mn = [](float a, float b) { return a != a ? b : (b != b ? a : (a < b ? a : (b < a ? b : (std::signbit(a) ? a : b)))); };
+    auto mx = [](float a, float b) { return a != a ? b : (b != b ? a : (a > b ? a : (b > a ? b : (std::signbit(a) ? b : a)))); };
+    for (size_t i = 0; i < n; ++i) {
+      const uint32_t off = (uint32_t)(i * triangle_stride / 4);
+      const uint32_t base = off * vs / 4;
+      if ((size_t)base + 2 * (size_t)vs + 3 > extent) return InvalidArgument;
+      RTAabb b;
+      for (int a = 0; a < 3; ++a) {
+        b.min[a] = 1e34f;
+        b.max[a] = -1e34f;
+      }
+      b.count = 0;
+      b.left_first = 0;
+      for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) {
+          const float v = vertices[base + (uint32_t)k * vs + a];
+          b.min[a] = mn(b.min[a], v);
+          b.max[a] = mx(b.max[a], v);
+        }
+      boxes[i] = b;
+    }
+    aabbs = boxes.data();
+  }
+  cudaStream_t s = legacy_stream();
+  Scratch<float> d_t;
+  Scratch<DAabb> d_a;
+  Scratch<float4> d_c;
+  cudaError_t e;
+  if ((e = d_t.alloc(9 * n, s)) || (e = d_a.alloc(n, s)) || (e = d_c.alloc(n, s)) ||
+      (e = cudaMemcpyAsync(d_t.ptr, tris.data(), 36 * n, cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemcpyAsync(d_a.ptr, aabbs, 32 * n, cudaMemcpyHostToDevice, s)) ||
+      (e = cudaMemcpyAsync(d_c.ptr, c4.data(), 16 * n, cudaMemcpyHostToDevice, s)))
+    return cuda_rc(e);
+  return spatial_and_store(d_a.ptr, d_c.ptr, d_t.ptr, n, prims_per_leaf, 0u, 0u, s, result);
 }
 
 ResultCode create_bvh(const RTAabb* aabbs, uintptr_t prim_count, const float* centers, uintptr_t center_stride,
@@ -343,7 +424,7 @@ ResultCode refit(const RTAabb* aabbs, RTBvh bvh) {
     std::lock_guard<std::mutex> lock(g_mu);
     Entry* e = lookup(bvh.id, false);
     if (!e) return Error;
-    n = e->prim_count;
+    n = e->vertex_count;
   }
   Scratch<DAabb> d_a;
   cudaError_t err;
@@ -555,6 +636,24 @@ ResultCode rtbvh_gpu_create_bvh_from_triangles(const float* vertices, uintptr_t 
   return build_and_store(d_a.ptr, d_c4.ptr, prim_count, prims_per_leaf, bvh_type, vertices, flags, s, result);
 }
 
+ResultCode rtbvh_gpu_create_spatial_bvh(const float* vertices, uintptr_t prim_count, const RTAabb* aabbs,
+                                        const float* centers, uintptr_t center_stride, uintptr_t prims_per_leaf,
+                                        uint32_t fixes, uint32_t flags, rtbvh_stream_t stream, RTBvh* result) {
+  if (result == nullptr || (vertices == nullptr && prim_count > 0)) return Error;
+  if (centers && (center_stride % 4 != 0 || center_stride < 12 || center_stride > 16)) return Error;
+  if (fixes & ~RTBVH_SPATIAL_FIX_ALL) return InvalidArgument;
+  if (prim_count == 0) return NoPrimitives;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Scratch<DAabb> d_a;
+  Scratch<float4> d_c4;
+  cudaError_t e;
+  if ((e = d_a.alloc(prim_count, s)) || (e = d_c4.alloc(prim_count, s))) return cuda_rc(e);
+  if ((e = launch_triangle_prep(vertices, prim_count, d_a.ptr, d_c4.ptr, s))) return cuda_rc(e);
+  if (centers && (e = launch_pack_centers(centers, center_stride / 4, prim_count, d_c4.ptr, s))) return cuda_rc(e);
+  const DAabb* boxes = aabbs ? reinterpret_cast<const DAabb*>(aabbs) : d_a.ptr;
+  return spatial_and_store(boxes, d_c4.ptr, vertices, prim_count, prims_per_leaf, fixes, flags, s, result);
+}
+
 ResultCode rtbvh_gpu_create_bvh(const RTAabb* aabbs, uintptr_t prim_count, const float* centers,
                                 uintptr_t center_stride, uintptr_t prims_per_leaf, BvhType bvh_type, uint32_t flags,
                                 rtbvh_stream_t stream, RTBvh* result) {
@@ -574,7 +673,8 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   if (result == nullptr) return Error;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DAabb* d_nodes;
-  uint32_t node_count, prim_count;
+  uint32_t node_count, prim_count, vertex_count;
+  bool lower_bound;
   const uint32_t* d_indices;
   const float4* d_tris;
   const float* d_vertices;
@@ -585,6 +685,8 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     d_nodes = src->d_nodes;
     node_count = src->node_count;
     prim_count = src->prim_count;
+    vertex_count = src->vertex_count;
+    lower_bound = src->vertex_lower_bound;
     d_indices = src->d_indices;
     d_tris = src->d_tris;
     d_vertices = src->d_vertices;
@@ -592,11 +694,14 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   auto e = std::make_unique<Entry>();
   e->alive = true;
   e->prim_count = prim_count;
+  e->vertex_count = vertex_count;
+  e->vertex_lower_bound = lower_bound;
   e->source_bvh = bvh.id;
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
-  if ((rc = build_wide(d_nodes, node_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount)) != Ok) {
+  if ((rc = build_wide(d_nodes, node_count, d_indices, prim_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount)) !=
+      Ok) {
     e->release();
     return rc;
   }
@@ -615,8 +720,9 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     if ((err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * prim_count, s)) ||
         (err = cudaMemcpyAsync(e->d_tris, d_tris, 16 * (size_t)kTriFloat4 * prim_count, cudaMemcpyDeviceToDevice,
                                s)) ||
-        (err = device_alloc(&e->d_vertices, 9 * (size_t)prim_count, s)) ||
-        (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s))) {
+        (err = device_alloc(&e->d_vertices, 9 * (size_t)vertex_count, s)) ||
+        (err = cudaMemcpyAsync(e->d_vertices, d_vertices, 36 * (size_t)vertex_count, cudaMemcpyDeviceToDevice,
+                               s))) {
       e->release();
       return cuda_rc(err);
     }
@@ -643,12 +749,22 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
   std::lock_guard<std::mutex> lock(g_mu);
   Entry* e = lookup(structure_id, is_mbvh != 0);
   if (!e || vertices == nullptr) return Error;
-  if (prim_count != e->prim_count) return InequalAabbsAndPrimitives;
+  // a structure loaded from bytes knows only a lower bound of its
+  // primitive count (its largest index + 1)
+  if (e->vertex_lower_bound ? prim_count < e->vertex_count : prim_count != e->vertex_count)
+    return InequalAabbsAndPrimitives;
   cudaError_t err;
+  if (e->d_vertices && prim_count != e->vertex_count) {
+    void* const old_arrays[] = {e->d_vertices};
+    pool_free_now(old_arrays, 1);
+    e->d_vertices = nullptr;
+  }
+  e->vertex_count = (uint32_t)prim_count;
+  e->vertex_lower_bound = false;
   if (!e->d_vertices && (err = device_alloc(&e->d_vertices, 9 * (size_t)prim_count, s))) return cuda_rc(err);
-  if (!e->d_tris && (err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * prim_count, s))) return cuda_rc(err);
+  if (!e->d_tris && (err = device_alloc(&e->d_tris, (size_t)kTriFloat4 * e->prim_count, s))) return cuda_rc(err);
   if ((err = cudaMemcpyAsync(e->d_vertices, vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
-      (err = launch_gather_triangles(e->d_vertices, e->d_indices, prim_count, e->d_tris, s)))
+      (err = launch_gather_triangles(e->d_vertices, e->d_indices, e->prim_count, e->d_tris, s)))
     return cuda_rc(err);
   return Ok;
 }
@@ -889,7 +1005,7 @@ ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode** exact, const
 // `vertices` when given, and the host mirror refreshed.
 static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, const float* vertices,
                              cudaStream_t s) {
-  const size_t n = m->prim_count;
+  const size_t n = m->vertex_count, slots = m->prim_count;
   DMNode* fresh = nullptr;
   uint32_t count = 0;
   ResultCode rc;
@@ -908,12 +1024,14 @@ static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, 
   m->d_qnodes = nullptr;
   m->d_wnodes = nullptr;
   m->wcount = 0;
-  if ((rc = build_wide(nodes, node_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok) return rc;
+  if ((rc = build_wide(nodes, node_count, m->d_indices, m->prim_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) !=
+      Ok)
+    return rc;
   if (vertices) {
     if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
-    if (!m->d_tris && (err = device_alloc(&m->d_tris, (size_t)kTriFloat4 * n, s))) return cuda_rc(err);
+    if (!m->d_tris && (err = device_alloc(&m->d_tris, (size_t)kTriFloat4 * slots, s))) return cuda_rc(err);
     if ((err = cudaMemcpyAsync(m->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
-        (err = launch_gather_triangles(m->d_vertices, m->d_indices, n, m->d_tris, s)))
+        (err = launch_gather_triangles(m->d_vertices, m->d_indices, slots, m->d_tris, s)))
       return cuda_rc(err);
   }
   if (m->mirrored && (rc = mirror_mbvh(*m, s)) != Ok) return rc;
@@ -943,8 +1061,8 @@ ResultCode rtbvh_gpu_refit_mbvh(uint32_t mbvh_id, const float* vertices, const R
   Scratch<float4> d_c4;
   const DAabb* boxes = nullptr;
   cudaError_t err;
-  if ((err = refit_boxes(vertices, aabbs, m->prim_count, d_a, d_c4, &boxes, s))) return cuda_rc(err);
-  ResultCode rc = refit_bvh(m->d_nodes, m->bvh_node_count, m->d_indices, m->prim_count, boxes, s);
+  if ((err = refit_boxes(vertices, aabbs, m->vertex_count, d_a, d_c4, &boxes, s))) return cuda_rc(err);
+  ResultCode rc = refit_bvh(m->d_nodes, m->bvh_node_count, m->d_indices, m->prim_count, m->vertex_count, boxes, s);
   if (rc != Ok) return rc;
   return recollapse(m, m->d_nodes, m->bvh_node_count, vertices, s);
 }
@@ -961,7 +1079,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     m = lookup(mbvh_id, true);
     if (!m || m->source_bvh != bvh_id) return Error;
   }
-  const size_t n = b->prim_count;
+  const size_t n = b->vertex_count;
   Scratch<DAabb> d_a;
   Scratch<float4> d_c4;
   const DAabb* boxes = reinterpret_cast<const DAabb*>(aabbs);
@@ -972,11 +1090,11 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     boxes = d_a.ptr;
     if (b->d_vertices) {
       if ((err = cudaMemcpyAsync(b->d_vertices, vertices, 36 * n, cudaMemcpyDeviceToDevice, s)) ||
-          (err = launch_gather_triangles(b->d_vertices, b->d_indices, n, b->d_tris, s)))
+          (err = launch_gather_triangles(b->d_vertices, b->d_indices, b->prim_count, b->d_tris, s)))
         return cuda_rc(err);
     }
   }
-  ResultCode rc = refit_bvh(b->d_nodes, b->node_count, b->d_indices, b->prim_count, boxes, s);
+  ResultCode rc = refit_bvh(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count, boxes, s);
   if (rc != Ok) return rc;
   if (m) {
     if (m->d_nodes && (err = cudaMemcpyAsync(m->d_nodes, b->d_nodes, (size_t)b->node_count * sizeof(DAabb),
@@ -991,7 +1109,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
 ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb* aabbs, rtbvh_stream_t stream) {
   if (aabbs == nullptr) return Error;
   DAabb* nodes;
-  uint32_t node_count, prim_count;
+  uint32_t node_count, prim_count, vertex_count;
   const uint32_t* indices;
   {
     std::lock_guard<std::mutex> lock(g_mu);
@@ -1000,9 +1118,10 @@ ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb* aabbs, rtbvh_s
     nodes = b->d_nodes;
     node_count = b->node_count;
     prim_count = b->prim_count;
+    vertex_count = b->vertex_count;
     indices = b->d_indices;
   }
-  return refit_bvh_noalloc(nodes, node_count, indices, prim_count, reinterpret_cast<const DAabb*>(aabbs),
+  return refit_bvh_noalloc(nodes, node_count, indices, prim_count, vertex_count, reinterpret_cast<const DAabb*>(aabbs),
                            static_cast<cudaStream_t>(stream));
 }
 
@@ -1103,6 +1222,10 @@ bool indices_valid(const uint32_t* idx, uint64_t count) {
 // Uploads nodes and indices into a new entry (status word, host mirror).
 ResultCode upload_entry(Entry& e, const RTAabb* nodes, uint64_t node_count, const uint32_t* idx, uint64_t prim_count,
                         cudaStream_t s) {
+  uint32_t largest = 0;
+  for (uint64_t i = 0; i < prim_count; ++i) largest = std::max(largest, idx[i]);
+  e.vertex_count = largest + 1;
+  e.vertex_lower_bound = true;
   cudaError_t err;
   if ((err = device_alloc(&e.d_status, 4, s)) || (err = cudaMemsetAsync(e.d_status, 0, 16, s)) ||
       (err = device_alloc(&e.d_nodes, node_count, s)) ||
@@ -1241,7 +1364,9 @@ ResultCode rtbvh_deserialize_mbvh(const uint8_t* buffer, uintptr_t size, uint32_
         (check.size() != nq || std::memcmp(check.data(), hq.data(), nq * 128) != 0))
       rc = InvalidArgument;
   }
-  if (rc == Ok) rc = build_wide(e->d_nodes, e->bvh_node_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount);
+  if (rc == Ok)
+    rc = build_wide(e->d_nodes, e->bvh_node_count, e->d_indices, e->prim_count, s, &e->d_wnodes, &e->d_qnodes,
+                    &e->wcount);
   if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_mbvh(*e, s);
   if (rc != Ok) {
     e->release();

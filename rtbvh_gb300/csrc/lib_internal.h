@@ -91,15 +91,29 @@ ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n, cudaS
 ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n, size_t prims_per_leaf,
                             cudaStream_t s, BuildOutput* out);
 
+// SpatialSahBuilder::build (src/builders/spatial_sah.rs:926-1034): tris
+// are the n triangles (9 floats each, prim-id order), centers their
+// Primitive::center. *index_count gets the length of prim_indices
+// (max_reference_count; entries past the leaves' ranges are 0). fixes:
+// RTBVH_SPATIAL_FIX_* bits, 0 = the reference as written. Error where the
+// reference panics.
+uint64_t spatial_max_refs(size_t n);
+ResultCode build_spatial_sah(const DAabb* aabbs, const float4* centers, const float* tris, size_t n,
+                             size_t prims_per_leaf, uint32_t fixes, cudaStream_t s, BuildOutput* out,
+                             uint32_t* index_count);
+
 // Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here.
 ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes,
                       uint32_t* mnode_count);
 // The closest-hit traversal tree: a 4-wide collapse of the BVH2 with tight
 // slot boxes (largest-area child opened first), as exact nodes and compact
 // copies; *wcount nodes, root 0. No tree (*wcount 0, Ok) when a node's box
-// does not contain its children's (closest hit then reads the exact nodes).
-ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** wnodes, DQNode** wq,
-                      uint32_t* wcount);
+// does not contain its children's, or (indices given) when the leaves do not
+// hold each of the index_count slots and each primitive exactly once --
+// spatial-split trees, whose leaf boxes bound fragments -- closest hit then
+// reads the exact nodes in the reference's order.
+ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                      cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount);
 // Traversal trees of a concatenated forest (LOCB meshes): mesh m's tree in
 // nodes [off_m, off_m + n_m) of wnodes (exact) and wq (compact), root off_m;
 // q0/q1 hold total_prims entries each.
@@ -111,14 +125,15 @@ cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const 
 cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,
                                  const uint32_t* live_count = nullptr);
 
-// Bvh::refit (src/bvh.rs:176-205) bounds, topology kept.
-ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
-                     const DAabb* aabbs, cudaStream_t s);
+// Bvh::refit (src/bvh.rs:176-205) bounds, topology kept. Leaves index
+// `indices` (index_count slots), which index `aabbs` (prim_count boxes).
+ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                     uint32_t prim_count, const DAabb* aabbs, cudaStream_t s);
 
 // refit_bvh with its scratch in a static device array instead of per-call
 // allocations (see rtbvh_gpu_refit_noalloc). Asynchronous on `s`.
-ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
-                             const DAabb* aabbs, cudaStream_t s);
+ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                             uint32_t prim_count, const DAabb* aabbs, cudaStream_t s);
 
 // ------------------------------------------------------------------ traversal
 struct TraceArgs {

@@ -299,7 +299,8 @@ __global__ void __launch_bounds__(kBlock) k_collapse_segments(SegCollapseParams 
 // exact, so the boxes equal the reference's reverse-order loop bit for bit.
 // Unlike the reference, count/left_first are kept (see include/rtbvh.h).
 __global__ void __launch_bounds__(kBlock)
-    k_refit(DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices, uint32_t prim_count,
+    k_refit(DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices, uint32_t index_count,
+            uint32_t prim_count,
             const DAabb* __restrict__ aabbs, const uint32_t* __restrict__ parent, uint32_t* __restrict__ arrive,
             uint32_t* __restrict__ status) {
   uint32_t c = blockIdx.x * kBlock + threadIdx.x;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(kBlock)
   if (nd.left_first >= 0) {
     for (int32_t i = 0; i < nd.count; ++i) {
       uint32_t slot = (uint32_t)nd.left_first + (uint32_t)i;
-      if (slot >= prim_count) { atomicOr(status, kStatusBadIndex); break; }
+      if (slot >= index_count) { atomicOr(status, kStatusBadIndex); break; }
       uint32_t p = __ldg(indices + slot);
       if (p >= prim_count) { atomicOr(status, kStatusBadIndex); break; }
       DAabb b = load_aabb(aabbs + p);
@@ -421,8 +422,8 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
 
 namespace rtbvh {
 
-ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
-                     const DAabb* aabbs, cudaStream_t s) {
+ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                     uint32_t prim_count, const DAabb* aabbs, cudaStream_t s) {
   if (node_count == 0) return Ok;
   cudaError_t e;
   Scratch<uint32_t> parent, arrive, status;
@@ -433,8 +434,8 @@ ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices,
     return cuda_rc(e);
   const unsigned blocks = (node_count + kBlock - 1) / kBlock;
   k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, status.ptr);
-  k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, prim_count, aabbs, parent.ptr, arrive.ptr,
-                                    status.ptr);
+  k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, index_count, prim_count, aabbs, parent.ptr,
+                                    arrive.ptr, status.ptr);
   uint32_t st = 0;
   if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&st, status.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
       (e = cudaStreamSynchronize(s)))
@@ -483,8 +484,8 @@ cudaError_t noalloc_scratch(uint32_t** out) {
 
 }  // namespace
 
-ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t prim_count,
-                             const DAabb* aabbs, cudaStream_t s) {
+ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                             uint32_t prim_count, const DAabb* aabbs, cudaStream_t s) {
   if (node_count == 0) return Ok;
   if (node_count > RTBVH_REFIT_NOALLOC_MAX_NODES) return InvalidArgument;
   uint32_t* base = nullptr;
@@ -500,7 +501,8 @@ ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* 
     return cuda_rc(e);
   const unsigned blocks = (node_count + kBlock - 1) / kBlock;
   k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent, arrive, status);
-  k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, prim_count, aabbs, parent, arrive, status);
+  k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, index_count, prim_count, aabbs, parent, arrive,
+                                    status);
   return cuda_rc(cudaGetLastError());
 }
 
@@ -842,6 +844,33 @@ __global__ void __launch_bounds__(kBlock) k_check_nested(const DAabb* __restrict
   if (!ok) atomicOr(not_nested, 1u);
 }
 
+// The leaves of the object-split builders hold every index slot once and
+// every primitive once, so their boxes cover whole primitives. Spatial-split
+// trees (several fragments of a triangle, fragment boxes, unused slots) do
+// not: any of those sets *bad.
+__global__ void __launch_bounds__(kBlock) k_check_leaves(const DAabb* __restrict__ nodes, uint32_t node_count,
+                                                         const uint32_t* __restrict__ indices, uint32_t index_count,
+                                                         uint32_t* __restrict__ seen, uint32_t* __restrict__ total,
+                                                         uint32_t* __restrict__ bad) {
+  const uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  const DAabb n = load_aabb(nodes + c);
+  if (n.count < 0 || n.left_first < 0) return;
+  atomicAdd(total, (uint32_t)n.count);
+  for (int32_t k = 0; k < n.count; ++k) {
+    const uint32_t slot = (uint32_t)n.left_first + (uint32_t)k;
+    if (slot >= index_count) {
+      atomicOr(bad, 1u);
+      return;
+    }
+    const uint32_t p = __ldg(indices + slot);
+    if (p >= index_count || atomicAdd(seen + p, 1u) != 0u) {
+      atomicOr(bad, 1u);
+      return;
+    }
+  }
+}
+
 __global__ void k_wide_init(uint2* queue0, uint32_t* qcount, uint32_t* walloc) {
   if (threadIdx.x == 0) {
     queue0[0] = make_uint2(0u, 0u);
@@ -914,8 +943,8 @@ cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const 
   return launch_quantize_mbvh(wnodes, total_prims, wq, s);
 }
 
-ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** wnodes_out,
-                      DQNode** wq_out, uint32_t* wcount) {
+ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                      cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount) {
   *wnodes_out = nullptr;
   *wq_out = nullptr;
   *wcount = 0;
@@ -939,13 +968,21 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   if ((e = device_alloc(&wn, capacity, s))) return fail(cuda_rc(e));
   if ((e = cudaMemsetAsync(status.ptr, 0, 16, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
     return fail(cuda_rc(e));
-  // status[1]: not nested -> no traversal tree (closest hit uses the exact nodes)
+  // status[1]: not nested, or leaves that are not whole primitives once
+  // each -> no traversal tree (closest hit uses the exact nodes)
   k_check_nested<<<(node_count + kBlock - 1) / kBlock, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
   {
-    uint32_t nn = 0;
-    if ((e = cudaMemcpyAsync(&nn, status.ptr + 1, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+    Scratch<uint32_t> seen;
+    if (indices) {
+      if ((e = seen.alloc(index_count, s)) || (e = cudaMemsetAsync(seen.ptr, 0, (size_t)index_count * 4, s)))
+        return fail(cuda_rc(e));
+      k_check_leaves<<<(node_count + kBlock - 1) / kBlock, kBlock, 0, s>>>(nodes, node_count, indices, index_count,
+                                                                           seen.ptr, status.ptr + 2, status.ptr + 1);
+    }
+    uint32_t h[2] = {0, 0};
+    if ((e = cudaMemcpyAsync(h, status.ptr + 1, 8, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
       return fail(cuda_rc(e));
-    if (nn) return fail(Ok);
+    if (h[0] || (indices && h[1] != index_count)) return fail(Ok);
   }
   k_wide_init<<<1, 32, 0, s>>>(q0.ptr, qcount.ptr, walloc.ptr);
   int per_sm = 0;

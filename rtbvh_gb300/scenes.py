@@ -118,6 +118,19 @@ def incoherent(n, seed=2, median=0.005, sigma=0.5):
     return (c + dirs * length).astype(np.float32)
 
 
+def slivers(n, seed=5, length=1.0, width=0.01):
+    """Long thin triangles in random directions from points in the unit
+    cube: their boxes overlap heavily, the case spatial splits are for."""
+    rng = _rng(seed)
+    a = rng.uniform(0.0, 1.0, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    e = rng.normal(size=(n, 3))
+    e -= (e * d).sum(1, keepdims=True) * d
+    e /= np.linalg.norm(e, axis=1, keepdims=True)
+    return np.stack([a, a + length * d, a + 0.5 * length * d + width * e], axis=1).astype(np.float32)
+
+
 def incoherent_rays(count, seed=3, center=(0.5, 0.5, 0.5), radius=2.0, lo=0.0, hi=1.0):
     """Returns (rays (R,6) float32, any-hit t_max (R,) float32)."""
     rng = _rng(seed)
