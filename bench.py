@@ -281,6 +281,8 @@ def run_gpu(args):
         t_err = t_error_vs_fp64(tris, rays, step()[: 1 << 20].cpu().numpy())
     if rank == 0 and not args.no_extra:
         workloads["sphere_6400_binned_sah"] = workload_sphere_sah(not args.no_cpu_baseline)
+        workloads["spatial_sah_teapot"] = workload_spatial("teapot", not args.no_cpu_baseline)
+        workloads["spatial_sah_slivers_20k"] = workload_spatial("slivers", not args.no_cpu_baseline)
         workloads["differentiable_200k"] = workload_differentiable()
         workloads["batched_512_meshes"] = workload_batched()
         workloads["clustered_10M_binned_sah"] = workload_clustered()
@@ -378,6 +380,45 @@ def workload_sphere_sah(with_cpu):
         cpu_pk = len(rays) / (time.perf_counter() - t0) / 1e6
         out["cpu_baseline"] = {"sah_build_ms": round(cpu_build, 3), "closest_hit_mrays": round(cpu_rays, 2),
                                "packets_mbvh_mrays": round(cpu_pk, 2), "cores": threads, "kind": "port"}
+    return out
+
+
+def workload_spatial(name, with_cpu):
+    """Spatial-split SAH builds (src/builders/spatial_sah.rs) as the reference
+    writes them and with every correction, then MBVH closest hit over each
+    tree (exact nodes, the reference's order): the 6,320-triangle teapot the
+    reference's README times, or 20,000 long thin triangles."""
+    import torch
+
+    import rtbvh_gb300 as rb
+    from rtbvh_gb300 import _ffi, scenes
+    if name == "teapot":
+        tris = np.load(os.path.join(ROOT, "tests", "golden", "teapot_tris.npy")).astype(np.float32)
+        rays = scenes.camera_rays(1024, 1024, eye=(0.0, 1.5, 8.0), fov_deg=40.0)
+    else:
+        tris = scenes.slivers(20000, seed=5, length=0.2)
+        rays, _ = scenes.incoherent_rays(1 << 20, seed=8)
+    d_tris, d_rays = torch.from_numpy(tris).cuda(), torch.from_numpy(rays).cuda()
+    b = rb.Builder(primitives=rb.Triangles(d_tris))
+    out = {"triangles": len(tris), "rays": len(rays)}
+    for label, fixes in (("as_written", 0), ("corrected", _ffi.SPATIAL_FIX_ALL)):
+        build_ms = _cuda_time(lambda: b.construct_spatial_sah(fixes=fixes, host_mirror=False))
+        g = b.construct_spatial_sah(fixes=fixes)
+        m = rb.Mbvh.construct(g, host_mirror=False)
+        trace_ms = _cuda_time(lambda: m.intersect(d_rays), reps=10)
+        ints = g.nodes().view(np.int32)
+        out[label] = {"build_ms": round(build_ms, 3), "nodes": len(ints),
+                      "leaf_references": int(ints[ints[:, 3] >= 0, 3].sum()),
+                      "every_primitive_referenced": g.validate(len(tris)),
+                      "closest_hit_mrays": round(len(rays) / (trace_ms * 1e-3) / 1e6, 1)}
+    if with_cpu:
+        import oracle
+        cpu = {}
+        for label, fixes in (("as_written", 0), ("corrected", oracle.SPATIAL_FIX_ALL)):
+            t0 = time.perf_counter()
+            oracle.build_spatial(tris, fixes=fixes)
+            cpu[label + "_build_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+        out["cpu_baseline"] = {**cpu, "cores": 1, "kind": "port"}
     return out
 
 
@@ -637,6 +678,8 @@ def run_reference(args):
 
 ONLY_WORKLOADS = {
     "sphere_6400_binned_sah": lambda: workload_sphere_sah(False),
+    "spatial_sah_teapot": lambda: workload_spatial("teapot", True),
+    "spatial_sah_slivers_20k": lambda: workload_spatial("slivers", True),
     "differentiable_200k": lambda: workload_differentiable(),
     "batched_512_meshes": lambda: workload_batched(),
     "clustered_10M_binned_sah": lambda: workload_clustered(False),
