@@ -791,11 +791,196 @@ __device__ void sb_apply_object(const SbArgs& A, SbShared& sh, uint32_t t, int a
   sb_allocate_children(A, sh, t, s, end, lb, rbx, true);
 }
 
-// apply_spatial_split (:605-724). The classes are computed in parallel; the
-// swap loop, the equal-count fallback and the straddler loop are replayed
-// by thread 0 on a permutation of slots; then every thread builds the new
-// reference order (fragments clipped from the triangle) and all three
-// arrays receive it.
+// Class bytes read through a window of 8 loaded at once (the replay below
+// walks them forwards from the front and backwards from the back).
+struct SbWin {
+  unsigned long long bits;
+  uint32_t base;
+  bool valid;
+};
+__device__ __forceinline__ uint32_t sb_cls_fwd(const uint8_t* C, uint32_t n, SbWin& w, uint32_t k) {
+  if (!w.valid || k < w.base || k >= w.base + 8) {
+    w.base = k;
+    w.valid = true;
+    unsigned long long v = 0;
+#pragma unroll
+    for (uint32_t t = 0; t < 8; ++t)
+      if (k + t < n) v |= (unsigned long long)__ldcg(C + k + t) << (8 * t);
+    w.bits = v;
+  }
+  return (uint32_t)(w.bits >> (8 * (k - w.base))) & 0xffu;
+}
+__device__ __forceinline__ uint32_t sb_cls_bwd(const uint8_t* C, SbWin& w, uint32_t k) {
+  if (!w.valid || k < w.base || k >= w.base + 8) {
+    w.base = k >= 7 ? k - 7 : 0;
+    w.valid = true;
+    unsigned long long v = 0;
+#pragma unroll
+    for (uint32_t t = 0; t < 8; ++t)
+      if (w.base + t <= k) v |= (unsigned long long)__ldcg(C + w.base + t) << (8 * t);
+    w.bits = v;
+  }
+  return (uint32_t)(w.bits >> (8 * (k - w.base))) & 0xffu;
+}
+
+constexpr uint32_t kSbRing = kSbTile * 2;  // straddler queue in the sort tile (u32 entries)
+
+// The reference's partition loops (:622-702) replayed by thread 0 without
+// moving references, writing the final order into P (slot | kind):
+//  * the swap loop takes the front reference; a right one goes to the next
+//    slot from the back and the reference there is taken next, a left one to
+//    the next slot from the front, where the straddler it displaces moves
+//    behind the others -- so left references keep their processing order,
+//    right ones fill the back in processing order, and the straddlers form a
+//    queue that every left reference processed after the first straddler
+//    rotates by one;
+//  * the fallback and the straddler loop then walk that queue from both
+//    ends the same way.
+// The queue lives in shared memory (m <= kSbRing straddlers). Returns false
+// where the reference panics.
+__device__ bool sb_replay_ring(const SbArgs& A, SbShared& sh, uint32_t n, uint32_t m) {
+  const uint32_t begin = sh.begin;
+  uint32_t* P = A.perm + begin;
+  const uint8_t* C = A.cls + begin;
+  uint32_t* ring = reinterpret_cast<uint32_t*>(sh.u.tile);
+  constexpr uint32_t mask = kSbRing - 1;
+  uint32_t i = 0, j = 0, le = 0, rc = 0, qh = 0, qt = 0;
+  SbWin fw{0ull, 0u, false}, bw{0ull, 0u, false};
+  while (i + j < n) {
+    uint32_t src = i, c = sb_cls_fwd(C, n, fw, i);
+    bool done = false;
+    while (c == kClsRight) {
+      P[n - 1 - rc] = src;
+      ++rc;
+      ++j;
+      if (i + j >= n) {
+        done = true;
+        break;
+      }
+      src = n - j;
+      c = sb_cls_bwd(C, bw, src);
+    }
+    if (done) break;
+    if (c == kClsLeft) {
+      P[le++] = src;
+      if (qt != qh) {
+        ring[qt & mask] = ring[qh & mask];
+        ++qt;
+        ++qh;
+      }
+    } else {
+      ring[qt & mask] = src;
+      ++qt;
+    }
+    ++i;
+  }
+  uint32_t lc = le, rcnt = rc;
+  if ((lc == 0 || rcnt == 0) && m == 0) {  // equal-count fallback (:643-658)
+    if (lc > 0) {
+      if (A.fixes & kFixFallback) le = lc / 2;
+      else if (lc / 2 < begin) return false;  // left_end = left_count / 2 drops the begin: the slice panics
+      else le = lc / 2 - begin;
+    } else {
+      le += rcnt / 2;
+    }
+    sh.le = le;
+    sh.rb = le;
+    sh.re = n;
+    return true;
+  }
+  const uint32_t space = sh.split_end - begin;
+  uint32_t re = n, a = 0, bp = m;
+  uint32_t cur = m ? ring[qh & mask] : 0u;
+  while (a < bp) {
+    if (space - re > 0) {
+      P[le + a] = cur | kKindLeftFrag;
+      P[re++] = cur | kKindRightFrag;
+      ++a;
+      ++lc;
+      ++rcnt;
+      if (a < bp) cur = ring[(qh + a) & mask];
+    } else if (lc < rcnt) {
+      P[le + a] = cur;
+      ++a;
+      ++lc;
+      if (a < bp) cur = ring[(qh + a) & mask];
+    } else {
+      --bp;
+      P[le + bp] = cur;
+      ++rcnt;
+      if (a < bp) cur = ring[(qh + bp) & mask];
+    }
+  }
+  sh.le = le + a;
+  sh.rb = le + bp;
+  sh.re = re;
+  return true;
+}
+
+// The same replay with the references moved in P itself (any number of
+// straddlers; one dependent global access per step).
+__device__ bool sb_replay_global(const SbArgs& A, SbShared& sh, uint32_t n) {
+  const uint32_t begin = sh.begin;
+  uint32_t* P = A.perm + begin;
+  const uint8_t* C = A.cls + begin;
+  uint32_t i = 0, le = 0, rb = n, re = n;
+  while (i < rb) {
+    const uint32_t e = __ldcg(P + i);
+    const uint8_t c = __ldcg(C + e);
+    if (c == kClsLeft) {
+      P[i] = __ldcg(P + le);
+      P[le] = e;
+      ++i;
+      ++le;
+    } else if (c == kClsRight) {
+      --rb;
+      P[i] = __ldcg(P + rb);
+      P[rb] = e;
+    } else {
+      ++i;
+    }
+  }
+  uint32_t lc = le, rc = re - rb;
+  if ((lc == 0 || rc == 0) && le == rb) {
+    if (lc > 0) {
+      if (A.fixes & kFixFallback) le = lc / 2;
+      else if (lc / 2 < begin) return false;
+      else le = lc / 2 - begin;
+    } else {
+      le += rc / 2;
+    }
+    rb = le;
+  }
+  const uint32_t space = sh.split_end - begin;
+  while (le < rb) {
+    const uint32_t e = __ldcg(P + le);
+    if (space - re > 0) {
+      P[re] = e | kKindRightFrag;
+      P[le] = e | kKindLeftFrag;
+      ++re;
+      ++le;
+      ++lc;
+      ++rc;
+    } else if (lc < rc) {
+      ++le;
+      ++lc;
+    } else {
+      --rb;
+      P[le] = __ldcg(P + rb);
+      P[rb] = e;
+      ++rc;
+    }
+  }
+  sh.le = le;
+  sh.rb = rb;
+  sh.re = re;
+  return true;
+}
+
+// apply_spatial_split (:605-724). The classes are computed in parallel, the
+// partition is replayed by thread 0 into a permutation of slots, then every
+// thread builds the new reference order (fragments clipped from the
+// triangle) and all three arrays receive it.
 __device__ void sb_apply_spatial(const SbArgs& A, SbShared& sh, uint32_t t) {
   const uint32_t begin = sh.begin, end = sh.end, n = end - begin;
   const int ax = (int)sh.sp_axis;
@@ -803,68 +988,21 @@ __device__ void sb_apply_spatial(const SbArgs& A, SbShared& sh, uint32_t t) {
   SbRef* S = A.refs[ax];
   uint32_t* P = A.perm + begin;
   uint8_t* C = A.cls + begin;
+  uint32_t straddlers = 0;
   for (uint32_t k = threadIdx.x; k < n; k += kSbThreads) {
     const SbBox b = sb_ref_box(sb_load(S + begin + k));
-    C[k] = b.mx[ax] <= pos ? kClsLeft : (b.mn[ax] >= pos ? kClsRight : kClsStraddle);
-    P[k] = k;
+    const uint8_t c = b.mx[ax] <= pos ? kClsLeft : (b.mn[ax] >= pos ? kClsRight : kClsStraddle);
+    C[k] = c;
+    straddlers += c == kClsStraddle;
   }
+  const uint32_t m = sb_block_sum(sh, straddlers);
+  const bool ring = m <= kSbRing;
+  if (!ring)
+    for (uint32_t k = threadIdx.x; k < n; k += kSbThreads) P[k] = k;
   __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t i = 0, le = 0, rb = n, re = n;
-    while (i < rb) {
-      const uint32_t e = __ldcg(P + i);
-      const uint8_t c = __ldcg(C + e);
-      if (c == kClsLeft) {
-        P[i] = __ldcg(P + le);
-        P[le] = e;
-        ++i;
-        ++le;
-      } else if (c == kClsRight) {
-        --rb;
-        P[i] = __ldcg(P + rb);
-        P[rb] = e;
-      } else {
-        ++i;
-      }
-    }
-    uint32_t lc = le, rc = re - rb;
-    if ((lc == 0 || rc == 0) && le == rb) {
-      if (lc > 0) {
-        if (A.fixes & kFixFallback) {
-          le = lc / 2;
-        } else if (lc / 2 < begin) {  // left_end = left_count / 2 drops the begin: the slice panics
-          sh.fail |= kSbPanic;
-        } else {
-          le = lc / 2 - begin;
-        }
-      } else {
-        le += rc / 2;
-      }
-      rb = le;
-    }
-    const uint32_t space = sh.split_end - begin;
-    while (!sh.fail && le < rb) {
-      const uint32_t e = __ldcg(P + le);
-      if (space - re > 0) {
-        P[re] = e | kKindRightFrag;
-        P[le] = e | kKindLeftFrag;
-        ++re;
-        ++le;
-        ++lc;
-        ++rc;
-      } else if (lc < rc) {
-        ++le;
-        ++lc;
-      } else {
-        --rb;
-        P[le] = __ldcg(P + rb);
-        P[rb] = e;
-        ++rc;
-      }
-    }
-    sh.le = le;
-    sh.rb = rb;
-    sh.re = re;
+    const bool ok = ring ? sb_replay_ring(A, sh, n, m) : sb_replay_global(A, sh, n);
+    if (!ok) sh.fail |= kSbPanic;
   }
   __syncthreads();
   if (sh.fail) {
@@ -1025,6 +1163,33 @@ __global__ void k_sb_init(SbArgs A, const DAabb* aabbs, const DAabb* world) {
   }
 }
 
+// The root's find_object_split sort (:316-331) for one axis, before the
+// build: keys are the order-preserving centre bits (-0 as +0), values the
+// reference index; a stable LSD radix sort of (key, index) in index order
+// gives the stable order on the centre.
+__global__ void k_sb_root_keys(const float4* __restrict__ centers, uint32_t n, int ax, uint32_t* keys,
+                               uint32_t* vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 c4 = __ldg(centers + i);
+  float c = sb_axis(c4.x, c4.y, c4.z, ax);
+  if (c == 0.0f) c = 0.0f;
+  keys[i] = float_to_ordered(c);
+  vals[i] = i;
+}
+__global__ void k_sb_root_gather(const DAabb* __restrict__ aabbs, const uint32_t* __restrict__ order, uint32_t n,
+                                 SbRef* refs) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t i = order[k];
+  const DAabb a = load_aabb(aabbs + i);
+  SbRef r;
+  r.lo = make_float4(a.min[0], a.min[1], a.min[2], __uint_as_float(i));
+  r.hi = make_float4(a.max[0], a.max[1], a.max[2], 0.0f);
+  sb_store(refs + k, r);
+}
+__global__ void k_sb_root_sorted(SbTask* tasks) { tasks[0].meta |= 1u << 8; }
+
 // ------------------------------------------------------------------ numbering
 struct SbNumArgs {
   const SbTask* tasks;
@@ -1140,7 +1305,7 @@ ResultCode build_spatial_sah(const DAabb* aabbs, const float4* centers, const fl
   Scratch<SbRef> r0, r1, r2, scr;
   Scratch<unsigned long long> k0, k1;
   Scratch<float> fbuf;
-  Scratch<uint32_t> perm, hk, hv, ready, child, arrive, ic, lr, ib, lb, acc6;
+  Scratch<uint32_t> perm, hk, hv, ready, child, arrive, ic, lr, ib, lb, acc6, rstat;
   Scratch<uint8_t> cls;
   Scratch<SbTask> tasks;
   Scratch<SbCtl> ctl;
@@ -1153,7 +1318,8 @@ ResultCode build_spatial_sah(const DAabb* aabbs, const float4* centers, const fl
       (e = tasks.alloc(task_cap, s)) || (e = ready.alloc(task_cap, s)) || (e = child.alloc(task_cap, s)) ||
       (e = arrive.alloc(task_cap, s)) || (e = ic.alloc(task_cap, s)) || (e = lr.alloc(task_cap, s)) ||
       (e = ib.alloc(task_cap, s)) || (e = lb.alloc(task_cap, s)) || (e = ctl.alloc(1, s)) ||
-      (e = world.alloc(1, s)) || (e = acc6.alloc(6, s)))
+      (e = world.alloc(1, s)) || (e = acc6.alloc(6, s)) || (e = rstat.alloc(1, s)) ||
+      (e = cudaMemsetAsync(rstat.ptr, 0, 4, s)))
     return cuda_rc(e);
   if ((e = launch_world_bounds(aabbs, n, world.ptr, acc6.ptr, s))) return cuda_rc(e);
   SbArgs A;
@@ -1180,14 +1346,29 @@ ResultCode build_spatial_sah(const DAabb* aabbs, const float4* centers, const fl
   A.max_leaf = prims_per_leaf == 0 ? 1u : (uint32_t)std::min<size_t>(prims_per_leaf, 0xffffffffu);
   A.fixes = fixes;
   k_sb_init<<<(task_cap + 255) / 256, 256, 0, s>>>(A, aabbs, world.ptr);
+  if (n > 1) {  // the root's three sorts, device wide
+    Scratch<uint32_t> rk, rv;
+    Scratch<uint8_t> temp;
+    const size_t tb = radix_sort_temp_bytes(n);
+    if ((e = rk.alloc(n, s)) || (e = rv.alloc(n, s)) || (e = temp.alloc(tb, s))) return cuda_rc(e);
+    const unsigned g = (unsigned)((n + 255) / 256);
+    for (int ax = 0; ax < 3; ++ax) {
+      k_sb_root_keys<<<g, 256, 0, s>>>(centers, (uint32_t)n, ax, rk.ptr, rv.ptr);
+      if ((e = radix_sort_pairs(rk.ptr, rv.ptr, n, 32, temp.ptr, tb, rstat.ptr, s))) return cuda_rc(e);
+      k_sb_root_gather<<<g, 256, 0, s>>>(aabbs, rv.ptr, (uint32_t)n, A.refs[ax]);
+    }
+    k_sb_root_sorted<<<1, 1, 0, s>>>(tasks.ptr);
+  }
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sb_build, kSbThreads, 0);
   k_sb_build<<<sm_count() * std::max(per_sm, 1), kSbThreads, 0, s>>>(A);
   if ((e = cudaGetLastError())) return cuda_rc(e);
   SbCtl h;
-  if ((e = cudaMemcpyAsync(&h, ctl.ptr, sizeof(SbCtl), cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+  uint32_t sort_status = 0;
+  if ((e = cudaMemcpyAsync(&h, ctl.ptr, sizeof(SbCtl), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(&sort_status, rstat.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
     return cuda_rc(e);
-  if (h.status & kStatusTimeout) return Timeout;
+  if ((h.status | sort_status) & kStatusTimeout) return Timeout;
   if (h.status & kSbAbort) return Error;  // the reference panics on this input
   SbNumArgs na{tasks.ptr, child.ptr, ctl.ptr, arrive.ptr, ic.ptr, lr.ptr, ib.ptr, lb.ptr};
   const unsigned grid = (h.tail + 255) / 256;
