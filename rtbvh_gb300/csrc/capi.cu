@@ -31,7 +31,8 @@ struct Entry {
   bool vertex_lower_bound = false;  // loaded from bytes: vertex_count is the largest index + 1
   DAabb* d_nodes = nullptr;       // Bvh; Mbvh: its own copy of the source Bvh's nodes
   uint32_t bvh_node_count = 0;    // Mbvh: entries of d_nodes
-  uint32_t build_type = 0;        // Bvh: the crate's BuildType (1 LOCB, 2 binned SAH, 3 spatial)
+  uint32_t build_type = 0;        // the crate's BuildType (1 LOCB, 2 binned SAH, 3 spatial; 0 unknown);
+                                  // an Mbvh keeps its source Bvh's
   DMNode* d_mnodes = nullptr;     // Mbvh
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
@@ -80,6 +81,13 @@ uint32_t store(std::unique_ptr<Entry> e, bool mbvh) {
   auto& t = mbvh ? g_mbvh : g_bvh;
   t.push_back(std::move(e));
   return (uint32_t)(t.size() - 1);
+}
+
+// Indices for build_wide's leaf check: trees of the object-split builders
+// (LOCB, binned SAH) hold each primitive once by construction and skip it;
+// spatial-split trees and structures of unknown origin are checked.
+const uint32_t* leaf_check(uint32_t build_type, const uint32_t* indices) {
+  return (build_type == 1 || build_type == 2) ? nullptr : indices;
 }
 
 cudaStream_t legacy_stream() {
@@ -673,7 +681,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   if (result == nullptr) return Error;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DAabb* d_nodes;
-  uint32_t node_count, prim_count, vertex_count;
+  uint32_t node_count, prim_count, vertex_count, build_type;
   bool lower_bound;
   const uint32_t* d_indices;
   const float4* d_tris;
@@ -687,6 +695,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     prim_count = src->prim_count;
     vertex_count = src->vertex_count;
     lower_bound = src->vertex_lower_bound;
+    build_type = src->build_type;
     d_indices = src->d_indices;
     d_tris = src->d_tris;
     d_vertices = src->d_vertices;
@@ -696,12 +705,13 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   e->prim_count = prim_count;
   e->vertex_count = vertex_count;
   e->vertex_lower_bound = lower_bound;
+  e->build_type = build_type;
   e->source_bvh = bvh.id;
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
-  if ((rc = build_wide(d_nodes, node_count, d_indices, prim_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount)) !=
-      Ok) {
+  if ((rc = build_wide(d_nodes, node_count, leaf_check(build_type, d_indices), prim_count, s, &e->d_wnodes,
+                       &e->d_qnodes, &e->wcount)) != Ok) {
     e->release();
     return rc;
   }
@@ -1024,8 +1034,8 @@ static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, 
   m->d_qnodes = nullptr;
   m->d_wnodes = nullptr;
   m->wcount = 0;
-  if ((rc = build_wide(nodes, node_count, m->d_indices, m->prim_count, s, &m->d_wnodes, &m->d_qnodes, &m->wcount)) !=
-      Ok)
+  if ((rc = build_wide(nodes, node_count, leaf_check(m->build_type, m->d_indices), m->prim_count, s, &m->d_wnodes,
+                       &m->d_qnodes, &m->wcount)) != Ok)
     return rc;
   if (vertices) {
     if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
@@ -1365,8 +1375,8 @@ ResultCode rtbvh_deserialize_mbvh(const uint8_t* buffer, uintptr_t size, uint32_
       rc = InvalidArgument;
   }
   if (rc == Ok)
-    rc = build_wide(e->d_nodes, e->bvh_node_count, e->d_indices, e->prim_count, s, &e->d_wnodes, &e->d_qnodes,
-                    &e->wcount);
+    rc = build_wide(e->d_nodes, e->bvh_node_count, leaf_check(e->build_type, e->d_indices), e->prim_count, s,
+                    &e->d_wnodes, &e->d_qnodes, &e->wcount);
   if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_mbvh(*e, s);
   if (rc != Ok) {
     e->release();
