@@ -44,6 +44,8 @@ constexpr int kSbPasses = 2;
 constexpr uint32_t kSbMaxDepth = 64;
 constexpr int kSbTile = 2048;  // keys sorted in shared memory at once
 constexpr int kSbMergeItems = 8;
+constexpr uint32_t kSbClsWords = 1024;            // shared class words: 16 classes each
+constexpr uint32_t kSbClsCap = kSbClsWords * 16;  // tasks up to this size replay from shared memory
 constexpr uint32_t kSbFrag = 0x80000000u;
 constexpr uint32_t kSbNone = 0xffffffffu;
 constexpr uint32_t kSbSpin = 1u << 22;  // queue waits (~1 us apart): a few seconds, then kStatusTimeout
@@ -246,6 +248,7 @@ struct SbShared {
   uint32_t redu[kSbWarps][2];
   float redc[kSbWarps];
   uint32_t redk[kSbWarps][2];
+  uint32_t cls2[kSbClsWords];  // spatial partition classes, 2 bits each
   union {
     unsigned long long tile[kSbTile];
     struct {
@@ -791,8 +794,13 @@ __device__ void sb_apply_object(const SbArgs& A, SbShared& sh, uint32_t t, int a
   sb_allocate_children(A, sh, t, s, end, lb, rbx, true);
 }
 
-// Class bytes read through a window of 8 loaded at once (the replay below
-// walks them forwards from the front and backwards from the back).
+__device__ __forceinline__ uint32_t sb_cls_at(const SbShared& sh, uint32_t k) {
+  return (sh.cls2[k >> 4] >> ((k & 15u) * 2u)) & 3u;
+}
+
+// Class bytes in global memory read through windows of 8 loaded at once
+// (the replay walks them forwards from the front and backwards from the
+// back), for tasks whose classes do not fit the shared words.
 struct SbWin {
   unsigned long long bits;
   uint32_t base;
@@ -822,6 +830,15 @@ __device__ __forceinline__ uint32_t sb_cls_bwd(const uint8_t* C, SbWin& w, uint3
   }
   return (uint32_t)(w.bits >> (8 * (k - w.base))) & 0xffu;
 }
+// Bits 0..15 of x to the even bit positions.
+__device__ __forceinline__ uint32_t sb_spread16(uint32_t x) {
+  x &= 0xffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
 
 constexpr uint32_t kSbRing = kSbTile * 2;  // straddler queue in the sort tile (u32 entries)
 
@@ -836,9 +853,10 @@ constexpr uint32_t kSbRing = kSbTile * 2;  // straddler queue in the sort tile (
 //    rotates by one;
 //  * the fallback and the straddler loop then walk that queue from both
 //    ends the same way.
-// The queue lives in shared memory (m <= kSbRing straddlers). Returns false
-// where the reference panics.
-__device__ bool sb_replay_ring(const SbArgs& A, SbShared& sh, uint32_t n, uint32_t m) {
+// The queue (m <= kSbRing straddlers) lives in shared memory, the classes
+// too (2 bits each) when `packed`, else they are read from C through
+// windows. Returns false where the reference panics.
+__device__ bool sb_replay_ring(const SbArgs& A, SbShared& sh, uint32_t n, uint32_t m, bool packed) {
   const uint32_t begin = sh.begin;
   uint32_t* P = A.perm + begin;
   const uint8_t* C = A.cls + begin;
@@ -847,7 +865,7 @@ __device__ bool sb_replay_ring(const SbArgs& A, SbShared& sh, uint32_t n, uint32
   uint32_t i = 0, j = 0, le = 0, rc = 0, qh = 0, qt = 0;
   SbWin fw{0ull, 0u, false}, bw{0ull, 0u, false};
   while (i + j < n) {
-    uint32_t src = i, c = sb_cls_fwd(C, n, fw, i);
+    uint32_t src = i, c = packed ? sb_cls_at(sh, i) : sb_cls_fwd(C, n, fw, i);
     bool done = false;
     while (c == kClsRight) {
       P[n - 1 - rc] = src;
@@ -858,7 +876,7 @@ __device__ bool sb_replay_ring(const SbArgs& A, SbShared& sh, uint32_t n, uint32
         break;
       }
       src = n - j;
-      c = sb_cls_bwd(C, bw, src);
+      c = packed ? sb_cls_at(sh, src) : sb_cls_bwd(C, bw, src);
     }
     if (done) break;
     if (c == kClsLeft) {
@@ -988,12 +1006,28 @@ __device__ void sb_apply_spatial(const SbArgs& A, SbShared& sh, uint32_t t) {
   SbRef* S = A.refs[ax];
   uint32_t* P = A.perm + begin;
   uint8_t* C = A.cls + begin;
+  // classes: one reference per thread (coalesced); up to kSbClsCap
+  // references they are packed 2 bits each into shared memory by warp
+  // ballots, beyond that (and for the global replay) bytes in C
   uint32_t straddlers = 0;
-  for (uint32_t k = threadIdx.x; k < n; k += kSbThreads) {
-    const SbBox b = sb_ref_box(sb_load(S + begin + k));
-    const uint8_t c = b.mx[ax] <= pos ? kClsLeft : (b.mn[ax] >= pos ? kClsRight : kClsStraddle);
-    C[k] = c;
-    straddlers += c == kClsStraddle;
+  const bool packed = n <= kSbClsCap;
+  for (uint32_t kb = 0; kb < n; kb += kSbThreads) {
+    const uint32_t k = kb + threadIdx.x;
+    uint32_t c = 0;
+    if (k < n) {
+      const SbBox b = sb_ref_box(sb_load(S + begin + k));
+      c = b.mx[ax] <= pos ? kClsLeft : (b.mn[ax] >= pos ? kClsRight : kClsStraddle);
+      C[k] = (uint8_t)c;
+      straddlers += c == kClsStraddle;
+    }
+    if (packed) {
+      const uint32_t b0 = __ballot_sync(0xffffffffu, c & 1u), b1 = __ballot_sync(0xffffffffu, c >> 1);
+      const uint32_t w0 = (kb + (threadIdx.x & ~31u)) >> 4;
+      if ((threadIdx.x & 31) == 0 && w0 < kSbClsWords) {
+        sh.cls2[w0] = sb_spread16(b0) | (sb_spread16(b1) << 1);
+        if (w0 + 1 < kSbClsWords) sh.cls2[w0 + 1] = sb_spread16(b0 >> 16) | (sb_spread16(b1 >> 16) << 1);
+      }
+    }
   }
   const uint32_t m = sb_block_sum(sh, straddlers);
   const bool ring = m <= kSbRing;
@@ -1001,7 +1035,7 @@ __device__ void sb_apply_spatial(const SbArgs& A, SbShared& sh, uint32_t t) {
     for (uint32_t k = threadIdx.x; k < n; k += kSbThreads) P[k] = k;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const bool ok = ring ? sb_replay_ring(A, sh, n, m) : sb_replay_global(A, sh, n);
+    const bool ok = ring ? sb_replay_ring(A, sh, n, m, packed) : sb_replay_global(A, sh, n);
     if (!ok) sh.fail |= kSbPanic;
   }
   __syncthreads();

@@ -131,6 +131,20 @@ def slivers(n, seed=5, length=1.0, width=0.01):
     return np.stack([a, a + length * d, a + 0.5 * length * d + width * e], axis=1).astype(np.float32)
 
 
+def plane_slivers(n, seed=32):
+    """Thin triangles stretched along x, lying on the planes y = 0, 1/3 and
+    2/3: spatial splits along y find no straddlers, the case of the spatial
+    builder's equal-count fallback."""
+    rng = _rng(seed)
+    a = rng.uniform(0.0, 1.0, size=(n, 3))
+    a[:, 1] = rng.integers(0, 3, n) / 3.0
+    b = a.copy()
+    b[:, 0] += rng.uniform(0.3, 1.0, n)
+    c = a.copy()
+    c[:, 2] += 0.01
+    return np.stack([a, b, c], axis=1).astype(np.float32)
+
+
 def incoherent_rays(count, seed=3, center=(0.5, 0.5, 0.5), radius=2.0, lo=0.0, hi=1.0):
     """Returns (rays (R,6) float32, any-hit t_max (R,) float32)."""
     rng = _rng(seed)

@@ -188,6 +188,27 @@ def test_refit_and_bytes(fixes, tmp_path):
     assert torch.equal(h1.view(torch.int32), h2.view(torch.int32))
 
 
+def test_panicking_inputs_return_error():
+    # inputs on which the reference's equal-count fallback panics (the
+    # oracle raises): the as-written build returns Error, the corrected
+    # builds match the oracle
+    for seed, n in ((32, 40), (87, 40), (261, 120)):
+        tris = scenes.plane_slivers(n, seed)
+        with pytest.raises(rb.RtbvhError) as e:
+            gpu_spatial(tris, 0)
+        assert e.value.code == rb.ResultCode.Error
+        for fixes in (oracle.SPATIAL_FIX_FALLBACK, oracle.SPATIAL_FIX_ALL):
+            g = gpu_spatial(tris, fixes)
+            on, oi = oracle.build_spatial(tris, fixes=fixes)
+            assert np.array_equal(u32(g.nodes()), u32(on)) and np.array_equal(g.indices(), oi)
+    # seeds of the same family where the reference does not panic
+    for seed in (1, 2, 3):
+        tris = scenes.plane_slivers(40, seed)
+        g = gpu_spatial(tris, 0)
+        on, oi = oracle.build_spatial(tris, fixes=0)
+        assert np.array_equal(u32(g.nodes()), u32(on)) and np.array_equal(g.indices(), oi)
+
+
 def test_argument_errors():
     lib = _ffi.load()
     out = _ffi.RTBvh()

@@ -106,3 +106,16 @@ def test_leaf_size_and_depth():
     same = np.tile(tris[:1], (64, 1, 1))
     nodes, idx = oracle.build_spatial(same, fixes=oracle.SPATIAL_FIX_ALL)
     assert oracle.validate(nodes, idx, 64)
+
+
+def test_reference_panics_in_the_equal_count_fallback():
+    # :643-658: with every reference on the left and none straddling,
+    # left_end = left_count / 2 ignores the task's begin; below begin the
+    # next slice panics. Thin triangles on three planes reach it; the
+    # corrected builder references every primitive.
+    for seed, n in ((32, 40), (87, 40), (261, 120)):
+        tris = scenes.plane_slivers(n, seed)
+        with pytest.raises(oracle.OracleError, match="panics"):
+            oracle.build_spatial(tris, fixes=0)
+        oracle.build_spatial(tris, fixes=oracle.SPATIAL_FIX_FALLBACK)  # no panic
+        assert oracle.validate(*oracle.build_spatial(tris, fixes=oracle.SPATIAL_FIX_ALL), n)
