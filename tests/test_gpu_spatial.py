@@ -209,6 +209,32 @@ def test_panicking_inputs_return_error():
         assert np.array_equal(u32(g.nodes()), u32(on)) and np.array_equal(g.indices(), oi)
 
 
+def _degenerate(kind):
+    t = scenes.incoherent(50, seed=3)
+    if kind == "identical_64":
+        return np.tile(t[:1], (64, 1, 1))
+    if kind == "collinear":
+        return np.stack([t[:, 0], t[:, 1], t[:, 0] + 2 * (t[:, 1] - t[:, 0])], 1).astype(np.float32)
+    if kind == "single":
+        return t[:1].copy()
+    return np.repeat(t[:, :1], 3, axis=1).astype(np.float32)  # all three vertices equal
+
+
+@pytest.mark.parametrize("fixes", FIXES)
+@pytest.mark.parametrize("kind", ["identical_64", "collinear", "single", "points"])
+def test_degenerate_inputs(kind, fixes):
+    tris = _degenerate(kind)
+    try:
+        on, oi = oracle.build_spatial(tris, fixes=fixes)
+    except oracle.OracleError:
+        with pytest.raises(rb.RtbvhError) as e:
+            gpu_spatial(tris, fixes)
+        assert e.value.code == rb.ResultCode.Error
+        return
+    g = gpu_spatial(tris, fixes)
+    assert np.array_equal(u32(g.nodes()), u32(on)) and np.array_equal(g.indices(), oi)
+
+
 def test_argument_errors():
     lib = _ffi.load()
     out = _ffi.RTBvh()
