@@ -299,9 +299,12 @@ ResultCode rtbvh_gpu_bvh_candidates(RTBvh bvh, const float *rays, const float *t
                                     uint32_t max_per_ray, uint32_t *candidates, uint32_t *counts,
                                     rtbvh_stream_t stream);
 
-/* Same as rtbvh_gpu_intersect_mbvh with HOST rays / t_max / hits: copies in,
- * traces and copies out in chunks on two internal streams, and returns when
- * the hits are in host memory. Page-locked host buffers give full speed. */
+/* Same as rtbvh_gpu_intersect_mbvh with HOST rays / t_max / hits, returning
+ * when the hits are in host memory. When every buffer is page-locked and
+ * mapped for the device (cudaHostAlloc / cudaMallocHost / pinned tensors)
+ * the traversal reads the rays and writes the hits in host memory itself;
+ * otherwise it copies in, traces and copies out in chunks on two internal
+ * streams. */
 ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float *rays, const float *t_max, uintptr_t ray_count,
                                       float *hits, uint32_t flags);
 

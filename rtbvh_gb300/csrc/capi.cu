@@ -926,6 +926,17 @@ static size_t next_chunk(size_t done, size_t remaining) {
   return remaining - M;
 }
 
+// Device address of page-locked host memory the GPU can read and write
+// directly (pinned and mapped into the device's address space), else NULL.
+static const void* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (p == nullptr || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
                                       float* hits, uint32_t flags) {
   if (ray_count == 0) return Ok;
@@ -936,6 +947,21 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
     cudaStreamCreateWithFlags(&streams[0], cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&streams[1], cudaStreamNonBlocking);
   });
+  cudaError_t e;
+  // Pinned, mapped host buffers: the traversal reads the rays and writes the
+  // hits in host memory itself (40 bytes per ray over the CPU-GPU link,
+  // overlapped with the walk), no staging copies.
+  {
+    const float* dr = static_cast<const float*>(mapped_host(rays));
+    float* dh = static_cast<float*>(const_cast<void*>(mapped_host(hits)));
+    const float* dt = t_max ? static_cast<const float*>(mapped_host(t_max)) : nullptr;
+    if (dr && dh && (t_max == nullptr || dt)) {
+      ResultCode rc = trace_common(mbvh.id, true, dr, dt, ray_count, dh, flags & ~RTBVH_TRACE_STATS, nullptr,
+                                   streams[0]);
+      if ((e = cudaStreamSynchronize(streams[0]))) return cuda_rc(e);
+      return rc;
+    }
+  }
   size_t per = 0;
   for (size_t done = 0; done < ray_count;) {
     const size_t c = next_chunk(done, ray_count - done);
@@ -944,7 +970,6 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
   }
   Scratch<float> d_rays[2], d_tmax[2];
   Scratch<float4> d_hits[2];
-  cudaError_t e;
   for (int k = 0; k < 2; ++k) {
     if ((e = d_rays[k].alloc(6 * per, streams[k])) || (e = d_hits[k].alloc(per, streams[k]))) return cuda_rc(e);
     if (t_max && (e = d_tmax[k].alloc(per, streams[k]))) return cuda_rc(e);

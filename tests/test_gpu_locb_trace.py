@@ -122,6 +122,31 @@ def test_host_buffer_entry_matches_device_entry(count):
     assert np.array_equal(u32(host_a), u32(dev_a.cpu().numpy()))
 
 
+def test_pinned_host_buffers_are_traced_in_place():
+    # page-locked host buffers: the traversal reads rays and writes hits in
+    # host memory directly; mixed (pinned rays, pageable hits) takes the
+    # staged copies; both equal the device entry
+    tris = scene("incoherent_20k")
+    m = rb.Mbvh.construct(gpu_build(tris, "locb"))
+    rays, tmax = scenes.incoherent_rays(2_000_000, seed=19)
+    lib = _ffi.load()
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_tmax = torch.from_numpy(tmax).pin_memory()
+    for any_hit in (False, True):
+        dev, _ = m.intersect(to_cuda(rays), t_max=to_cuda(tmax) if any_hit else None, any_hit=any_hit)
+        want = u32(dev.cpu().numpy())
+        flags = _ffi.TRACE_ANY_HIT if any_hit else 0
+        tptr = ctypes.c_void_p(h_tmax.data_ptr()) if any_hit else None
+        h_hits = torch.empty((len(rays), 4), dtype=torch.float32).pin_memory()
+        assert lib.rtbvh_intersect_mbvh_batch(m.handle, ctypes.c_void_p(h_rays.data_ptr()), tptr, len(rays),
+                                              ctypes.c_void_p(h_hits.data_ptr()), flags) == 0
+        assert np.array_equal(u32(h_hits.numpy()), want)
+        pageable = np.empty((len(rays), 4), np.float32)
+        assert lib.rtbvh_intersect_mbvh_batch(m.handle, ctypes.c_void_p(h_rays.data_ptr()), tptr, len(rays),
+                                              pageable.ctypes.data_as(ctypes.c_void_p), flags) == 0
+        assert np.array_equal(u32(pageable), want)
+
+
 def test_legacy_c_abi_roundtrip(lib):
     # create_bvh / create_mbvh / intersect_mbvh / free_* with host inputs,
     # as a C caller of the reference uses them
