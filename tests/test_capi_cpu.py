@@ -63,7 +63,17 @@ def test_create_bvh_argument_errors(lib):
     for stride in (8, 13, 20):  # the reference aborts; this library reports Error
         assert lib.create_bvh(None, 27, cp, stride, 1, 1, ctypes.byref(out)) == _ffi.ResultCode.Error
     assert lib.create_bvh(None, 0, cp, 16, 1, 1, ctypes.byref(out)) == _ffi.ResultCode.NoPrimitives
+    # create_spatial_Bvh (rtbvh_ffi/src/lib.rs:345-389): no vertices, no
+    # centres (the wrapper dereferences both), a stride that is not a
+    # multiple of 4 (assert_eq! in the reference), no primitives
+    vp = np.zeros((27, 3, 4), np.float32).ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     assert lib.create_spatial_Bvh(None, 27, cp, 16, None, 0, 0, 1, ctypes.byref(out)) == _ffi.ResultCode.Error
+    assert lib.create_spatial_Bvh(None, 27, None, 16, vp, 16, 48, 1, ctypes.byref(out)) == _ffi.ResultCode.Error
+    assert lib.create_spatial_Bvh(None, 27, cp, 14, vp, 16, 48, 1, ctypes.byref(out)) == _ffi.ResultCode.Error
+    assert lib.create_spatial_Bvh(None, 27, cp, 16, vp, 16, 48, 1, None) == _ffi.ResultCode.Error
+    assert lib.create_spatial_Bvh(None, 0, cp, 16, vp, 16, 48, 1, ctypes.byref(out)) == _ffi.ResultCode.NoPrimitives
+    assert lib.rtbvh_gpu_create_spatial_bvh(None, 0, None, None, 0, 1, 0, 0, None,
+                                            ctypes.byref(out)) == _ffi.ResultCode.NoPrimitives
 
 
 def test_create_mbvh_and_refit_null_checks(lib):
