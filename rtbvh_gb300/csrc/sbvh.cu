@@ -608,32 +608,76 @@ __device__ void sb_spatial_search(const SbArgs& A, SbShared& sh, uint32_t begin,
         atomicAdd(&sh.u.bins.exit[(A.fixes & kFixExitBin) ? last : first], 1u);
       }
       __syncthreads();
-      if (threadIdx.x == 0) {
-        SbBox suffix[kSbBins];
-        SbBox cur = sb_empty();
-        for (int b = kSbBins; b > 0; --b) {
-          sb_grow(cur, sb_bin_box(sh, b - 1));
-          suffix[b - 1] = cur;
+      if (threadIdx.x < 32) {
+        // the 15-boundary sweep of :557-576 with one bin per lane: suffix
+        // unions (the reference overwrites the bins with them), the left
+        // boxes as unions of bins or of suffixes 0..i, counts as prefix
+        // sums, then the first strict minimum below the incoming cost
+        const int l = threadIdx.x;
+        const bool in = l < kSbBins;
+        const SbBox bin = in ? sb_bin_box(sh, l) : sb_empty();
+        SbBox suf = bin;
+#pragma unroll
+        for (int o = 1; o < kSbBins; o <<= 1) {
+          SbBox y;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            y.mn[k] = __shfl_down_sync(0xffffffffu, suf.mn[k], o);
+            y.mx[k] = __shfl_down_sync(0xffffffffu, suf.mx[k], o);
+          }
+          if (l + o < kSbBins) sb_grow(suf, y);
         }
-        uint32_t left_count = 0, right_count = end - begin;
-        cur = sb_empty();
-        uint32_t found = 0;
-        for (int b = 0; b < kSbBins - 1; ++b) {
-          left_count += sh.u.bins.entry[b];
-          right_count -= sh.u.bins.exit[b];
-          sb_grow(cur, (A.fixes & kFixSweepBox) ? sb_bin_box(sh, b) : suffix[b]);
-          const float cost = (float)left_count * sb_half_area(cur) + (float)right_count * sb_half_area(suffix[b + 1]);
-          if (cost < sh.sp_cost) {
-            sh.sp_cost = cost;
-            sh.sp_axis = ax;
-            sh.sp_pos = mn + (float)(b + 1) * bin_size;
-            found = 1;
+        SbBox lb = (A.fixes & kFixSweepBox) ? bin : suf;
+        uint32_t ent = in ? sh.u.bins.entry[l] : 0u, ext = in ? sh.u.bins.exit[l] : 0u;
+#pragma unroll
+        for (int o = 1; o < kSbBins; o <<= 1) {
+          SbBox y;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            y.mn[k] = __shfl_up_sync(0xffffffffu, lb.mn[k], o);
+            y.mx[k] = __shfl_up_sync(0xffffffffu, lb.mx[k], o);
+          }
+          const uint32_t ye = __shfl_up_sync(0xffffffffu, ent, o), yx = __shfl_up_sync(0xffffffffu, ext, o);
+          if (l >= o) {
+            sb_grow(lb, y);
+            ent += ye;
+            ext += yx;
           }
         }
-        sh.found = found;
-        if (found) {
-          sh.pass_lo = sh.sp_pos - bin_size;
-          sh.pass_hi = sh.sp_pos + bin_size;
+        SbBox rbox;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          rbox.mn[k] = __shfl_down_sync(0xffffffffu, suf.mn[k], 1);
+          rbox.mx[k] = __shfl_down_sync(0xffffffffu, suf.mx[k], 1);
+        }
+        const float incoming = sh.sp_cost;
+        float cost = FLT_MAX;
+        bool ok = false;
+        if (l < kSbBins - 1) {
+          cost = (float)ent * sb_half_area(lb) + (float)((end - begin) - ext) * sb_half_area(rbox);
+          ok = cost < incoming;
+        }
+        float bc = ok ? cost : FLT_MAX;
+        int bl = ok ? l : 64;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float c2 = __shfl_xor_sync(0xffffffffu, bc, o);
+          const int l2 = __shfl_xor_sync(0xffffffffu, bl, o);
+          if (l2 < 64 && (bl == 64 || c2 < bc || (c2 == bc && l2 < bl))) {
+            bc = c2;
+            bl = l2;
+          }
+        }
+        if (l == 0) {
+          const uint32_t found = bl < 64 ? 1u : 0u;
+          if (found) {
+            sh.sp_cost = bc;
+            sh.sp_axis = ax;
+            sh.sp_pos = mn + (float)(bl + 1) * bin_size;
+            sh.pass_lo = sh.sp_pos - bin_size;
+            sh.pass_hi = sh.sp_pos + bin_size;
+          }
+          sh.found = found;
         }
       }
       __syncthreads();
