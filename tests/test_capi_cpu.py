@@ -103,6 +103,13 @@ def test_python_builder_errors():
     with pytest.raises(rb.BuildError) as e:
         rb.Builder(aabbs=np.zeros((0, 8), np.float32), primitives=rb.Points(np.zeros((1, 3)))).construct_binned_sah()
     assert e.value == rb.BuildError.InequalAabbsAndPrimitives(0, 1)
+    # construct_spatial_sah (src/bvh.rs:59-85): no primitives first; the
+    # builder needs SpatialTriangle primitives
+    with pytest.raises(rb.BuildError) as e:
+        rb.Builder(primitives=None).construct_spatial_sah()
+    assert e.value == rb.BuildError.NoPrimitives()
+    with pytest.raises(TypeError):
+        rb.Builder(primitives=rb.Points(np.zeros((4, 3)))).construct_spatial_sah()
 
 
 class _UserData(ctypes.Structure):
