@@ -40,7 +40,7 @@ def lib():
         L.ror_spatial_max_refs.argtypes = [ctypes.c_size_t]
         L.ror_spatial_max_refs.restype = ctypes.c_uint64
         L.ror_build_spatial.argtypes = [f32p, f32p, f32p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32,
-                                        f32p, ctypes.c_size_t, u32p, ctypes.c_size_t]
+                                        ctypes.c_size_t, f32p, ctypes.c_size_t, u32p, ctypes.c_size_t]
         L.ror_build_spatial.restype = ctypes.c_int64
         L.ror_mbvh.argtypes = [f32p, ctypes.c_size_t, f32p]
         L.ror_mbvh.restype = ctypes.c_int64
@@ -151,10 +151,12 @@ def spatial_max_refs(n: int) -> int:
     return int(lib().ror_spatial_max_refs(n))
 
 
-def build_spatial(tris, aabbs=None, centers=None, prims_per_leaf: int = 1, fixes: int = 0):
+def build_spatial(tris, aabbs=None, centers=None, prims_per_leaf: int = 1, fixes: int = 0, spawn_threshold: int = 0):
     """Spatial-split SAH build (src/builders/spatial_sah.rs). Returns (nodes
     (m,8) float32, prim_indices (max_refs,) uint32, the reference's full
-    index vector). Raises OracleError where the reference panics."""
+    index vector). Raises OracleError where the reference panics.
+    spawn_threshold > 0 runs the reference's threading (1024 in the
+    reference) with the same output."""
     t = _c(tris, np.float32).reshape(-1, 9)
     n = len(t)
     if n == 0:
@@ -168,7 +170,8 @@ def build_spatial(tris, aabbs=None, centers=None, prims_per_leaf: int = 1, fixes
     mr = spatial_max_refs(n)
     nodes = np.zeros((2 * mr + 1, 8), np.float32)
     idx = np.zeros(mr, np.uint32)
-    m = lib().ror_build_spatial(_f(a), _f(c), _f(t), n, prims_per_leaf, fixes, _f(nodes), len(nodes), _u(idx), len(idx))
+    m = lib().ror_build_spatial(_f(a), _f(c), _f(t), n, prims_per_leaf, fixes, spawn_threshold, _f(nodes), len(nodes),
+                                _u(idx), len(idx))
     if m == -3:
         raise OracleError("the reference panics on this input")
     if m < 0:

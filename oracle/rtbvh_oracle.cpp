@@ -1162,15 +1162,23 @@ struct SpatialBuild {
   uint32_t fixes = 0;
   float threshold = 0.0f;
   std::vector<BvhNode> nodes;
-  size_t node_count = 1;
+  std::atomic<size_t> node_count{1};   // AtomicNodeStack's counter
   std::vector<uint32_t> prim_indices;
-  size_t ref_counter = 0;
+  std::atomic<size_t> ref_counter{0};  // make_leaf's reference_count
   std::vector<Aabb> acc;
   std::vector<SRef> refs[3];
-  std::vector<uint8_t> marks;
-  int err = 0;  // 1: the reference panics or writes out of bounds here
+  std::vector<size_t> work;  // work_size() of the WorkItem each node was created with
+  std::atomic<int> err{0};   // 1: the reference panics or writes out of bounds here
   const float* tri(uint32_t p) const { return tris + 9 * (size_t)p; }
 };
+
+// reference_marks of apply_object_split, one array per thread (the
+// reference allocates one per call; all entries are false between calls).
+std::vector<uint8_t>& sb_marks(size_t size) {
+  thread_local std::vector<uint8_t> marks;
+  if (marks.size() < size) marks.assign(size, 0);
+  return marks;
+}
 
 // spatial_sah.rs:314-368
 ObjSplit sb_find_object_split(SpatialBuild& b, size_t begin, size_t end, bool sorted) {
@@ -1276,9 +1284,8 @@ SpSplit sb_find_spatial_split(SpatialBuild& b, const SWork& w) {
 // spatial_sah.rs:370-438
 bool sb_allocate_children(SpatialBuild& b, const SWork& w, size_t right_begin, size_t right_end, const Aabb& left_box,
                           const Aabb& right_box, bool sorted, SWork& lw, SWork& rw) {
-  if (b.node_count + 1 >= b.nodes.size()) { b.err = 1; return false; }  // AtomicNodeStack::allocate -> None
-  const size_t left = b.node_count;
-  b.node_count += 2;
+  const size_t left = b.node_count.fetch_add(2);
+  if (left + 1 >= b.nodes.size()) { b.err = 1; return false; }  // AtomicNodeStack::allocate -> None
   BvhNode& parent = b.nodes[w.node];
   parent.extra2 = (int32_t)left;
   parent.extra1 = -1;
@@ -1301,6 +1308,8 @@ bool sb_allocate_children(SpatialBuild& b, const SWork& w, size_t right_begin, s
   lw = SWork{left, w.begin, right_begin, fix ? right_begin + lsc : right_begin, w.depth + 1, sorted};
   rw = fix ? SWork{left + 1, right_begin + lsc, right_end + lsc, w.split_end, w.depth + 1, sorted}
            : SWork{left + 1, right_begin, right_end, w.split_end, w.depth + 1, sorted};
+  b.work[left] = lw.end - lw.begin;
+  b.work[left + 1] = rw.end - rw.begin;
   return true;
 }
 
@@ -1309,16 +1318,17 @@ bool sb_apply_object_split(SpatialBuild& b, const SWork& w, const ObjSplit& spli
   const size_t s = (size_t)split.index;
   if (split.index < (int64_t)w.begin || s >= w.end) { b.err = 1; return false; }  // assert!
   std::vector<SRef>& r = b.refs[split.axis];
-  for (size_t i = w.begin; i < s; ++i) b.marks[r[i].prim] = 1;
-  for (size_t i = s; i < w.end; ++i) b.marks[r[i].prim] = 0;
+  std::vector<uint8_t>& marks = sb_marks(b.max_ref);
+  for (size_t i = w.begin; i < s; ++i) marks[r[i].prim] = 1;
+  for (size_t i = s; i < w.end; ++i) marks[r[i].prim] = 0;
   // sort_by with "Less exactly when a is marked and b is not": a stable
   // partition, marked references first.
   for (int o = 1; o <= 2; ++o) {
     std::vector<SRef>& q = b.refs[(split.axis + o) % 3];
-    std::stable_partition(q.begin() + w.begin, q.begin() + w.end, [&b](const SRef& x) { return b.marks[x.prim] != 0; });
+    std::stable_partition(q.begin() + w.begin, q.begin() + w.end, [&marks](const SRef& x) { return marks[x.prim] != 0; });
   }
   for (int axis = 0; axis < 3; ++axis)  // the reference allocates fresh marks per call
-    for (size_t i = w.begin; i < w.end; ++i) b.marks[b.refs[axis][i].prim] = 0;
+    for (size_t i = w.begin; i < w.end; ++i) marks[b.refs[axis][i].prim] = 0;
   return sb_allocate_children(b, w, s, w.end, split.left, split.right, true, lw, rw);
 }
 
@@ -1391,8 +1401,7 @@ bool sb_apply_spatial_split(SpatialBuild& b, const SWork& w, const SpSplit& spli
 // make_leaf, spatial_sah.rs:733-744
 void sb_make_leaf(SpatialBuild& b, const SWork& w) {
   const size_t count = w.end - w.begin;
-  const size_t first = b.ref_counter;
-  b.ref_counter += count;
+  const size_t first = b.ref_counter.fetch_add(count);
   if (first + count > b.max_ref) { b.err = 1; return; }
   for (size_t i = 0; i < count; ++i) b.prim_indices[first + i] = b.refs[0][w.begin + i].prim;
   b.nodes[w.node].extra2 = (int32_t)first;
@@ -1445,7 +1454,7 @@ void build_spatial(SpatialBuild& b, const Aabb* aabbs, const V3* centers) {
   b.nodes.assign(2 * b.max_ref + 1, node_new());
   b.prim_indices.assign(b.max_ref, 0u);
   b.acc.assign(b.max_ref, aabb_new());
-  b.marks.assign(b.max_ref, 0);
+  b.work.assign(2 * b.max_ref + 1, 0);
   for (int axis = 0; axis < 3; ++axis) {
     b.refs[axis].assign(b.max_ref, SRef{aabb_new(), v3(0.0f, 0.0f, 0.0f), 0u});
     for (size_t i = 0; i < n; ++i) b.refs[axis][i] = SRef{aabbs[i], centers[i], (uint32_t)i};
@@ -1454,6 +1463,7 @@ void build_spatial(SpatialBuild& b, const Aabb* aabbs, const V3* centers) {
   b.threshold = kSbAlpha * 2.0f * aabb_half_area(root);
   b.node_count = 1;
   b.nodes[0] = root;
+  b.work[0] = n;
   std::vector<SWork> stack{SWork{0, 0, n, b.max_ref, 0, false}};
   while (!stack.empty() && !b.err) {
     SWork w = stack.back();
@@ -1465,7 +1475,92 @@ void build_spatial(SpatialBuild& b, const Aabb* aabbs, const V3* centers) {
       stack.push_back(a);
     }
   }
+  if (!b.err) b.nodes.resize(b.node_count);
+}
+
+// TaskSpawner::run_task (src/utils.rs:246-283): the child with more
+// references goes to a new thread when it has more than `threshold` of
+// them, else onto this thread's stack after the other one; spawned threads
+// are joined at the end. Tasks touch disjoint reference ranges and fresh
+// nodes, so they run concurrently; numbers and leaf ranges come out in
+// thread-timing order and sb_canonical renumbers them.
+void sb_run_task_threads(SpatialBuild& b, SWork root, size_t threshold) {
+  std::vector<std::thread> spawned;
+  std::vector<SWork> stack{root};
+  while (!stack.empty() && !b.err) {
+    SWork w = stack.back();
+    stack.pop_back();
+    SWork a, c;
+    if (sb_run(b, w, a, c)) {
+      if (a.end - a.begin < c.end - c.begin) std::swap(a, c);
+      stack.push_back(c);
+      if (a.end - a.begin <= threshold) {
+        stack.push_back(a);
+        continue;
+      }
+      spawned.emplace_back([&b, a, threshold]() { sb_run_task_threads(b, a, threshold); });
+    }
+  }
+  for (auto& t : spawned) t.join();
+}
+
+// Renumbers a finished tree in the single-thread order of build_spatial:
+// node pairs handed out in pre-order with the child of larger work first,
+// leaf index ranges in the same order.
+void sb_canonical(SpatialBuild& b) {
+  std::vector<BvhNode> out(b.node_count);
+  std::vector<uint32_t> idx(b.max_ref, 0u);
+  std::vector<std::pair<size_t, size_t>> stack{{0, 0}};  // (old id, new id)
+  size_t next_pair = 1, next_ref = 0;
+  while (!stack.empty()) {
+    const std::pair<size_t, size_t> top = stack.back();
+    stack.pop_back();
+    BvhNode nd = b.nodes[top.first];
+    if (nd.extra1 < 0) {
+      const size_t old_left = (size_t)nd.extra2, pair = next_pair;
+      next_pair += 2;
+      nd.extra2 = (int32_t)pair;
+      size_t a = old_left, c = old_left + 1, na = pair, nc = pair + 1;
+      if (b.work[a] < b.work[c]) {
+        std::swap(a, c);
+        std::swap(na, nc);
+      }
+      stack.push_back({c, nc});
+      stack.push_back({a, na});
+    } else {
+      const size_t count = (size_t)nd.extra1, first = (size_t)nd.extra2;
+      for (size_t k = 0; k < count; ++k) idx[next_ref + k] = b.prim_indices[first + k];
+      nd.extra2 = (int32_t)next_ref;
+      next_ref += count;
+    }
+    out[top.second] = nd;
+  }
+  b.nodes.swap(out);
+  b.prim_indices.swap(idx);
+}
+
+// build_spatial with the reference's threading (spawn_threshold references:
+// 1024 in TaskSpawner::new), numbered afterwards as build_spatial numbers.
+void build_spatial_threads(SpatialBuild& b, const Aabb* aabbs, const V3* centers, size_t spawn_threshold) {
+  const size_t n = b.n;
+  b.max_ref = n + (size_t)rs_f32_to_usize((float)n * kSbSplitFactor);
+  b.nodes.assign(2 * b.max_ref + 1, node_new());
+  b.prim_indices.assign(b.max_ref, 0u);
+  b.acc.assign(b.max_ref, aabb_new());
+  b.work.assign(2 * b.max_ref + 1, 0);
+  for (int axis = 0; axis < 3; ++axis) {
+    b.refs[axis].assign(b.max_ref, SRef{aabb_new(), v3(0.0f, 0.0f, 0.0f), 0u});
+    for (size_t i = 0; i < n; ++i) b.refs[axis][i] = SRef{aabbs[i], centers[i], (uint32_t)i};
+  }
+  const Aabb root = aabb_union_of_list(aabbs, n);
+  b.threshold = kSbAlpha * 2.0f * aabb_half_area(root);
+  b.node_count = 1;
+  b.nodes[0] = root;
+  b.work[0] = n;
+  sb_run_task_threads(b, SWork{0, 0, n, b.max_ref, 0, false}, spawn_threshold);
+  if (b.err) return;
   b.nodes.resize(b.node_count);
+  sb_canonical(b);
 }
 
 void load_aabbs(const float* raw, size_t n, std::vector<Aabb>& out) {
@@ -1578,7 +1673,9 @@ int64_t ror_build(const float* aabbs, const float* centers, size_t n, size_t pri
 }
 
 // Spatial-split SAH (src/builders/spatial_sah.rs; see build_spatial for the
-// task order). tris: n x 9 vertices, aabbs: n x 8, centers: n x 3. nodes_out
+// task order). spawn_threshold: 0 = one thread, else TaskSpawner's
+// threading with that threshold (same output). tris: n x 9 vertices,
+// aabbs: n x 8, centers: n x 3. nodes_out
 // holds nodes_cap nodes (2 * max_refs + 1 suffice), idx_out idx_cap entries
 // (max_refs: the reference returns all of them, unused ones 0). Returns the
 // node count, -2 no primitives, -3 an input on which the reference panics or
@@ -1586,7 +1683,8 @@ int64_t ror_build(const float* aabbs, const float* centers, size_t n, size_t pri
 uint64_t ror_spatial_max_refs(size_t n) { return n + rs_f32_to_usize((float)n * kSbSplitFactor); }
 
 int64_t ror_build_spatial(const float* aabbs, const float* centers, const float* tris, size_t n, size_t prims_per_leaf,
-                          uint32_t fixes, float* nodes_out, size_t nodes_cap, uint32_t* idx_out, size_t idx_cap) {
+                          uint32_t fixes, size_t spawn_threshold, float* nodes_out, size_t nodes_cap, uint32_t* idx_out,
+                          size_t idx_cap) {
   if (n == 0) return -2;
   std::vector<Aabb> a;
   std::vector<V3> c;
@@ -1597,7 +1695,8 @@ int64_t ror_build_spatial(const float* aabbs, const float* centers, const float*
   b.n = n;
   b.max_leaf = prims_per_leaf == 0 ? 1 : prims_per_leaf;
   b.fixes = fixes;
-  build_spatial(b, a.data(), c.data());
+  if (spawn_threshold == 0) build_spatial(b, a.data(), c.data());
+  else build_spatial_threads(b, a.data(), c.data(), spawn_threshold);
   if (b.err) return -3;
   if (b.nodes.size() > nodes_cap || b.prim_indices.size() > idx_cap) return -4;
   std::memcpy(nodes_out, b.nodes.data(), b.nodes.size() * sizeof(BvhNode));

@@ -119,3 +119,18 @@ def test_reference_panics_in_the_equal_count_fallback():
             oracle.build_spatial(tris, fixes=0)
         oracle.build_spatial(tris, fixes=oracle.SPATIAL_FIX_FALLBACK)  # no panic
         assert oracle.validate(*oracle.build_spatial(tris, fixes=oracle.SPATIAL_FIX_ALL), n)
+
+
+@pytest.mark.parametrize("fixes", [0, oracle.SPATIAL_FIX_ALL])
+def test_threaded_build_equals_the_single_thread_order(golden, fixes):
+    # TaskSpawner's threading (a thread per task above the threshold, here
+    # also far below the reference's 1024 to run many at once), renumbered
+    # afterwards: the same nodes and indices as the single-thread build
+    cases = [golden["teapot"], scenes.incoherent(20000, seed=1), scenes.slivers(3000, seed=5, length=0.5)]
+    for tris in cases:
+        want = oracle.build_spatial(tris, fixes=fixes)
+        for threshold in (8, 64, 1024):
+            for _ in range(2):
+                got = oracle.build_spatial(tris, fixes=fixes, spawn_threshold=threshold)
+                assert np.array_equal(got[0].view(np.uint32), want[0].view(np.uint32))
+                assert np.array_equal(got[1], want[1])
