@@ -375,17 +375,22 @@ ResultCode rtbvh_deserialize_mbvh(const uint8_t *buffer, uintptr_t size, uint32_
  * memory while they run, such as a per-frame animation loop that must not
  * call cudaMalloc (it can synchronise the device or fail mid-frame). It
  * allocates nothing: its scratch is a fixed array inside the library
- * (8 MiB + 256 bytes, reserved on every GPU that loads the library until
- * the process exits).
+ * (8 MiB + 256 bytes). The array is reserved on a GPU when the library's
+ * code is first used there -- with CUDA's lazy module loading at the latest
+ * on the first call -- and stays reserved until the process exits.
  * - Updates the Bvh's device nodes only, asynchronously on `stream`; the
  *   host mirror behind the handle's node pointer and any Mbvh made from the
  *   Bvh are left as they were.
  * - Trees with more than RTBVH_REFIT_NOALLOC_MAX_NODES nodes are rejected
  *   with InvalidArgument before anything runs.
+ * - A tree whose leaves index past the Bvh's index or primitive counts is
+ *   not read out of bounds; the error is recorded in the Bvh's status word,
+ *   which rtbvh_gpu_status reports (Error) once the stream has run.
  * - The first call on a device looks up the array's device address, so make
  *   that first call before any stream capture.
  * - All calls share the one array: calls that can overlap on the GPU (other
- *   streams, other host threads) race and must be serialised by the caller. */
+ *   streams, other host threads) race and must be serialised by the caller.
+ *   The Bvh must not be freed while a call on it can still be running. */
 ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb *aabbs, rtbvh_stream_t stream);
 
 /* Backward pass of the closest-hit triangle test for rays traced with
@@ -445,6 +450,10 @@ typedef struct RTBatchTuning {
   uint32_t trace_ray_batch;     /* rays a warp takes from the global ray counter at a time (default 128, at most 4096) */
   uint32_t cluster_min_prims;   /* meshes with more primitives get a thread-block cluster (default 4096) */
   float pipeline_ms;            /* tune: measured build + trace time with the chosen values */
+  uint32_t trace_stack;         /* stack entries per ray of the closest-hit walk: 32, 48 or 64
+                                   (0 in set_tuning: 64); a ray that needs more reports prim -2
+                                   and StackOverflow (the reference's stack holds 32,
+                                   src/iter_indices.rs:22) */
 } RTBatchTuning;
 /* Times candidate values on this batch's own meshes and rays (the pipeline
  * runs several times on `stream`, overwriting the hits), keeps the fastest

@@ -84,7 +84,8 @@ class RTGpuBatchView(ctypes.Structure):
 
 class RTBatchTuning(ctypes.Structure):
     _fields_ = [("trace_blocks_per_sm", ctypes.c_uint32), ("trace_ray_batch", ctypes.c_uint32),
-                ("cluster_min_prims", ctypes.c_uint32), ("pipeline_ms", ctypes.c_float)]
+                ("cluster_min_prims", ctypes.c_uint32), ("pipeline_ms", ctypes.c_float),
+                ("trace_stack", ctypes.c_uint32)]
 
 
 class RTGpuView(ctypes.Structure):

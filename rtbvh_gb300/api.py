@@ -549,17 +549,18 @@ class Batch:
         t = _ffi.RTBatchTuning()
         check(self._lib.rtbvh_gpu_batch_tune(self._b, _stream(stream), ctypes.byref(t)), "batch_tune")
         return {"trace_blocks_per_sm": t.trace_blocks_per_sm, "trace_ray_batch": t.trace_ray_batch,
-                "cluster_min_prims": t.cluster_min_prims, "pipeline_ms": t.pipeline_ms}
+                "cluster_min_prims": t.cluster_min_prims, "trace_stack": t.trace_stack,
+                "pipeline_ms": t.pipeline_ms}
 
     @property
     def tuning(self):
         t = _ffi.RTBatchTuning()
         check(self._lib.rtbvh_gpu_batch_get_tuning(self._b, ctypes.byref(t)), "batch_get_tuning")
         return {"trace_blocks_per_sm": t.trace_blocks_per_sm, "trace_ray_batch": t.trace_ray_batch,
-                "cluster_min_prims": t.cluster_min_prims}
+                "cluster_min_prims": t.cluster_min_prims, "trace_stack": t.trace_stack}
 
-    def set_tuning(self, trace_blocks_per_sm=0, trace_ray_batch=0, cluster_min_prims=0, stream=None):
-        t = _ffi.RTBatchTuning(trace_blocks_per_sm, trace_ray_batch, cluster_min_prims, 0.0)
+    def set_tuning(self, trace_blocks_per_sm=0, trace_ray_batch=0, cluster_min_prims=0, trace_stack=0, stream=None):
+        t = _ffi.RTBatchTuning(trace_blocks_per_sm, trace_ray_batch, cluster_min_prims, 0.0, trace_stack)
         check(self._lib.rtbvh_gpu_batch_set_tuning(self._b, ctypes.byref(t), _stream(stream)), "batch_set_tuning")
 
     def view(self):

@@ -156,7 +156,7 @@ struct Plan {
   DevBuf<uint32_t> cluster_sums;
   std::vector<uint32_t> sizes_in_order;  // host: primitive count of order[q]
   // launch parameters (RTBatchTuning; 0 = default)
-  uint32_t trace_blocks_per_sm = 0, trace_ray_batch = 0, cluster_min = kSegClusterMinPrims;
+  uint32_t trace_blocks_per_sm = 0, trace_ray_batch = 0, cluster_min = kSegClusterMinPrims, trace_stack = 0;
   cudaStream_t side = nullptr;  // small meshes' clustering runs here, forked from the main stream
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -248,6 +248,7 @@ cudaError_t run_trace(Plan& p, cudaStream_t s) {
     }
     a.blocks_per_sm = p.trace_blocks_per_sm;
     a.ray_batch = p.trace_ray_batch;
+    a.stack_limit = p.trace_stack;
     if ((e = launch_trace_mbvh(a, s))) return e;
   }
   return cudaGetLastError();
@@ -429,6 +430,7 @@ ResultCode rtbvh_gpu_batch_get_tuning(RTBatch batch, RTBatchTuning* result) {
   result->trace_ray_batch = p->trace_ray_batch;
   result->cluster_min_prims = p->cluster_min;
   result->pipeline_ms = 0.0f;
+  result->trace_stack = p->trace_stack ? p->trace_stack : 64u;
   return Ok;
 }
 
@@ -436,10 +438,13 @@ ResultCode rtbvh_gpu_batch_set_tuning(RTBatch batch, const RTBatchTuning* t, rtb
   Plan* p = find_plan(batch.id);
   if (!p || t == nullptr) return Error;
   if (t->trace_blocks_per_sm > 64 || t->trace_ray_batch > 4096u) return InvalidArgument;
+  if (t->trace_stack != 0 && t->trace_stack != 32 && t->trace_stack != 48 && t->trace_stack != 64)
+    return InvalidArgument;
   cudaError_t e;
   if ((e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream)))) return cuda_rc(e);
   p->trace_blocks_per_sm = t->trace_blocks_per_sm;
   p->trace_ray_batch = t->trace_ray_batch;
+  p->trace_stack = t->trace_stack;
   set_cluster_min(*p, t->cluster_min_prims ? t->cluster_min_prims : kSegClusterMinPrims);
   return cuda_rc(capture(*p));
 }
@@ -487,6 +492,32 @@ ResultCode rtbvh_gpu_batch_tune(RTBatch batch, rtbvh_stream_t stream, RTBatchTun
   }
   p->trace_blocks_per_sm = best_b;
   p->trace_ray_batch = best_r;
+  // 3. stack bound of the closest-hit walk (local memory per lane): the
+  // fastest of the bounds that no ray of this batch overflows. The status
+  // word is saved and restored around the trial runs, whose overflow bits
+  // only rate the candidates.
+  uint32_t best_st = 64u;
+  if (p->total_rays && !(p->flags & (RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_EXACT_NODES))) {
+    uint32_t prior = 0;
+    if ((e = cudaMemcpy(&prior, p->status.ptr, 4, cudaMemcpyDeviceToHost))) return cuda_rc(e);
+    static const uint32_t kStack[] = {32u, 48u, 64u};
+    best = 3.4e38f;
+    for (uint32_t st : kStack) {
+      p->trace_stack = st;
+      float ms;
+      uint32_t word = 0;
+      if ((e = cudaMemsetAsync(p->status.ptr, 0, 4, s)) ||
+          (e = time_ms([&] { return run_trace(*p, s); }, s, 2, &ms)) ||
+          (e = cudaMemcpy(&word, p->status.ptr, 4, cudaMemcpyDeviceToHost)))
+        return cuda_rc(e);
+      if (!(word & kStatusStackOverflow) && ms < best) {
+        best = ms;
+        best_st = st;
+      }
+    }
+    if ((e = cudaMemcpy(p->status.ptr, &prior, 4, cudaMemcpyHostToDevice))) return cuda_rc(e);
+  }
+  p->trace_stack = best_st;
   if ((e = capture(*p))) return cuda_rc(e);
   float total = 0.0f;
   if ((e = time_ms([&] { return cudaGraphLaunch(p->exec, s); }, s, 3, &total))) return cuda_rc(e);
@@ -495,6 +526,7 @@ ResultCode rtbvh_gpu_batch_tune(RTBatch batch, rtbvh_stream_t stream, RTBatchTun
     result->trace_ray_batch = best_r;
     result->cluster_min_prims = best_c;
     result->pipeline_ms = total;
+    result->trace_stack = best_st;
   }
   return Ok;
 }

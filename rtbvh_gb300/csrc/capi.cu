@@ -1143,21 +1143,15 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
 
 ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb* aabbs, rtbvh_stream_t stream) {
   if (aabbs == nullptr) return Error;
-  DAabb* nodes;
-  uint32_t node_count, prim_count, vertex_count;
-  const uint32_t* indices;
-  {
-    std::lock_guard<std::mutex> lock(g_mu);
-    Entry* b = lookup(bvh_id, false);
-    if (!b) return Error;
-    nodes = b->d_nodes;
-    node_count = b->node_count;
-    prim_count = b->prim_count;
-    vertex_count = b->vertex_count;
-    indices = b->d_indices;
-  }
-  return refit_bvh_noalloc(nodes, node_count, indices, prim_count, vertex_count, reinterpret_cast<const DAabb*>(aabbs),
-                           static_cast<cudaStream_t>(stream));
+  // The structure lock is held while the (asynchronous) work is queued, so a
+  // concurrent free_bvh cannot release the arrays in between; the queued
+  // kernels report index errors in the Bvh's own status word, which
+  // rtbvh_gpu_status reads.
+  std::lock_guard<std::mutex> lock(g_mu);
+  Entry* b = lookup(bvh_id, false);
+  if (!b) return Error;
+  return refit_bvh_noalloc(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count,
+                           reinterpret_cast<const DAabb*>(aabbs), b->d_status, static_cast<cudaStream_t>(stream));
 }
 
 ResultCode rtbvh_gpu_intersect_backward(const float* vertices, uintptr_t prim_count, const float* rays,

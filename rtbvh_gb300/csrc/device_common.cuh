@@ -49,8 +49,10 @@ static_assert(sizeof(DMNode) == 128, "DMNode must be 128 bytes");
 // children and counts are exact (counts as int16). A closest-hit traversal
 // over boxes that contain the reference's finds the same nearest triangle
 // (only its visit order, and so the winner among triangles hit at exactly
-// the same t, can differ). flags bit 0 (exps >> 24): values out of range,
-// read the exact node instead.
+// the same t, can differ). Flags (exps >> 24): kQFlagExact -- the bounds do
+// not fit the grid (or a count not int16), read the exact node instead;
+// kQFlagOutOfRange -- a bound beyond kCompactRange, the ray leaves the
+// compact walk and is traced again over the exact Mbvh.
 struct alignas(64) DQNode {
   float lo[3];
   uint32_t exps;          // biased exponents of the steps: x | y << 8 | z << 16 | flags << 24
@@ -60,7 +62,19 @@ struct alignas(64) DQNode {
   int16_t counts[4];
 };
 static_assert(sizeof(DQNode) == 64, "DQNode must be 64 bytes");
-constexpr float kQuantRange = 1e18f;  // larger box values (or ray origins / inverse directions) use exact nodes
+constexpr uint32_t kQFlagExact = 1u;
+constexpr uint32_t kQFlagOutOfRange = 2u;
+constexpr float kQuantRange = 1e18f;  // larger inverse-direction components use the exact nodes
+// Magnitude bound of the compact walk: ray origins and node bounds within
+// +-kCompactRange. Every leaf box of the trees that get a traversal tree is
+// its primitive's box grown by 1e-4, and below this magnitude the rounding of
+// a slab test, about 2^-23 * (|bound| + |origin|) <= 3.1e-5 in space, stays
+// well inside that margin: a box that holds a triangle hit by the ray passes
+// the test in both the compact (one fma per plane) and the exact (subtract,
+// multiply) arithmetic, and a box that one form rejects and the other keeps
+// holds no nearer hit. Beyond it the two forms can disagree on a box that
+// matters, so such rays and nodes use the exact Mbvh in the reference's order.
+constexpr float kCompactRange = 128.0f;
 
 // ------------------------------------------------------------- float helpers
 // Vec3::min / Vec3::max of the reference (Rust f32::min/max): NaN operands are

@@ -131,9 +131,10 @@ ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices,
                      uint32_t prim_count, const DAabb* aabbs, cudaStream_t s);
 
 // refit_bvh with its scratch in a static device array instead of per-call
-// allocations (see rtbvh_gpu_refit_noalloc). Asynchronous on `s`.
+// allocations (see rtbvh_gpu_refit_noalloc). Asynchronous on `s`; index
+// errors are ORed into *status (the structure's status word).
 ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                             uint32_t prim_count, const DAabb* aabbs, cudaStream_t s);
+                             uint32_t prim_count, const DAabb* aabbs, uint32_t* status, cudaStream_t s);
 
 // ------------------------------------------------------------------ traversal
 struct TraceArgs {
@@ -171,6 +172,11 @@ struct TraceArgs {
   const DMNode* qexact = nullptr;
   uint32_t q_count = 0;
   const uint32_t* seg_qroot = nullptr;
+  // Stack bound of the compact closest-hit walk: 32, 48 or 64 entries (0:
+  // 64). A ray that needs more reports prim -2 and kStatusStackOverflow.
+  uint32_t stack_limit = 0;
+  // Internal: the ray count is read from this device word (at most ray_count).
+  const unsigned int* ray_count_dev = nullptr;
 };
 cudaError_t launch_trace_mbvh(const TraceArgs& a, cudaStream_t s);
 cudaError_t launch_trace_bvh(const TraceArgs& a, cudaStream_t s);

@@ -450,15 +450,16 @@ ResultCode refit_bvh(DAabb* nodes, uint32_t node_count, const uint32_t* indices,
 // for example a renderer that refits every frame inside a region where it
 // is not allowed to call cudaMalloc (an allocation can synchronise the
 // device and can fail mid-frame). Its scratch (parent pointers, arrival
-// counters, a status word) lives in this file-scope array instead of being
-// allocated per call. The array is reserved on every GPU that loads the
-// library and stays reserved until the process exits.
+// counters) lives in this file-scope array instead of being allocated per
+// call; errors go to the Bvh's own status word. The array is reserved on a
+// GPU when this module is first used there (with lazy module loading, at
+// the latest on the first call) and stays reserved until the process exits.
 namespace rtbvh {
 
 namespace {
 
-constexpr uint32_t kNoAllocStatusWords = 64;  // 256 bytes, keeps the arrays 256-byte aligned
-static __device__ __align__(256) uint32_t g_refit_scratch[kNoAllocStatusWords + 2u * RTBVH_REFIT_NOALLOC_MAX_NODES];
+constexpr uint32_t kNoAllocHeadWords = 64;  // 256 bytes ahead of the arrays (unused), keeps them 256-byte aligned
+static __device__ __align__(256) uint32_t g_refit_scratch[kNoAllocHeadWords + 2u * RTBVH_REFIT_NOALLOC_MAX_NODES];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
@@ -485,20 +486,17 @@ cudaError_t noalloc_scratch(uint32_t** out) {
 }  // namespace
 
 ResultCode refit_bvh_noalloc(DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                             uint32_t prim_count, const DAabb* aabbs, cudaStream_t s) {
+                             uint32_t prim_count, const DAabb* aabbs, uint32_t* status, cudaStream_t s) {
   if (node_count == 0) return Ok;
   if (node_count > RTBVH_REFIT_NOALLOC_MAX_NODES) return InvalidArgument;
   uint32_t* base = nullptr;
   cudaError_t e = noalloc_scratch(&base);
   if (e != cudaSuccess) return cuda_rc(e);
-  uint32_t* status = base;
-  uint32_t* parent = base + kNoAllocStatusWords;
+  uint32_t* parent = base + kNoAllocHeadWords;
   uint32_t* arrive = parent + RTBVH_REFIT_NOALLOC_MAX_NODES;
   // The array keeps the previous call's contents: reset what must start
   // clean (k_parents zeroes the arrival counters itself).
-  if ((e = cudaMemsetAsync(parent, 0xff, (size_t)node_count * 4, s)) ||
-      (e = cudaMemsetAsync(status, 0, kNoAllocStatusWords * 4, s)))
-    return cuda_rc(e);
+  if ((e = cudaMemsetAsync(parent, 0xff, (size_t)node_count * 4, s))) return cuda_rc(e);
   const unsigned blocks = (node_count + kBlock - 1) / kBlock;
   k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent, arrive, status);
   k_refit<<<blocks, kBlock, 0, s>>>(nodes, node_count, indices, index_count, prim_count, aabbs, parent, arrive,
@@ -653,7 +651,14 @@ __global__ void __launch_bounds__(kBlock) k_quantize(const DMNode* __restrict__ 
     q.qx[0] = q.qx[1] = q.qy[0] = q.qy[1] = q.qz[0] = q.qz[1] = 0u;
     ex = ey = ez = 0;
   }
-  q.exps = ex | (ey << 8) | (ez << 16) | ((ok ? 0u : 1u) << 24);
+  bool in_range = true;
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    in_range = in_range && fabsf(m.min_x[k]) <= kCompactRange && fabsf(m.max_x[k]) <= kCompactRange &&
+               fabsf(m.min_y[k]) <= kCompactRange && fabsf(m.max_y[k]) <= kCompactRange &&
+               fabsf(m.min_z[k]) <= kCompactRange && fabsf(m.max_z[k]) <= kCompactRange;
+  const uint32_t flags = (ok ? 0u : kQFlagExact) | (in_range ? 0u : kQFlagOutOfRange);
+  q.exps = ex | (ey << 8) | (ez << 16) | (flags << 24);
   const float4* src = reinterpret_cast<const float4*>(&q);
   float4* dst = reinterpret_cast<float4*>(out + i);
 #pragma unroll

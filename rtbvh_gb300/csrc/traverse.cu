@@ -166,54 +166,6 @@ __device__ __forceinline__ float qbyte(uint32_t w, uint32_t i) {
   return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7440u + i)) - 8388608.0f;
 }
 
-// The slab test of quad_intersect<true> on a DQNode: the plane of step q is
-// at lo + q * step, so its ray parameter is q * (step * inv) + (lo - o) * inv.
-// The decoded boxes contain the exact ones; the sort network and the mask
-// rule are the reference's.
-__device__ __forceinline__ void quad_intersect_q(const float (&h0)[8], const float (&h1)[8], const RayState& r,
-                                                 uint32_t& mask, uint32_t& ids, int4& children, int4& counts) {
-  const uint32_t exps = __float_as_uint(h0[3]);
-  const float sx = __uint_as_float((exps & 0xffu) << 23);
-  const float sy = __uint_as_float(((exps >> 8) & 0xffu) << 23);
-  const float sz = __uint_as_float(((exps >> 16) & 0xffu) << 23);
-  const float ax = sx * r.ix, bx = (h0[0] - r.ox) * r.ix;
-  const float ay = sy * r.iy, by = (h0[1] - r.oy) * r.iy;
-  const float az = sz * r.iz, bz = (h0[2] - r.oz) * r.iz;
-  // with a negative inverse direction the upper plane is the near one; the
-  // fma is monotonic in q, so this selection equals min/max of the two
-  const uint32_t xl = __float_as_uint(h0[4]), xh = __float_as_uint(h0[5]);
-  const uint32_t yl = __float_as_uint(h0[6]), yh = __float_as_uint(h0[7]);
-  const uint32_t zl = __float_as_uint(h1[0]), zh = __float_as_uint(h1[1]);
-  const uint32_t xn = r.ix < 0.0f ? xh : xl, xf = r.ix < 0.0f ? xl : xh;
-  const uint32_t yn = r.iy < 0.0f ? yh : yl, yf = r.iy < 0.0f ? yl : yh;
-  const uint32_t zn = r.iz < 0.0f ? zh : zl, zf = r.iz < 0.0f ? zl : zh;
-  children = make_int4(__float_as_int(h1[2]), __float_as_int(h1[3]), __float_as_int(h1[4]), __float_as_int(h1[5]));
-  const uint32_t c01 = __float_as_uint(h1[6]), c23 = __float_as_uint(h1[7]);
-  counts = make_int4((int)(int16_t)(c01 & 0xffffu), (int)(int16_t)(c01 >> 16), (int)(int16_t)(c23 & 0xffffu),
-                     (int)(int16_t)(c23 >> 16));
-  float tmin[4];
-  uint32_t m = 0;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const float tn = fmaxf(fmaf(qbyte(xn, i), ax, bx), fmaxf(fmaf(qbyte(yn, i), ay, by), fmaf(qbyte(zn, i), az, bz)));
-    const float tx = fminf(fmaf(qbyte(xf, i), ax, bx), fminf(fmaf(qbyte(yf, i), ay, by), fmaf(qbyte(zf, i), az, bz)));
-    tmin[i] = tn;
-    if ((tx >= tn) && (tn < r.t)) m |= 1u << i;
-  }
-  // a full 4-element sorting network (near to far); the reference's last
-  // comparator is (2, 3), which leaves slots 1 and 2 unordered
-  uint32_t i0 = 0, i1 = 1, i2 = 2, i3 = 3;
-  float t0 = tmin[0], t1 = tmin[1], t2 = tmin[2], t3 = tmin[3], tt;
-  uint32_t ti;
-  if (t0 > t1) { tt = t0; t0 = t1; t1 = tt; ti = i0; i0 = i1; i1 = ti; }
-  if (t2 > t3) { tt = t2; t2 = t3; t3 = tt; ti = i2; i2 = i3; i3 = ti; }
-  if (t0 > t2) { tt = t0; t0 = t2; t2 = tt; ti = i0; i0 = i2; i2 = ti; }
-  if (t1 > t3) { tt = t1; t1 = t3; t3 = tt; ti = i1; i1 = i3; i3 = ti; }
-  if (t1 > t2) { ti = i1; i1 = i2; i2 = ti; }
-  mask = m;
-  ids = i0 | (i1 << 2) | (i2 << 4) | (i3 << 6);
-}
-
 __device__ __forceinline__ bool finite_ray(const RayState& r) {
   return isfinite(r.ox) && isfinite(r.oy) && isfinite(r.oz) && isfinite(r.dx) && isfinite(r.dy) && isfinite(r.dz) &&
          isfinite(r.ix) && isfinite(r.iy) && isfinite(r.iz);
@@ -223,17 +175,72 @@ __device__ __forceinline__ int sel4(const int4& v, uint32_t i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
-// Persistent MBVH traversal with per-lane ray refill: a lane whose ray has
-// finished takes the next ray from a warp-local pool (refilled 128 rays at a
-// time from the global counter), so the warp's lanes stay busy instead of
-// idling until the warp's slowest ray ends. Each loop iteration visits one
-// quad node per lane; a ray's node/triangle order is the reference's.
+// Per-lane ray refill shared by the persistent MBVH kernels: a lane whose ray
+// has finished takes the next ray from a warp-local pool (refilled `batch`
+// rays at a time from the global counter), so the warp's lanes stay busy
+// instead of idling until the warp's slowest ray ends.
 constexpr uint32_t kPoolBatch = 128;  // default rays per pool refill (TraceArgs::ray_batch)
 
-template <bool ANY_HIT, bool STATS, bool COMPACT>
+struct WarpPool {
+  uint32_t next = 0, end = 0;  // warp-uniform (ray counts < 2^32 - 2^25)
+  bool exhausted = false;      // warp-uniform
+  // Calls start(k) on every lane that is not active, for the next unclaimed
+  // ray positions k; start decides whether the lane becomes active.
+  template <class Start>
+  __device__ __forceinline__ void refill(bool active, uint32_t batch, uint32_t ray_count, unsigned int* work,
+                                         Start&& start) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint32_t need = __ballot_sync(0xffffffffu, !active);
+    if (!need) return;
+    // first from what is left in the pool ...
+    const uint32_t avail = end - next;
+    if (avail) {
+      const uint32_t rank = __popc(need & lt_mask);
+      const bool mine = (need >> lane) & 1u;
+      if (mine && rank < avail) start(next + rank);
+      const uint32_t c = __popc(need);
+      next += c < avail ? c : avail;
+      need = __ballot_sync(0xffffffffu, mine && rank >= avail);
+    }
+    // ... then from a fresh batch of the global counter
+    if (need) {
+      unsigned int base = 0;
+      if (lane == 0) base = atomicAdd(work, batch);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= ray_count) {
+        exhausted = true;
+      } else {
+        next = base;
+        end = (ray_count - base > batch) ? base + batch : ray_count;
+        const uint32_t avail2 = end - next;
+        const bool mine = (need >> lane) & 1u;
+        const uint32_t rank = __popc(need & lt_mask);
+        if (mine && rank < avail2) start(next + rank);
+        const uint32_t c = __popc(need);
+        next += c < avail2 ? c : avail2;
+      }
+    }
+  }
+};
+
+// Mesh of ray r in a forest: m with seg_ray_off[m] <= r < seg_ray_off[m + 1].
+__device__ __forceinline__ uint32_t ray_mesh(const TraceArgs& a, uint32_t r) {
+  uint32_t lo = 0, hi = a.seg_count;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(a.seg_ray_off + mid) <= r) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Persistent MBVH traversal over the exact quad nodes with per-lane ray
+// refill. Each loop iteration visits one quad node per lane; a ray's
+// node/triangle order is the reference's. With ray_count_dev the number of
+// rays is read from the device (the rays the compact kernel deferred).
+template <bool ANY_HIT, bool STATS>
 __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int* work) {
-  const int lane = threadIdx.x & 31;
-  const uint32_t lt_mask = (1u << lane) - 1u;
   RayState ray;
   float hu = 0.0f, hv = 0.0f;
   int32_t prim = -1;
@@ -246,19 +253,14 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   int sp = -1;
   int32_t next = -1;
   uint32_t r = 0;
-  bool active = false, fast = true, compact = false;
-  uint32_t pool_next = 0, pool_end = 0;  // warp-uniform (ray_count < 2^32 - 1024)
-  bool exhausted = false;              // warp-uniform
+  bool active = false, fast = true;
+  WarpPool pool;
   const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
-  const uint32_t ray_count = (uint32_t)a.ray_count;
+  const uint32_t ray_count = a.ray_count_dev ? *a.ray_count_dev : (uint32_t)a.ray_count;
   auto start_ray = [&](uint32_t rr) {
     r = a.order ? __ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
     fast = finite_ray(ray);
-    if (COMPACT)
-      compact = fast && fabsf(ray.ox) <= kQuantRange && fabsf(ray.oy) <= kQuantRange &&
-                fabsf(ray.oz) <= kQuantRange && fabsf(ray.ix) <= kQuantRange && fabsf(ray.iy) <= kQuantRange &&
-                fabsf(ray.iz) <= kQuantRange && a.q_count > 0;
     hu = hv = 0.0f;
     prim = -1;
     visits = tests = max_depth = 0;
@@ -274,14 +276,9 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
       next = 0;
       active = true;
       if (a.seg_count) {
-        uint32_t lo = 0, hi = a.seg_count;  // mesh with seg_ray_off[m] <= r < seg_ray_off[m + 1]
-        while (hi - lo > 1) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (__ldg(a.seg_ray_off + mid) <= r) lo = mid;
-          else hi = mid;
-        }
-        const uint32_t root = __ldg(a.seg_root + lo);
-        if (root == __ldg(a.seg_root + lo + 1)) {
+        const uint32_t m = ray_mesh(a, r);
+        const uint32_t root = __ldg(a.seg_root + m);
+        if (root == __ldg(a.seg_root + m + 1)) {
           active = false;
           a.hits[r] = make_float4(ray.t, 0.0f, 0.0f, __int_as_float(-1));
           if (STATS) {
@@ -291,52 +288,20 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
           }
         }
         next = (int32_t)root;
-        if (COMPACT && compact) next = (int32_t)__ldg(a.seg_qroot + lo);
       }
     }
   };
   for (;;) {
-    if (!exhausted) {
-      uint32_t need = __ballot_sync(0xffffffffu, !active);
-      if (need) {
-        // first from what is left in the pool ...
-        const uint32_t avail = (uint32_t)(pool_end - pool_next);
-        if (avail) {
-          const uint32_t rank = __popc(need & lt_mask);
-          if (!active && rank < avail) start_ray(pool_next + rank);
-          const uint32_t c = __popc(need);
-          pool_next += c < avail ? c : avail;
-          need = __ballot_sync(0xffffffffu, !active && rank >= avail);
-        }
-        // ... then from a fresh batch of the global counter
-        if (need) {
-          unsigned int base = 0;
-          if (lane == 0) base = atomicAdd(work, batch);
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (base >= ray_count) {
-            exhausted = true;
-          } else {
-            pool_next = base;
-            pool_end = (ray_count - base > batch) ? base + batch : ray_count;
-            const uint32_t avail2 = (uint32_t)(pool_end - pool_next);
-            const bool mine = (need >> lane) & 1u;
-            const uint32_t rank = __popc(need & lt_mask);
-            if (mine && rank < avail2) start_ray(pool_next + rank);
-            const uint32_t c = __popc(need);
-            pool_next += c < avail2 ? c : avail2;
-          }
-        }
-      }
-    }
+    if (!pool.exhausted) pool.refill(active, batch, ray_count, work, start_ray);
     if (!__any_sync(0xffffffffu, active)) {
-      if (exhausted) break;
+      if (pool.exhausted) break;
       continue;
     }
     if (!active) continue;
     // ---- one quad node
     const int32_t current = next >= 0 ? next : stack[sp--];
     next = -1;
-    if ((uint32_t)current >= ((COMPACT && compact) ? a.q_count : a.node_count)) {
+    if ((uint32_t)current >= a.node_count) {
       atomicOr(a.status, kStatusBadIndex);
       active = false;
       continue;
@@ -344,47 +309,6 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     uint32_t mask, ids;
     int4 children, counts;
     bool done = false;
-    if (COMPACT && compact) {
-      // traversal tree: slots sorted near to far and visited far to near, as
-      // in the reference's loop (a leaf's triangles at once, interior slots
-      // pushed, the nearest one visited next); this simple loop keeps the
-      // kernel free of spills, which pays more than testing leaves near first
-      const float* qn = reinterpret_cast<const float*>(a.qnodes + current);
-      float h0[8], h1[8];
-      ld8(qn, h0);
-      ld8(qn + 8, h1);
-      if (!(__float_as_uint(h0[3]) >> 24)) {
-        quad_intersect_q(h0, h1, ray, mask, ids, children, counts);
-      } else {
-        quad_intersect<true>(a.qexact + current, ray, mask, ids, children, counts);
-      }
-#pragma unroll 1
-      for (int i = 0; i < 4; ++i) {
-        const uint32_t id = (ids >> (2 * (3 - i))) & 3u;
-        if (!((mask >> id) & 1u)) continue;
-        const int32_t count = sel4(counts, id);
-        const int32_t lf = sel4(children, id);
-        if (count > -1) {
-          if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
-            atomicOr(a.status, kStatusBadIndex);
-            done = true;
-            break;
-          }
-          for (int32_t j = 0; j < count; ++j) mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim);
-        } else if (lf > -1) {
-          if (next >= 0) {
-            if (sp + 1 >= kStack) {
-              atomicOr(a.status, kStatusStackOverflow);
-              prim = -2;
-              done = true;
-              break;
-            }
-            stack[++sp] = next;
-          }
-          next = lf;
-        }
-      }
-    } else {
     if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
     else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
     if (STATS) ++visits;
@@ -426,7 +350,6 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
         if (STATS && (uint32_t)(sp + 2) > max_depth) max_depth = (uint32_t)(sp + 2);
       }
     }
-    }
     if (done || (next < 0 && sp < 0)) {
       a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
       if (STATS) {
@@ -436,6 +359,241 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
       }
       active = false;
     }
+  }
+}
+
+// Slots of a traversal-tree node in near-to-far order. key[i] is the entry
+// t of the i-th nearest slot the ray hits; slots it misses, and empty slots
+// (child -1), get +inf and sort last. Each slot's child and count travel
+// with its key through the sorting network, so the caller reads them by
+// position without run-time indexing. A hit slot's key is finite: it is
+// below the ray's t (no NaN arises on the compact path's finite rays).
+__device__ __forceinline__ void sort_slots(float (&key)[4], int32_t (&ch)[4], int32_t (&ct)[4]) {
+  auto cswap = [&](int a, int b) {
+    const bool s = key[b] < key[a];
+    const float ka = key[a], kb = key[b];
+    const int32_t ca = ch[a], cb = ch[b], na = ct[a], nb = ct[b];
+    key[a] = s ? kb : ka;
+    key[b] = s ? ka : kb;
+    ch[a] = s ? cb : ca;
+    ch[b] = s ? ca : cb;
+    ct[a] = s ? nb : na;
+    ct[b] = s ? na : nb;
+  };
+  cswap(0, 1);
+  cswap(2, 3);
+  cswap(0, 2);
+  cswap(1, 3);
+  cswap(1, 2);
+}
+
+// The slab test of quad_intersect<true> on a compact node: the plane of step
+// q is at lo + q * step, so its ray parameter is q * (step * inv) +
+// (lo - o) * inv (one fma). With a negative inverse direction the upper
+// plane is the near one; the fma is monotonic in q, so selecting the planes
+// by sign equals min/max of the two.
+__device__ __forceinline__ void slot_keys_q(const float (&h0)[8], const float (&h1)[8], const RayState& r,
+                                            float (&key)[4], int32_t (&ch)[4], int32_t (&ct)[4]) {
+  const uint32_t exps = __float_as_uint(h0[3]);
+  const float sx = __uint_as_float((exps & 0xffu) << 23);
+  const float sy = __uint_as_float(((exps >> 8) & 0xffu) << 23);
+  const float sz = __uint_as_float(((exps >> 16) & 0xffu) << 23);
+  const float ax = sx * r.ix, bx = (h0[0] - r.ox) * r.ix;
+  const float ay = sy * r.iy, by = (h0[1] - r.oy) * r.iy;
+  const float az = sz * r.iz, bz = (h0[2] - r.oz) * r.iz;
+  const uint32_t xl = __float_as_uint(h0[4]), xh = __float_as_uint(h0[5]);
+  const uint32_t yl = __float_as_uint(h0[6]), yh = __float_as_uint(h0[7]);
+  const uint32_t zl = __float_as_uint(h1[0]), zh = __float_as_uint(h1[1]);
+  const uint32_t xn = r.ix < 0.0f ? xh : xl, xf = r.ix < 0.0f ? xl : xh;
+  const uint32_t yn = r.iy < 0.0f ? yh : yl, yf = r.iy < 0.0f ? yl : yh;
+  const uint32_t zn = r.iz < 0.0f ? zh : zl, zf = r.iz < 0.0f ? zl : zh;
+  const uint32_t c01 = __float_as_uint(h1[6]), c23 = __float_as_uint(h1[7]);
+  ch[0] = __float_as_int(h1[2]);
+  ch[1] = __float_as_int(h1[3]);
+  ch[2] = __float_as_int(h1[4]);
+  ch[3] = __float_as_int(h1[5]);
+  ct[0] = (int32_t)(int16_t)(c01 & 0xffffu);
+  ct[1] = (int32_t)(int16_t)(c01 >> 16);
+  ct[2] = (int32_t)(int16_t)(c23 & 0xffffu);
+  ct[3] = (int32_t)(int16_t)(c23 >> 16);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float tn = fmaxf(fmaf(qbyte(xn, i), ax, bx), fmaxf(fmaf(qbyte(yn, i), ay, by), fmaf(qbyte(zn, i), az, bz)));
+    const float tx = fminf(fmaf(qbyte(xf, i), ax, bx), fminf(fmaf(qbyte(yf, i), ay, by), fmaf(qbyte(zf, i), az, bz)));
+    key[i] = (tx >= tn && tn < r.t && ch[i] >= 0) ? tn : __int_as_float(0x7f800000);
+  }
+  sort_slots(key, ch, ct);
+}
+
+// The same keys from a node's exact (128-byte) copy, for compact nodes whose
+// bounds did not fit the grid; FAST arithmetic (finite rays only).
+__device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RayState& r, float (&key)[4],
+                                                int32_t (&ch)[4], int32_t (&ct)[4]) {
+  const float* q = reinterpret_cast<const float*>(node);
+  float vx[8], vy[8], vz[8], vc[8];
+  ld8(q, vx);
+  ld8(q + 8, vy);
+  ld8(q + 16, vz);
+  ld8(q + 24, vc);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    ch[i] = __float_as_int(vc[i]);
+    ct[i] = __float_as_int(vc[4 + i]);
+    const float tx0 = (vx[i] - r.ox) * r.ix, tx1 = (vx[4 + i] - r.ox) * r.ix;
+    const float ty0 = (vy[i] - r.oy) * r.iy, ty1 = (vy[4 + i] - r.oy) * r.iy;
+    const float tz0 = (vz[i] - r.oz) * r.iz, tz1 = (vz[4 + i] - r.oz) * r.iz;
+    const float tn = fmaxf(fminf(tx0, tx1), fmaxf(fminf(ty0, ty1), fminf(tz0, tz1)));
+    const float tx = fminf(fmaxf(tx0, tx1), fminf(fmaxf(ty0, ty1), fmaxf(tz0, tz1)));
+    key[i] = (tx >= tn && tn < r.t && ch[i] >= 0) ? tn : __int_as_float(0x7f800000);
+  }
+  sort_slots(key, ch, ct);
+}
+
+// Closest hit over the compact (64-byte) nodes of the traversal tree, with
+// the leaf tests taken out of the slot loop. A loop iteration has a node
+// phase -- each lane with no untested leaf visits its next node, pushes the
+// node's hit interior slots far to near (the nearest stays in `next`) and
+// notes its hit leaf slots -- and a triangle phase -- each lane with noted
+// leaves tests the nearest one. The lanes of a warp meet again before the
+// triangle phase, so the warp runs it once per iteration for all of its
+// lanes. A lane visits no node while it has untested leaves, so every node
+// is entered with the t the reference-order loop would have after the
+// previous node's leaves; only the order among one node's leaves (near to
+// far here) differs, which can change the winner among triangles hit at
+// exactly the same t.
+//
+// Rays the compact walk does not take -- a zero or non-finite component, an
+// inverse direction beyond kQuantRange, an origin beyond kCompactRange, or a
+// node flagged out of range on the way -- are appended to `deferred` and
+// traced afterwards by k_trace_mbvh over the exact Mbvh.
+template <int STACK>
+__global__ void __launch_bounds__(kBlock) k_trace_compact(TraceArgs a, unsigned int* work, uint32_t* deferred,
+                                                           unsigned int* deferred_count) {
+  RayState ray;
+  float hu = 0.0f, hv = 0.0f;
+  int32_t prim = -1;
+  int32_t stack[STACK];
+  int sp = -1;
+  int32_t next = -1;
+  // the last visited node's hit leaf slots not yet tested, as bits of their
+  // near-to-far positions in lch / lct (first primitive slot, count)
+  uint32_t pend = 0;
+  int32_t lch[4] = {0, 0, 0, 0}, lct[4] = {0, 0, 0, 0};
+  uint32_t r = 0;
+  bool active = false;
+  WarpPool pool;
+  const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
+  const uint32_t ray_count = (uint32_t)a.ray_count;
+  auto finish = [&]() {
+    a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
+    active = false;
+  };
+  auto defer = [&]() {
+    deferred[atomicAdd(deferred_count, 1u)] = r;
+    active = false;
+  };
+  auto start_ray = [&](uint32_t rr) {
+    r = a.order ? __ldg(a.order + rr) : rr;
+    ray = load_ray(a.rays, r, a.t_max);
+    hu = hv = 0.0f;
+    prim = -1;
+    sp = -1;
+    pend = 0;
+    next = 0;
+    if (a.node_count == 0) {
+      finish();
+      return;
+    }
+    if (a.seg_count) {
+      const uint32_t m = ray_mesh(a, r);
+      if (__ldg(a.seg_root + m) == __ldg(a.seg_root + m + 1)) {
+        finish();  // a mesh without nodes: a miss
+        return;
+      }
+      next = (int32_t)__ldg(a.seg_qroot + m);
+    }
+    // |x| <= bound is false for NaN and infinities
+    const bool ok = fabsf(ray.ox) <= kCompactRange && fabsf(ray.oy) <= kCompactRange &&
+                    fabsf(ray.oz) <= kCompactRange && fabsf(ray.dx) <= 3.0e38f && fabsf(ray.dy) <= 3.0e38f &&
+                    fabsf(ray.dz) <= 3.0e38f && fabsf(ray.ix) <= kQuantRange && fabsf(ray.iy) <= kQuantRange &&
+                    fabsf(ray.iz) <= kQuantRange;
+    if (!ok) {
+      defer();
+      return;
+    }
+    active = true;
+  };
+  for (;;) {
+    if (!pool.exhausted) pool.refill(active, batch, ray_count, work, start_ray);
+    const uint32_t amask = __ballot_sync(0xffffffffu, active);
+    if (!amask) {
+      if (pool.exhausted) break;
+      continue;
+    }
+    if (!active) continue;
+    // ---- node phase (no early exits: the lanes of amask meet below)
+    if (pend == 0) {
+      const int32_t current = next >= 0 ? next : stack[sp--];
+      next = -1;
+      if ((uint32_t)current >= a.q_count) {
+        atomicOr(a.status, kStatusBadIndex);
+        active = false;
+      } else {
+        const float* qn = reinterpret_cast<const float*>(a.qnodes + current);
+        float h0[8], h1[8];
+        ld8(qn, h0);
+        ld8(qn + 8, h1);
+        const uint32_t flags = __float_as_uint(h0[3]) >> 24;
+        if (flags & kQFlagOutOfRange) {
+          defer();
+        } else {
+          float key[4];
+          int32_t ch[4], ct[4];
+          if (!flags) slot_keys_q(h0, h1, ray, key, ch, ct);
+          else slot_keys_exact(a.qexact + current, ray, key, ch, ct);
+          bool overflow = false;
+#pragma unroll
+          for (int i = 3; i >= 0; --i) {  // far to near
+            if (key[i] < __int_as_float(0x7f800000)) {
+              if (ct[i] > -1) {
+                pend |= 1u << i;
+              } else {
+                if (next >= 0) {
+                  if (sp + 1 < STACK) stack[++sp] = next;
+                  else overflow = true;
+                }
+                next = ch[i];
+              }
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            lch[i] = ch[i];
+            lct[i] = ct[i];
+          }
+          if (overflow) {
+            atomicOr(a.status, kStatusStackOverflow);
+            prim = -2;
+            finish();
+          }
+        }
+      }
+    }
+    __syncwarp(amask);
+    // ---- triangle phase
+    if (active && pend) {
+      const uint32_t i = __ffs(pend) - 1;
+      pend &= pend - 1u;
+      const int32_t lf = i == 0 ? lch[0] : (i == 1 ? lch[1] : (i == 2 ? lch[2] : lch[3]));
+      const int32_t count = i == 0 ? lct[0] : (i == 1 ? lct[1] : (i == 2 ? lct[2] : lct[3]));
+      if (lf < 0 || (uint32_t)lf + (uint32_t)count > a.prim_count) {
+        atomicOr(a.status, kStatusBadIndex);
+        active = false;
+      } else {
+        for (int32_t j = 0; j < count; ++j) mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim);
+      }
+    }
+    if (active && pend == 0 && next < 0 && sp < 0) finish();
   }
 }
 
@@ -761,9 +919,10 @@ __global__ void __launch_bounds__(256) k_ray_keys(const float* __restrict__ rays
   vals[i] = (uint32_t)i;
 }
 
-template <bool MBVH, bool ANY_HIT, bool STATS, bool COMPACT = false>
-cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
-  auto kern = MBVH ? k_trace_mbvh<ANY_HIT, STATS, COMPACT> : k_trace_bvh<ANY_HIT, STATS>;
+// Persistent grid: resident blocks per SM (occupancy, capped by
+// blocks_per_sm) on every SM, no more blocks than the rays need.
+template <class K>
+unsigned persistent_grid(K kern, const TraceArgs& a) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
@@ -771,8 +930,28 @@ cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
   size_t grid = (size_t)sm_count() * per_sm;
   const size_t need = (a.ray_count + kBlock - 1) / kBlock;
   if (grid > need) grid = need;
-  kern<<<(unsigned)grid, kBlock, 0, s>>>(a, work);
+  return (unsigned)grid;
+}
+
+template <bool MBVH, bool ANY_HIT, bool STATS>
+cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
+  auto kern = MBVH ? k_trace_mbvh<ANY_HIT, STATS> : k_trace_bvh<ANY_HIT, STATS>;
+  kern<<<persistent_grid(kern, a), kBlock, 0, s>>>(a, work);
   return cudaGetLastError();
+}
+
+// Closest hit through the compact traversal tree, then the rays it deferred
+// over the exact Mbvh. counters: [0] compact ray counter, [1] deferred rays,
+// [2] exact ray counter (zeroed).
+cudaError_t launch_compact(const TraceArgs& a, cudaStream_t s, unsigned int* counters, uint32_t* deferred) {
+  auto kern = a.stack_limit == 32 ? k_trace_compact<32> : (a.stack_limit == 48 ? k_trace_compact<48> : k_trace_compact<64>);
+  kern<<<persistent_grid(kern, a), kBlock, 0, s>>>(a, counters, deferred, counters + 1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  TraceArgs b = a;
+  b.order = deferred;
+  b.ray_count_dev = counters + 1;
+  return launch3<true, false, false>(b, s, counters + 2);
 }
 
 template <bool MBVH>
@@ -781,12 +960,14 @@ cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
   // ray indices and the work counter are 32-bit; after the last batch every
   // warp adds one more ray_batch (<= 4096) to the counter, which must not wrap
   if (a0.ray_count > 0xffffffffull - (1ull << 25) || a0.ray_batch > 4096u) return cudaErrorInvalidValue;
+  if (a0.stack_limit != 0 && a0.stack_limit != 32 && a0.stack_limit != 48 && a0.stack_limit != 64)
+    return cudaErrorInvalidValue;
   TraceArgs a = a0;
   Scratch<unsigned int> work;
-  Scratch<uint32_t> keys, order, acc;
+  Scratch<uint32_t> keys, order, acc, deferred;
   Scratch<char> sort_temp;
   cudaError_t e;
-  if ((e = work.alloc(1, s)) || (e = cudaMemsetAsync(work.ptr, 0, sizeof(unsigned int), s))) return e;
+  if ((e = work.alloc(4, s)) || (e = cudaMemsetAsync(work.ptr, 0, 4 * sizeof(unsigned int), s))) return e;
   if (MBVH && a.order == nullptr && a.reorder && a.ray_count < (1u << 30)) {
     const size_t n = a.ray_count;
     const size_t tb = radix_sort_temp_bytes(n);
@@ -804,8 +985,10 @@ cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
   const bool st = a.stats != nullptr;
   if (a.any_hit) e = st ? launch3<MBVH, true, true>(a, s, work.ptr) : launch3<MBVH, true, false>(a, s, work.ptr);
   else if (st) e = launch3<MBVH, false, true>(a, s, work.ptr);
-  else if (MBVH && a.qnodes) e = launch3<MBVH, false, false, true>(a, s, work.ptr);
-  else e = launch3<MBVH, false, false>(a, s, work.ptr);
+  else if (MBVH && a.qnodes && a.q_count > 0) {
+    if ((e = deferred.alloc(a.ray_count, s))) return e;
+    e = launch_compact(a, s, work.ptr, deferred.ptr);
+  } else e = launch3<MBVH, false, false>(a, s, work.ptr);
   return e;
 }
 

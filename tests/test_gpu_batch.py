@@ -116,13 +116,20 @@ def test_batch_tuning_keeps_results(lib):
     assert chosen["trace_ray_batch"] in (32, 64, 128, 256)
     assert chosen["trace_blocks_per_sm"] in (0, 2, 4)
     assert chosen["pipeline_ms"] > 0
+    assert chosen["trace_stack"] in (32, 48, 64)
     assert batch.tuning["cluster_min_prims"] == chosen["cluster_min_prims"]
-    out = batch.run().clone()
-    torch.cuda.synchronize()
-    assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
-    # extreme settings: every mesh of > 2 primitives clustered, one block per SM, 1-ray batches
-    batch.set_tuning(trace_blocks_per_sm=1, trace_ray_batch=1, cluster_min_prims=2)
+    assert batch.tuning["trace_stack"] == chosen["trace_stack"]
     out = batch.run().clone()
     torch.cuda.synchronize()
     assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
     assert batch.status() == rb.ResultCode.Ok
+    # extreme settings: every mesh of > 2 primitives clustered, one block per SM, 1-ray batches
+    for stack in (32, 48, 64):
+        batch.set_tuning(trace_blocks_per_sm=1, trace_ray_batch=1, cluster_min_prims=2, trace_stack=stack)
+        out = batch.run().clone()
+        torch.cuda.synchronize()
+        assert torch.equal(out.view(torch.int32), ref.view(torch.int32)), f"stack bound {stack}"
+        assert batch.status() == rb.ResultCode.Ok
+    with pytest.raises(rb.RtbvhError):
+        batch.set_tuning(trace_stack=40)
+

@@ -64,3 +64,51 @@ def test_refit_noalloc_rejects_trees_over_the_limit(lib):
     assert rc == _ffi.ResultCode.InvalidArgument
     torch.cuda.synchronize()
     assert np.array_equal(u32(device_nodes(lib, big)), u32(before))
+
+
+def test_refit_noalloc_reports_bad_leaf_ranges_in_the_status(lib):
+    """A leaf whose index range runs past the Bvh's index slots is skipped by
+    the kernel's bounds checks, and the error shows up in rtbvh_gpu_status
+    for that Bvh; a repaired tree refits cleanly again."""
+    torch.cuda.set_device(0)
+    tris = scenes.incoherent(5000, seed=43)
+    bvh = gpu_build(tris, "locb")
+    view = _ffi.RTGpuView()
+    assert lib.rtbvh_gpu_view(bvh.handle.id, 0, ctypes.byref(view)) == 0
+    nodes = torch.as_tensor(_DeviceArray(view.nodes, (view.node_count, 8)), device="cuda")
+    ints = nodes.view(torch.int32)
+    leaf = int(torch.nonzero(ints[:, 3] >= 0)[0])
+    good = int(ints[leaf, 7])
+    ints[leaf, 7] = view.index_count + 5  # host-side damage of the device tree: a leaf past the index slots
+    torch.cuda.synchronize()
+    d_aabbs = to_cuda(scenes.triangle_aabbs(tris))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.rtbvh_gpu_status(bvh.handle.id, 0) == _ffi.ResultCode.Ok
+    assert lib.rtbvh_gpu_refit_noalloc(bvh.handle.id, ctypes.c_void_p(d_aabbs.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    assert lib.rtbvh_gpu_status(bvh.handle.id, 0) == _ffi.ResultCode.Error
+    ints[leaf, 7] = good
+    torch.cuda.synchronize()
+    assert lib.rtbvh_gpu_refit_noalloc(bvh.handle.id, ctypes.c_void_p(d_aabbs.data_ptr()), stream) == 0
+    torch.cuda.synchronize()
+    assert lib.rtbvh_gpu_status(bvh.handle.id, 0) == _ffi.ResultCode.Ok
+
+
+def test_refit_noalloc_leaves_free_device_memory_unchanged(lib):
+    """After a first call (which may load the library's code on the device),
+    further calls take no device memory: the device's free memory is the same
+    before and after them."""
+    torch.cuda.set_device(0)
+    tris = scenes.incoherent(20000, seed=44)
+    bvh = gpu_build(tris, "locb")
+    d_aabbs = to_cuda(scenes.triangle_aabbs(tris))
+    ptr = ctypes.c_void_p(d_aabbs.data_ptr())
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.rtbvh_gpu_refit_noalloc(bvh.handle.id, ptr, stream) == 0
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        assert lib.rtbvh_gpu_refit_noalloc(bvh.handle.id, ptr, stream) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert lib.rtbvh_gpu_status(bvh.handle.id, 0) == _ffi.ResultCode.Ok
