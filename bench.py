@@ -39,6 +39,9 @@ N_RAYS = 16_777_216
 SCENE_SEED, RAY_SEED = 2, 3
 METRIC = "closest-hit Mrays/s (1M-tri incoherent LOCB+MBVH, 16.7M rays)"
 B_IN, B_OUT, B_NODE, B_TRI = 24, 16, 128, 40  # algorithmic bytes: ray in, hit out, quad node, triangle (36 + index 4)
+# algorithmic build bytes per primitive: triangle in 36, box 32, Morton code 4,
+# index 4, two 32-byte nodes out
+B_BUILD = 36 + 32 + 4 + 4 + 2 * 32
 
 
 def dist_env():
@@ -150,6 +153,52 @@ def t_error_vs_fp64(tris, rays, hits, sample=1 << 20):
             "median_rel": float(f"{np.median(rel):.3g}")}
 
 
+def _mt_t32(tri, rays):
+    """t of the reference's triangle test (SpatialTriangle::intersect,
+    src/builders/spatial_sah.rs:132-163) in float32 without contraction, per
+    row; NaN where the test rejects before t."""
+    f32 = np.float32
+    v0, v1, v2 = tri[:, 0].astype(f32), tri[:, 1].astype(f32), tri[:, 2].astype(f32)
+    o, d = rays[:, :3].astype(f32), rays[:, 3:].astype(f32)
+    e1, e2 = v1 - v0, v2 - v0
+
+    def cross(a, b):
+        return np.stack([a[:, 1] * b[:, 2] - b[:, 1] * a[:, 2], a[:, 2] * b[:, 0] - b[:, 2] * a[:, 0],
+                         a[:, 0] * b[:, 1] - b[:, 0] * a[:, 1]], axis=1)
+
+    def dot(a, b):
+        return (a[:, 0] * b[:, 0] + a[:, 1] * b[:, 1]) + a[:, 2] * b[:, 2]
+
+    h = cross(d, e2)
+    det = dot(e1, h)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f = f32(1.0) / det
+        q = cross(o - v0, e1)
+        t = f * dot(e2, q)
+    return np.where((det > -1e-5) & (det < 1e-5), np.float32(np.nan), t)
+
+
+def nearest_hit_parity(gpu, ref, tris, rays):
+    """GPU hits against the oracle's on the same rays: rays whose t differs
+    in any bit; rays whose triangle differs, and how many of those are ties
+    (the reported triangle is hit at exactly the same t by the reference's
+    triangle test, so both answers are a nearest hit); u/v differences on
+    rays with the same triangle."""
+    g32, r32 = np.ascontiguousarray(gpu).view(np.uint32), np.ascontiguousarray(ref).view(np.uint32)
+    t_bad = g32[:, 0] != r32[:, 0]
+    pg, pr = g32[:, 3].view(np.int32), r32[:, 3].view(np.int32)
+    diff = np.nonzero((pg != pr) & ~t_bad)[0]
+    ties = 0
+    if len(diff):
+        ok = (pg[diff] >= 0) & (pr[diff] >= 0)
+        t = _mt_t32(tris[np.maximum(pg[diff], 0)], rays[diff])
+        ties = int((ok & (t.view(np.uint32) == g32[diff, 0])).sum())
+    same = (pg == pr) & ~t_bad
+    uv_bad = int(((g32[same, 1] != r32[same, 1]) | (g32[same, 2] != r32[same, 2])).sum())
+    return {"rays": int(len(gpu)), "t_bit_mismatch": int(t_bad.sum()), "prim_mismatch": int(len(diff)),
+            "ties_proven": ties, "uv_mismatch_same_prim": uv_bad}
+
+
 def replica_value(total_ms, rays_per_step, steps, world_size, dist=None, device="cpu"):
     """Replicas (no exchange between ranks): every rank traces its own copy
     of the workload. Returns (whole-job Mrays/s = all ranks' rays / the
@@ -241,10 +290,21 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    mbvh.intersect(d_rays, t_max=d_tmax, any_hit=True)
+    any_hits, _ = mbvh.intersect(d_rays, t_max=d_tmax, any_hit=True)
     e1.record(stream)
     e1.synchronize()
     any_ms = e0.elapsed_time(e1)
+    any_hit_frac = float((any_hits[:, 3].contiguous().view(torch.int32) >= 0).float().mean())
+    # rays whose [0, t_max] segment enters the scene's root box (slab test in float64)
+    world = d_tris.reshape(-1, 3)
+    lo, hi = world.min(0).values.double(), world.max(0).values.double()
+    o64, d64 = d_rays[:, :3].double(), d_rays[:, 3:].double()
+    with torch.no_grad():
+        t0s, t1s = (lo - o64) / d64, (hi - o64) / d64
+        tn = torch.minimum(t0s, t1s).max(1).values.clamp_min(0.0)
+        tx = torch.maximum(t0s, t1s).min(1).values.minimum(d_tmax.double())
+        any_enter_frac = float((tx >= tn).double().mean())
+    del any_hits, o64, d64, t0s, t1s, tn, tx
 
     # ------------------------------------------------------------ e2e through the C ABI with host buffers
     h_rays = torch.from_numpy(rays).pin_memory()
@@ -273,12 +333,25 @@ def run_gpu(args):
             traffic = json.load(f).get("bytes_per_launch")
 
     cpu = None
+    parity = None
     workloads = {}
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(tris, rays)
     t_err = None
     if rank == 0:
-        t_err = t_error_vs_fp64(tris, rays, step()[: 1 << 20].cpu().numpy())
+        sample = 1 << 20
+        gpu_sample = step()[:sample].cpu().numpy()
+        t_err = t_error_vs_fp64(tris, rays, gpu_sample)
+        if not args.no_cpu_baseline:
+            cpu, ref_hits = cpu_baseline(tris, rays, sample=sample)
+            exact_sample, _ = mbvh.intersect(d_rays[:sample], exact_nodes=True)
+            parity = {"against": "oracle (CPU restatement of the reference's LOCB build and Mbvh traversal)",
+                      "default_walk": nearest_hit_parity(gpu_sample, ref_hits, tris, rays[:sample]),
+                      "exact_node_walk": nearest_hit_parity(exact_sample.cpu().numpy(), ref_hits, tris,
+                                                            rays[:sample]),
+                      "sample": f"first {sample} of the {N_RAYS} rays (the default walk's hits taken from one "
+                                "full-size launch)"}
+    build_roofline = {"bytes_per_primitive": B_BUILD, "unit": "GB/s", "peak": peak, "peak_source": peak_kind,
+                      "locb_1M": round(B_BUILD * N_TRIS / (statistics.median(build_ms) * 1e-3) / 1e9, 1)}
+    build_roofline["locb_1M_frac"] = round(build_roofline["locb_1M"] / peak, 4)
     if rank == 0 and not args.no_extra:
         workloads["sphere_6400_binned_sah"] = workload_sphere_sah(not args.no_cpu_baseline)
         workloads["spatial_sah_teapot"] = workload_spatial("teapot", not args.no_cpu_baseline)
@@ -309,9 +382,12 @@ def run_gpu(args):
             "clocks": clk.summary(),
             "build_ms": {"locb": round(statistics.median(build_ms), 3), "mbvh": round(statistics.median(mbvh_ms), 3)},
             "any_hit": {"value": round(ws * N_RAYS / (any_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
-                        "t_max": "0.5 x distance"},
+                        "t_max": "0.5 x distance", "rays_entering_root_box": round(any_enter_frac, 4),
+                        "rays_reporting_a_hit": round(any_hit_frac, 4)},
+            "build_roofline": build_roofline,
             "max_stack_depth": max_stack,
             "t_error_vs_fp64": t_err,
+            "parity": parity,
             "workloads": workloads,
         }
         print(json.dumps(line))
@@ -449,35 +525,56 @@ def workload_differentiable():
         h, _ = m.intersect(d_rays)
         diff.intersect_backward(verts, d_rays, h, g, gv, gr)
 
+    tri_v = verts.view(-1, 3, 3)
+    o, d = d_rays[:, :3], d_rays[:, 3:]
+    pgv = torch.empty_like(tri_v)
+
+    def cross(a, b):
+        return torch.stack([a[:, 1] * b[:, 2] - b[:, 1] * a[:, 2], a[:, 2] * b[:, 0] - b[:, 2] * a[:, 0],
+                            a[:, 0] * b[:, 1] - b[:, 0] * a[:, 1]], dim=1)
+
     def plain():
+        # the per-call path without the library's backward: the same trace,
+        # then the triangle test recomputed for the hit triangles and its
+        # gradient written out in PyTorch ops (no autograd graph), scattered
+        # to the triangles with index_add_
         h, _ = m.intersect(d_rays)
         prim = h[:, 3].contiguous().view(torch.int32)
-        hit = (prim >= 0).float()
+        hit = (prim >= 0).unsqueeze(1)
         idx = prim.clamp(min=0).long()
-        v = verts.detach().requires_grad_(True)
-        r = d_rays.detach().requires_grad_(True)
-        tri = v[idx]
-        o, d = r[:, :3], r[:, 3:]
-        e1, e2 = tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]
-        hh = torch.cross(d, e2, dim=1)
-        f = 1.0 / (e1 * hh).sum(1)
-        s = o - tri[:, 0]
-        u = f * (s * hh).sum(1)
-        q = torch.cross(s, e1, dim=1)
-        vv = f * (d * q).sum(1)
-        t = f * (e2 * q).sum(1)
-        loss = ((g[:, 0] * t + g[:, 1] * u + g[:, 2] * vv) * hit).sum()
-        loss.backward()
-        return v.grad, r.grad
+        tri = tri_v[idx]
+        v0 = tri[:, 0]
+        e1, e2 = tri[:, 1] - v0, tri[:, 2] - v0
+        hh = cross(d, e2)
+        f = (1.0 / (e1 * hh).sum(1, keepdim=True))
+        s = o - v0
+        q = cross(s, e1)
+        u = f * (s * hh).sum(1, keepdim=True)
+        vv = f * (d * q).sum(1, keepdim=True)
+        t = f * (e2 * q).sum(1, keepdim=True)
+        lam = f * (g[:, 0:1] * cross(e1, e2) + g[:, 1:2] * hh + g[:, 2:3] * cross(e1, d))
+        lam = torch.where(hit, lam, 0.0)  # misses contribute nothing (their triangle 0 may be degenerate)
+        dv = torch.where(hit.unsqueeze(2), torch.stack([-(1.0 - u - vv) * lam, -u * lam, -vv * lam], dim=1), 0.0)
+        pgv.zero_()
+        pgv.index_add_(0, idx, dv)
+        return pgv, torch.cat([lam, torch.where(hit, t * lam, 0.0)], dim=1)
 
     fwd_ms = _cuda_time(lambda: m.intersect(d_rays))
     fused_ms = _cuda_time(fused)
     plain_ms = _cuda_time(plain)
+    # both paths give the same gradients (the plain one sums in atomic order)
+    fused()
+    pv, pr = plain()
+    torch.cuda.synchronize()
+    rel_v = float((pv.reshape(-1) - gv.reshape(-1)).norm() / gv.norm())
+    rel_r = float((pr - gr).norm() / gr.norm())
     step_ms = _cuda_time(lambda: bvh.refit(triangles=verts, mbvh=m), reps=3)
     return {"triangles": len(tris), "rays": len(rays), "forward_ms": round(fwd_ms, 3),
             "forward_backward_ms": round(fused_ms, 3), "plain_forward_backward_ms": round(plain_ms, 3),
             "speedup_vs_plain": round(plain_ms / fused_ms, 2), "refit_and_recollapse_ms": round(step_ms, 3),
-            "plain": "same trace, then the triangle test recomputed and differentiated by PyTorch autograd"}
+            "plain_vs_fused_rel_diff": {"vertices": float(f"{rel_v:.3g}"), "rays": float(f"{rel_r:.3g}")},
+            "plain": "same trace, then the triangle test of the hit triangles recomputed and its gradient "
+                     "written in PyTorch ops (no autograd), index_add_ scatter to the triangles"}
 
 
 def secondary_rays(rays, hits, vertices, per_hit=3, total_hits=None, seed=9):
@@ -545,8 +642,12 @@ def workload_clustered(with_stats=True):
     R = allr.shape[0]
     ms = _cuda_time(lambda: m.intersect(allr), reps=3, warmup=2)
     sec_ms = _cuda_time(lambda: m.intersect(allr[primary.shape[0]:]), reps=3, warmup=1)
+    peak, kind = measured_peak()
+    sah_gbs = B_BUILD * int(d_tris.shape[0]) / (sah_ms * 1e-3) / 1e9
     out = {"triangles": int(d_tris.shape[0]), "rays": int(R), "primary_hits": primary_hits,
            "sah_build_ms": round(sah_ms, 2), "mbvh_ms": round(mbvh_ms, 2),
+           "build_roofline": {"bytes_per_primitive": B_BUILD, "achieved_gbs": round(sah_gbs, 1),
+                              "frac": round(sah_gbs / peak, 4), "peak_source": kind},
            "closest_hit_mrays": round(R / (ms * 1e-3) / 1e6, 1),
            "secondary_only_mrays": round((R - primary.shape[0]) / (sec_ms * 1e-3) / 1e6, 1)}
     if with_stats:
@@ -554,7 +655,6 @@ def workload_clustered(with_stats=True):
         st = st.to(torch.int64)
         nv, nt = float(st[:, 0].sum()) / R, float(st[:, 1].sum()) / R
         bpr = B_IN + B_OUT + B_NODE * nv + B_TRI * nt
-        peak, kind = measured_peak()
         ach = bpr * R / (ms * 1e-3) / 1e9
         out["roofline"] = {"bytes_per_ray": round(bpr, 1), "mean_node_visits": round(nv, 3),
                            "mean_tri_tests": round(nt, 3), "achieved_gbs": round(ach, 1),
@@ -621,9 +721,10 @@ def workload_batched(mesh_count=512, seed=44):
             "mrays_including_build": round(ro[-1] / (graph_ms * 1e-3) / 1e6, 1)}
 
 
-def cpu_baseline(tris, rays, threads=None, sample=1_000_000):
+def cpu_baseline(tris, rays, threads=None, sample=1 << 20):
     """CPU restatement of the reference (oracle) on the host cores: LOCB +
-    MBVH build once, then the rayon-style chunked traversal of a ray sample."""
+    MBVH build once, then the rayon-style chunked traversal of a ray sample.
+    Returns (the cpu_baseline entry, the oracle's hits of the sample)."""
     import oracle
     threads = threads or os.cpu_count() or 1
     a, c = oracle.triangle_prep(tris)
@@ -633,10 +734,10 @@ def cpu_baseline(tris, rays, threads=None, sample=1_000_000):
     build_s = time.perf_counter() - t0
     sub = rays[:sample]
     t0 = time.perf_counter()
-    oracle.trace("mbvh", m, idx, tris.reshape(-1, 9), sub, threads=threads, stats=False)
+    hits, _, _ = oracle.trace("mbvh", m, idx, tris.reshape(-1, 9), sub, threads=threads, stats=False)
     dt = time.perf_counter() - t0
     return {"value": round(len(sub) / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"first {len(sub)} of the {N_RAYS} rays; LOCB+MBVH build {build_s:.2f} s (not in value)"}
+            "sample": f"first {len(sub)} of the {N_RAYS} rays; LOCB+MBVH build {build_s:.2f} s (not in value)"}, hits
 
 
 def run_reference(args):
@@ -671,7 +772,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": "incoherent-1M-locb-mbvh", "triangles": N_TRIS, "rays": N_RAYS,
-                   "sample_rays_per_step": sample},
+                   "sample_rays_per_step": sample,
+                   "sampling": f"each step times a {sample}-ray slice of the {N_RAYS}-ray set (the CPU needs "
+                               "about 8 s for all of them); value = sampled rays / their time"},
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} consecutive rays per step of the {N_RAYS}-ray set"},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

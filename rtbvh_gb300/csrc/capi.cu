@@ -33,6 +33,7 @@ struct Entry {
   uint32_t bvh_node_count = 0;    // Mbvh: entries of d_nodes
   uint32_t build_type = 0;        // the crate's BuildType (1 LOCB, 2 binned SAH, 3 spatial; 0 unknown);
                                   // an Mbvh keeps its source Bvh's
+  bool boxes_cover = false;       // every leaf box contains its primitives (see boxes_cover())
   DMNode* d_mnodes = nullptr;     // Mbvh
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
@@ -88,6 +89,27 @@ uint32_t store(std::unique_ptr<Entry> e, bool mbvh) {
 // spatial-split trees and structures of unknown origin are checked.
 const uint32_t* leaf_check(uint32_t build_type, const uint32_t* indices) {
   return (build_type == 1 || build_type == 2) ? nullptr : indices;
+}
+
+// Leaf boxes contain their primitives for LOCB builds (a leaf is its
+// primitive's box grown by 1e-4, src/builders/locb.rs) and for every tree
+// after a refit (each box recomputed from the primitives,
+// src/bvh.rs:176-205). A binned-SAH build as written sizes a left child's
+// box from bins [0, best_splits[axis].count), which after the longest-axis
+// fallback is not the split (src/builders/binned_sah.rs:236-256), so its
+// leaves need not contain their primitives and only the reference's own
+// walk reproduces its hits: it gets no traversal tree.
+bool boxes_cover(uint32_t build_type) { return build_type == 1; }
+
+// build_wide when the leaf boxes contain their primitives, else no tree
+// (closest hit then walks the exact nodes in the reference's order).
+ResultCode build_wide_if(bool cover, const DAabb* nodes, uint32_t node_count, const uint32_t* indices,
+                         uint32_t index_count, cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount) {
+  *wnodes = nullptr;
+  *wq = nullptr;
+  *wcount = 0;
+  if (!cover) return Ok;
+  return build_wide(nodes, node_count, indices, index_count, s, wnodes, wq, wcount);
 }
 
 cudaStream_t legacy_stream() {
@@ -161,6 +183,7 @@ ResultCode store_bvh(const BuildOutput& out, uint32_t slots, size_t n, uint32_t 
   e->d_nodes = out.nodes;
   e->d_indices = out.indices;
   e->build_type = build_type;
+  e->boxes_cover = boxes_cover(build_type);
   ResultCode rc;
   cudaError_t err;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
@@ -682,7 +705,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   DAabb* d_nodes;
   uint32_t node_count, prim_count, vertex_count, build_type;
-  bool lower_bound;
+  bool lower_bound, cover;
   const uint32_t* d_indices;
   const float4* d_tris;
   const float* d_vertices;
@@ -696,6 +719,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
     vertex_count = src->vertex_count;
     lower_bound = src->vertex_lower_bound;
     build_type = src->build_type;
+    cover = src->boxes_cover;
     d_indices = src->d_indices;
     d_tris = src->d_tris;
     d_vertices = src->d_vertices;
@@ -706,12 +730,13 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   e->vertex_count = vertex_count;
   e->vertex_lower_bound = lower_bound;
   e->build_type = build_type;
+  e->boxes_cover = cover;
   e->source_bvh = bvh.id;
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
-  if ((rc = build_wide(d_nodes, node_count, leaf_check(build_type, d_indices), prim_count, s, &e->d_wnodes,
-                       &e->d_qnodes, &e->wcount)) != Ok) {
+  if ((rc = build_wide_if(cover, d_nodes, node_count, leaf_check(build_type, d_indices), prim_count, s,
+                          &e->d_wnodes, &e->d_qnodes, &e->wcount)) != Ok) {
     e->release();
     return rc;
   }
@@ -1059,8 +1084,10 @@ static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, 
   m->d_qnodes = nullptr;
   m->d_wnodes = nullptr;
   m->wcount = 0;
-  if ((rc = build_wide(nodes, node_count, leaf_check(m->build_type, m->d_indices), m->prim_count, s, &m->d_wnodes,
-                       &m->d_qnodes, &m->wcount)) != Ok)
+  // recollapse follows a refit: every box now comes from the primitives
+  m->boxes_cover = true;
+  if ((rc = build_wide_if(true, nodes, node_count, leaf_check(m->build_type, m->d_indices), m->prim_count, s,
+                          &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok)
     return rc;
   if (vertices) {
     if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
@@ -1131,6 +1158,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
   }
   ResultCode rc = refit_bvh(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count, boxes, s);
   if (rc != Ok) return rc;
+  b->boxes_cover = true;
   if (m) {
     if (m->d_nodes && (err = cudaMemcpyAsync(m->d_nodes, b->d_nodes, (size_t)b->node_count * sizeof(DAabb),
                                              cudaMemcpyDeviceToDevice, s)))
@@ -1150,8 +1178,11 @@ ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb* aabbs, rtbvh_s
   std::lock_guard<std::mutex> lock(g_mu);
   Entry* b = lookup(bvh_id, false);
   if (!b) return Error;
-  return refit_bvh_noalloc(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count,
-                           reinterpret_cast<const DAabb*>(aabbs), b->d_status, static_cast<cudaStream_t>(stream));
+  const ResultCode rc = refit_bvh_noalloc(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count,
+                                          reinterpret_cast<const DAabb*>(aabbs), b->d_status,
+                                          static_cast<cudaStream_t>(stream));
+  if (rc == Ok) b->boxes_cover = true;
+  return rc;
 }
 
 ResultCode rtbvh_gpu_intersect_backward(const float* vertices, uintptr_t prim_count, const float* rays,
@@ -1318,6 +1349,7 @@ ResultCode rtbvh_deserialize_bvh(const uint8_t* buffer, uintptr_t size, uint32_t
   e->node_count = (uint32_t)nn;
   e->prim_count = (uint32_t)ni;
   e->build_type = bt;
+  e->boxes_cover = boxes_cover(bt);
   ResultCode rc = upload_entry(*e, hn.data(), nn, hi.data(), ni, s);
   if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_bvh(*e, s);
   if (rc != Ok) {
@@ -1394,8 +1426,8 @@ ResultCode rtbvh_deserialize_mbvh(const uint8_t* buffer, uintptr_t size, uint32_
       rc = InvalidArgument;
   }
   if (rc == Ok)
-    rc = build_wide(e->d_nodes, e->bvh_node_count, leaf_check(e->build_type, e->d_indices), e->prim_count, s,
-                    &e->d_wnodes, &e->d_qnodes, &e->wcount);
+    rc = build_wide_if(e->boxes_cover, e->d_nodes, e->bvh_node_count, leaf_check(e->build_type, e->d_indices),
+                       e->prim_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount);
   if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_mbvh(*e, s);
   if (rc != Ok) {
     e->release();

@@ -185,14 +185,17 @@ struct WarpPool {
   uint32_t next = 0, end = 0;  // warp-uniform (ray counts < 2^32 - 2^25)
   bool exhausted = false;      // warp-uniform
   // Calls start(k) on every lane that is not active, for the next unclaimed
-  // ray positions k; start decides whether the lane becomes active.
+  // ray positions k; start decides whether the lane becomes active. A single
+  // idle lane waits for a second one (unless no lane is active), so that the
+  // ray set-up, which only the refilled lanes execute, runs for two or more
+  // lanes at a time.
   template <class Start>
   __device__ __forceinline__ void refill(bool active, uint32_t batch, uint32_t ray_count, unsigned int* work,
                                          Start&& start) {
     const int lane = threadIdx.x & 31;
     const uint32_t lt_mask = (1u << lane) - 1u;
     uint32_t need = __ballot_sync(0xffffffffu, !active);
-    if (!need) return;
+    if (!need || (__popc(need) < 2 && need != 0xffffffffu)) return;
     // first from what is left in the pool ...
     const uint32_t avail = end - next;
     if (avail) {
@@ -362,23 +365,21 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   }
 }
 
-// Slots of a traversal-tree node in near-to-far order. key[i] is the entry
-// t of the i-th nearest slot the ray hits; slots it misses, and empty slots
-// (child -1), get +inf and sort last. Each slot's child and count travel
-// with its key through the sorting network, so the caller reads them by
-// position without run-time indexing. A hit slot's key is finite: it is
+// Interior slots of a traversal-tree node in near-to-far order. key[i] is
+// the entry t of the i-th nearest interior slot the ray hits; other slots
+// (missed, empty, or leaves) get +inf and sort last. Each key's child
+// travels with it through the sorting network, so the caller reads children
+// by position without run-time indexing. A hit slot's key is finite: it is
 // below the ray's t (no NaN arises on the compact path's finite rays).
-__device__ __forceinline__ void sort_slots(float (&key)[4], int32_t (&ch)[4], int32_t (&ct)[4]) {
+__device__ __forceinline__ void sort_slots(float (&key)[4], int32_t (&ch)[4]) {
   auto cswap = [&](int a, int b) {
     const bool s = key[b] < key[a];
     const float ka = key[a], kb = key[b];
-    const int32_t ca = ch[a], cb = ch[b], na = ct[a], nb = ct[b];
+    const int32_t ca = ch[a], cb = ch[b];
     key[a] = s ? kb : ka;
     key[b] = s ? ka : kb;
     ch[a] = s ? cb : ca;
     ch[b] = s ? ca : cb;
-    ct[a] = s ? nb : na;
-    ct[b] = s ? na : nb;
   };
   cswap(0, 1);
   cswap(2, 3);
@@ -387,13 +388,24 @@ __device__ __forceinline__ void sort_slots(float (&key)[4], int32_t (&ch)[4], in
   cswap(1, 2);
 }
 
+// Key of slot i (interior slots only) and its bit in the leaf mask.
+__device__ __forceinline__ void slot_key(float tn, float tx, float t, int32_t child, int32_t count, int i,
+                                         float& key, uint32_t& leaves) {
+  const bool hit = tx >= tn && tn < t && child >= 0;
+  key = (hit && count < 0) ? tn : __int_as_float(0x7f800000);
+  leaves |= (hit && count >= 0) ? 1u << i : 0u;
+}
+
 // The slab test of quad_intersect<true> on a compact node: the plane of step
 // q is at lo + q * step, so its ray parameter is q * (step * inv) +
 // (lo - o) * inv (one fma). With a negative inverse direction the upper
 // plane is the near one; the fma is monotonic in q, so selecting the planes
-// by sign equals min/max of the two.
+// by sign equals min/max of the two. Outputs: the sorted interior keys and
+// children, the hit leaf slots as a mask over the node's own slot order, and
+// the node's children and counts in that order.
 __device__ __forceinline__ void slot_keys_q(const float (&h0)[8], const float (&h1)[8], const RayState& r,
-                                            float (&key)[4], int32_t (&ch)[4], int32_t (&ct)[4]) {
+                                            float (&key)[4], int32_t (&ich)[4], uint32_t& leaves,
+                                            int32_t (&ch)[4], int32_t (&ct)[4]) {
   const uint32_t exps = __float_as_uint(h0[3]);
   const float sx = __uint_as_float((exps & 0xffu) << 23);
   const float sy = __uint_as_float(((exps >> 8) & 0xffu) << 23);
@@ -416,25 +428,29 @@ __device__ __forceinline__ void slot_keys_q(const float (&h0)[8], const float (&
   ct[1] = (int32_t)(int16_t)(c01 >> 16);
   ct[2] = (int32_t)(int16_t)(c23 & 0xffffu);
   ct[3] = (int32_t)(int16_t)(c23 >> 16);
+  leaves = 0;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const float tn = fmaxf(fmaf(qbyte(xn, i), ax, bx), fmaxf(fmaf(qbyte(yn, i), ay, by), fmaf(qbyte(zn, i), az, bz)));
     const float tx = fminf(fmaf(qbyte(xf, i), ax, bx), fminf(fmaf(qbyte(yf, i), ay, by), fmaf(qbyte(zf, i), az, bz)));
-    key[i] = (tx >= tn && tn < r.t && ch[i] >= 0) ? tn : __int_as_float(0x7f800000);
+    slot_key(tn, tx, r.t, ch[i], ct[i], i, key[i], leaves);
+    ich[i] = ch[i];
   }
-  sort_slots(key, ch, ct);
+  sort_slots(key, ich);
 }
 
-// The same keys from a node's exact (128-byte) copy, for compact nodes whose
+// The same from a node's exact (128-byte) copy, for compact nodes whose
 // bounds did not fit the grid; FAST arithmetic (finite rays only).
 __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RayState& r, float (&key)[4],
-                                                int32_t (&ch)[4], int32_t (&ct)[4]) {
+                                                int32_t (&ich)[4], uint32_t& leaves, int32_t (&ch)[4],
+                                                int32_t (&ct)[4]) {
   const float* q = reinterpret_cast<const float*>(node);
   float vx[8], vy[8], vz[8], vc[8];
   ld8(q, vx);
   ld8(q + 8, vy);
   ld8(q + 16, vz);
   ld8(q + 24, vc);
+  leaves = 0;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     ch[i] = __float_as_int(vc[i]);
@@ -444,9 +460,10 @@ __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RaySta
     const float tz0 = (vz[i] - r.oz) * r.iz, tz1 = (vz[4 + i] - r.oz) * r.iz;
     const float tn = fmaxf(fminf(tx0, tx1), fmaxf(fminf(ty0, ty1), fminf(tz0, tz1)));
     const float tx = fminf(fmaxf(tx0, tx1), fminf(fmaxf(ty0, ty1), fmaxf(tz0, tz1)));
-    key[i] = (tx >= tn && tn < r.t && ch[i] >= 0) ? tn : __int_as_float(0x7f800000);
+    slot_key(tn, tx, r.t, ch[i], ct[i], i, key[i], leaves);
+    ich[i] = ch[i];
   }
-  sort_slots(key, ch, ct);
+  sort_slots(key, ich);
 }
 
 // Closest hit over the compact (64-byte) nodes of the traversal tree, with
@@ -454,12 +471,12 @@ __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RaySta
 // phase -- each lane with no untested leaf visits its next node, pushes the
 // node's hit interior slots far to near (the nearest stays in `next`) and
 // notes its hit leaf slots -- and a triangle phase -- each lane with noted
-// leaves tests the nearest one. The lanes of a warp meet again before the
+// leaves tests one of them. The lanes of a warp meet again before the
 // triangle phase, so the warp runs it once per iteration for all of its
 // lanes. A lane visits no node while it has untested leaves, so every node
 // is entered with the t the reference-order loop would have after the
-// previous node's leaves; only the order among one node's leaves (near to
-// far here) differs, which can change the winner among triangles hit at
+// previous node's leaves; only the order among one node's leaves (slot
+// order here) differs, which can change the winner among triangles hit at
 // exactly the same t.
 //
 // Rays the compact walk does not take -- a zero or non-finite component, an
@@ -476,7 +493,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_compact(TraceArgs a, unsigned 
   int sp = -1;
   int32_t next = -1;
   // the last visited node's hit leaf slots not yet tested, as bits of their
-  // near-to-far positions in lch / lct (first primitive slot, count)
+  // slots in lch / lct (first primitive slot, count)
   uint32_t pend = 0;
   int32_t lch[4] = {0, 0, 0, 0}, lct[4] = {0, 0, 0, 0};
   uint32_t r = 0;
@@ -548,28 +565,19 @@ __global__ void __launch_bounds__(kBlock) k_trace_compact(TraceArgs a, unsigned 
           defer();
         } else {
           float key[4];
-          int32_t ch[4], ct[4];
-          if (!flags) slot_keys_q(h0, h1, ray, key, ch, ct);
-          else slot_keys_exact(a.qexact + current, ray, key, ch, ct);
+          int32_t ich[4];
+          if (!flags) slot_keys_q(h0, h1, ray, key, ich, pend, lch, lct);
+          else slot_keys_exact(a.qexact + current, ray, key, ich, pend, lch, lct);
           bool overflow = false;
 #pragma unroll
           for (int i = 3; i >= 0; --i) {  // far to near
             if (key[i] < __int_as_float(0x7f800000)) {
-              if (ct[i] > -1) {
-                pend |= 1u << i;
-              } else {
-                if (next >= 0) {
-                  if (sp + 1 < STACK) stack[++sp] = next;
-                  else overflow = true;
-                }
-                next = ch[i];
+              if (next >= 0) {
+                if (sp + 1 < STACK) stack[++sp] = next;
+                else overflow = true;
               }
+              next = ich[i];
             }
-          }
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            lch[i] = ch[i];
-            lct[i] = ct[i];
           }
           if (overflow) {
             atomicOr(a.status, kStatusStackOverflow);

@@ -1,7 +1,11 @@
-"""Differentiable closest-hit ray cast: the hand-written backward kernel
-against an FP64 analytic gradient and FP64 central finite differences
-(h = 1e-4) on 4,096 sampled rays; determinism of the per-triangle sums; the
-autograd harness; one vertex step followed by the GPU refit."""
+"""Differentiable closest-hit ray cast on the full differentiable workload
+(200,000-triangle sphere, 2048 x 2048 camera): the hand-written backward
+kernel against an FP64 analytic gradient and FP64 central finite
+differences (h = 1e-4) on 4,096 rays sampled from the camera; determinism of
+the per-triangle sums; the autograd harness; one vertex step followed by the
+GPU refit."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -47,7 +51,7 @@ def analytic64(tri, ray, g):
 def setup(lib):
     torch.cuda.set_device(0)
     tris = scenes.sphere_fast(500, 200, radius=1.0, noise=0.05, seed=5)  # 200,000 triangles
-    rays = scenes.camera_rays(512, 512, eye=(0.0, 0.0, 3.0), fov_deg=45.0)
+    rays = scenes.camera_rays(2048, 2048, eye=(0.0, 0.0, 3.0), fov_deg=45.0)  # 4,194,304 rays
     bvh = rb.Builder(primitives=rb.Triangles(to_cuda(tris))).construct_binned_sah()
     mbvh = rb.Mbvh.construct(bvh)
     d_rays = to_cuda(rays)
@@ -182,7 +186,11 @@ def test_vertex_step_then_gpu_refit(setup):
     cols = [0, 1, 2, 4, 5, 6]
     assert np.array_equal(u32(nodes)[:, cols], u32(ref)[:, cols])
     h2, _ = mbvh.intersect(d_rays)
-    oh, _, _ = oracle.trace("mbvh", oracle.mbvh(nodes), bvh.indices(), moved.reshape(-1, 9), rays)
+    # every 16th ray against the oracle (the stepped triangles overlap a lot,
+    # which makes the CPU walk slow)
+    sub = slice(0, None, 16)
+    oh, _, _ = oracle.trace("mbvh", oracle.mbvh(nodes), bvh.indices(), moved.reshape(-1, 9), rays[sub],
+                            threads=os.cpu_count() or 1, stats=False)
     # the refitted tree is nested, so closest hit runs on the traversal tree:
     # the same nearest hit as the reference's traversal, ties aside
-    assert_same_nearest(h2.cpu().numpy(), oh, moved, rays)
+    assert_same_nearest(h2.cpu().numpy()[sub], oh, moved, rays[sub])
