@@ -6,17 +6,26 @@
 // level; the phases of a level are separated by grid barriers (bounded
 // waits), so no host round trip or relaunch happens between levels:
 //
-//   large tasks (more than kWarpMax primitives): the grid bins 2048-primitive
+//   large tasks (more than sub_max primitives): the grid bins 2048-primitive
 //     chunks into per-task global bins (runs of primitives in one bin merged
 //     in registers, then ordered-int atomics), one warp per task decides the
 //     split, and a chunked stable partition (decoupled look-back over the
 //     chunks of a task, bounded waits) scatters the primitive indices;
-//   small tasks of at most kThreadMax primitives: one thread each decides
-//     and partitions (exact sweep over the non-empty bins);
-//   other small tasks: one warp each from a queue (bins in shared memory,
-//     the warp-parallel decision, ballot partition);
 //   then a scan over the level's tasks numbers the children (breadth-first,
-//     deterministic) and builds the next level's task lists.
+//     deterministic) and builds the next level's task list. Children of at
+//     most sub_max primitives are not split level by level: they go to a
+//     subtree list. sub_max = n / 2048 clamped to [32, kWarpMax], so a small
+//     build keeps enough subtrees to fill the GPU.
+//
+// After the last level, k_sub_build builds every listed subtree depth first,
+// one warp per subtree (bins in shared memory, the warp-parallel decision,
+// ballot partition; tasks of at most kThreadMax primitives are finished by
+// single lanes, exact sweep over the non-empty bins), with no grid-wide
+// phases. The node pair of a split at primitive position m goes to scratch
+// slots 2(m-1), 2(m-1)+1 -- split positions are distinct across the whole
+// tree -- and a scan over the positions places the pairs after the
+// breadth-first part in position order, so the numbering stays
+// deterministic and gap-free.
 //
 // The split arithmetic is the reference's: node box + 1e-4; 16 bins per axis
 // with bin = min(15, max(c * (16/diag) + off, 0) as usize) (no FMA); the
@@ -63,13 +72,15 @@ static_assert(sizeof(Decision) == 80, "Decision layout");
 
 struct Counters {
   uint32_t large;       // tasks in the current large list
-  uint32_t small;       // tasks in the current small list
-  uint32_t node_count;  // nodes allocated so far
+  uint32_t sub;         // subtree tasks listed so far (all levels)
+  uint32_t node_count;  // nodes of the breadth-first part so far
   uint32_t chunks;      // chunks of the current large list
   uint32_t status;
   uint32_t ticket;      // chunk ticket of the partition kernel
-  uint32_t mq_count;    // small tasks of more than kThreadMax primitives queued this level
-  uint32_t mq_head;     // next queued task a warp takes
+  uint32_t sub_head;    // next subtree a warp of k_sub_build takes
+  uint32_t sub_splits;  // splits inside the subtrees (the scan's total)
+  uint32_t tiny;        // subtrees of at most kThreadMax primitives listed by k_sub_build
+  uint32_t tiny_head;   // next one a thread of k_sub_tiny takes
 };
 
 struct BinMap {
@@ -343,16 +354,21 @@ struct SahParams {
   uint32_t* idx_b;  // partition scratch
   uint32_t n;
   uint32_t max_leaf;
+  uint32_t sub_max;     // largest task built as a subtree (<= kWarpMax)
   Task* large[2];       // task lists of even / odd levels
-  Task* small[2];
-  Decision* dec;        // [large tasks | small tasks] of the level
+  Task* subs;           // subtree tasks (at most sub_max primitives), all levels
+  void* tiny;           // SubTask list: subtrees of at most kThreadMax primitives
+  Decision* dec;        // large tasks of the level
   float* tbox;          // 6 floats per large task (box with first offset)
   uint32_t* bins;       // kTaskBinWords per large task
   uint32_t* chunk_base; // large + 1
   uint32_t* chunk_status;
   uint64_t* scan_vals;  // per task of the level
   uint64_t* scan_sums;  // one per block
-  uint32_t* mqueue;     // small tasks queued for one warp each
+  DAabb* tnodes;        // subtree node pairs by split position: 2(m-1), 2(m-1)+1
+  uint32_t* sflag;      // 1 at the positions m where a subtree task splits
+  uint32_t* srank;      // exclusive scan of sflag
+  uint32_t* tile_off;   // per 4096-position tile: sums, then exclusive offsets
   Counters* cnt;
   GridBarrier* bar;
 };
@@ -361,10 +377,8 @@ struct SahParams {
 // barrier.
 struct Level {
   const Task* large;
-  const Task* small;
   Task* large_next;
-  Task* small_next;
-  uint32_t L, S, node_base;
+  uint32_t L, node_base, sub_base;
 };
 
 // Reads of data written earlier in the same launch (by any block) go to L2:
@@ -741,13 +755,14 @@ __device__ __forceinline__ uint32_t next_bin(uint32_t packed, uint32_t ws, int a
   return nb;
 }
 
-__device__ void small_task_thread(const SahParams& p, const Task& tk, uint32_t slot) {
-  const uint32_t ws = tk.end - tk.begin;
-  float mn[3], mx[3];
-  task_box(p.nodes, tk.node, mn, mx);
-  Decision d;
+// BinnedSahBuildTask::run (binned_sah.rs:132-282) after the node box is
+// known, for a task of at most kThreadMax primitives by one thread: `mn` /
+// `mx` is the node box with its first offset. On a split the task's indices
+// are left stably partitioned (left primitives first, in order).
+__device__ void decide_thread(const SahParams& p, uint32_t begin, uint32_t ws, uint32_t depth, const float mn[3],
+                              const float mx[3], Decision& d) {
   d.split = 0;
-  if (ws > 1 && tk.depth < kMaxDepth) {
+  if (ws > 1 && depth < kMaxDepth) {
     uint32_t prim[kThreadMax];
     uint32_t kb[kThreadMax][6];
     uint32_t packed[3] = {0u, 0u, 0u};
@@ -755,7 +770,7 @@ __device__ void small_task_thread(const SahParams& p, const Task& tk, uint32_t s
 #pragma unroll
     for (uint32_t j = 0; j < kThreadMax; ++j) {
       if (j < ws) {
-        prim[j] = __ldcg(p.idx_a + tk.begin + j);
+        prim[j] = p.idx_a[begin + j];
         const float4 c = __ldg(p.centers + prim[j]);
         const DAabb box = load_aabb(p.aabbs + prim[j]);
 #pragma unroll
@@ -836,8 +851,7 @@ __device__ void small_task_thread(const SahParams& p, const Task& tk, uint32_t s
           d.rbox[k] = rmn[k];
           d.rbox[3 + k] = rmx[k];
         }
-        // stable partition (left primitives first, in order)
-        uint32_t tpos = tk.begin, fpos = tk.begin + n_left;
+        uint32_t tpos = begin, fpos = begin + n_left;
 #pragma unroll
         for (uint32_t j = 0; j < kThreadMax; ++j) {
           if (j < ws) p.idx_a[((left >> j) & 1u) ? tpos++ : fpos++] = prim[j];
@@ -845,42 +859,29 @@ __device__ void small_task_thread(const SahParams& p, const Task& tk, uint32_t s
       }
     }
   }
-  if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
-  else write_leaf(p.nodes, tk, mn, mx);
-  p.dec[slot] = d;
 }
 
-// A small task of more than kThreadMax primitives, by one warp: bins in
-// shared memory, the warp-parallel decision, a ballot-based stable partition.
-__device__ void small_task_warp(const SahParams& p, const Task& tk, uint32_t slot, uint32_t* wb, uint32_t* sidx,
-                                Decision& d) {
+// The same for a task of more than kThreadMax primitives by one warp: bins
+// in shared memory (wb), indices staged in sidx, the warp-parallel decision,
+// a ballot-based stable partition. The decision is left in `d` (shared
+// memory, written by lane 0) for every lane.
+__device__ void decide_warp(const SahParams& p, uint32_t begin, uint32_t ws, uint32_t depth, const float mn[3],
+                            const float mx[3], uint32_t* wb, uint32_t* sidx, Decision& d) {
   const int lane = threadIdx.x & 31;
-  const uint32_t ws = tk.end - tk.begin;
-  float mn[3], mx[3];
-  task_box(p.nodes, tk.node, mn, mx);
   if (lane == 0) d.split = 0;
   __syncwarp();
-  if (ws > 1 && tk.depth < kMaxDepth && ws <= kWarpMax) {
+  if (ws > 1 && depth < kMaxDepth && ws <= kWarpMax) {
     init_bins(wb, lane, 32);
     // stage the task's indices (independent loads, all in flight at once)
-    for (uint32_t i = lane; i < ws; i += 32) sidx[i] = __ldcg(p.idx_a + tk.begin + i);
+    for (uint32_t i = lane; i < ws; i += 32) sidx[i] = p.idx_a[begin + i];
     __syncwarp();
     const BinMap bm = make_binmap(mn, mx);
-    for (uint32_t i = lane; i < ws; i += 32) {
-      const uint32_t prim = sidx[i];
-      const float4 c = __ldg(p.centers + prim);
-      const DAabb box = load_aabb(p.aabbs + prim);
-      const float cc[3] = {c.x, c.y, c.z};
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        uint32_t* b = wb + (a * kBins + bin_of(cc[a], bm.c2b[a], bm.off[a])) * kBinWords;
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          atomicMin(b + q, float_to_ordered(box.min[q]));
-          atomicMax(b + 3 + q, float_to_ordered(box.max[q]));
-        }
-        atomicAdd(b + 6, 1u);
-      }
+    {
+      // each lane bins a contiguous slice, merging runs of primitives that
+      // fall in one bin before its shared-memory atomics
+      const uint32_t per = (ws + 31) / 32;
+      const uint32_t lo = min(ws, (uint32_t)lane * per);
+      bin_run(p, bm, lo, min(ws, lo + per), [&](uint32_t i) { return sidx[i]; }, wb);
     }
     __syncwarp();
     {
@@ -909,10 +910,10 @@ __device__ void small_task_warp(const SahParams& p, const Task& tk, uint32_t slo
         const uint32_t V = __ballot_sync(0xffffffffu, valid);
         const uint32_t F = V & ~T;
         // written straight to the task's range: the staged copy is the source
-        if (pred) p.idx_a[tk.begin + tb + __popc(T & lt)] = prim;
+        if (pred) p.idx_a[begin + tb + __popc(T & lt)] = prim;
         else if (valid) {
           const uint32_t dst = n_left + fb + __popc(F & lt);
-          if (dst < ws) p.idx_a[tk.begin + dst] = prim;
+          if (dst < ws) p.idx_a[begin + dst] = prim;
         }
         tb += __popc(T);
         fb += __popc(F);
@@ -920,26 +921,183 @@ __device__ void small_task_warp(const SahParams& p, const Task& tk, uint32_t slo
     }
   }
   __syncwarp();
-  if (lane == 0) {
-    if (d.split) write_interior_box(p.nodes, tk.node, mn, mx);
-    else write_leaf(p.nodes, tk, mn, mx);
-    p.dec[slot] = d;
+}
+
+// ------------------------------------------------------------------ subtrees
+constexpr uint32_t kTemp = 0x80000000u;  // SubTask::loc bit: a scratch slot, else a node of the breadth-first part
+
+struct SubTask {
+  uint32_t loc, begin, end, depth;
+  float box[6];  // the box the parent gave the node (min xyz, max xyz), before the first offset
+};
+constexpr int kSubStack = (int)kMaxDepth + 2;
+constexpr int kSubBlock = 128;
+
+// Shared memory of one warp of k_sub_build.
+struct SubShared {
+  uint32_t bins[kTaskBinWords];
+  uint32_t idx[kWarpMax];
+  Decision dec;
+  SubTask stack[kSubStack];
+};
+
+__device__ __forceinline__ DAabb* sub_node(const SahParams& p, uint32_t loc) {
+  return (loc & kTemp) ? p.tnodes + (loc & ~kTemp) : p.nodes + loc;
+}
+
+// Writes task tk's node (mn / mx: its box with the first offset): an
+// interior node whose left_first is, until the relocation, the split
+// position m; or a leaf (make_leaf: second offset, first primitive, count).
+// On a split, notes m and returns the children.
+__device__ __forceinline__ bool sub_write(const SahParams& p, const SubTask& tk, const float mn[3], const float mx[3],
+                                          const Decision& d, SubTask& l, SubTask& r) {
+  DAabb b;
+  if (d.split) {
+    const uint32_t m = tk.begin + d.n_left;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      b.min[k] = mn[k];
+      b.max[k] = mx[k];
+    }
+    b.count = -1;
+    b.left_first = (int32_t)m;
+    store_aabb(sub_node(p, tk.loc), b);
+    p.sflag[m] = 1u;
+    l.loc = kTemp | (2u * (m - 1u));
+    l.begin = tk.begin;
+    l.end = m;
+    l.depth = tk.depth + 1u;
+    r.loc = kTemp | (2u * (m - 1u) + 1u);
+    r.begin = m;
+    r.end = tk.end;
+    r.depth = tk.depth + 1u;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      l.box[k] = d.lbox[k];
+      r.box[k] = d.rbox[k];
+    }
+    return true;
   }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    b.min[k] = mn[k] - 0.0001f;
+    b.max[k] = mx[k] + 0.0001f;
+  }
+  b.count = (int32_t)(tk.end - tk.begin);
+  b.left_first = (int32_t)tk.begin;
+  store_aabb(sub_node(p, tk.loc), b);
+  return false;
+}
+
+__device__ __forceinline__ void first_offset(const SubTask& tk, float mn[3], float mx[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    mn[k] = tk.box[k] - 0.0001f;
+    mx[k] = tk.box[3 + k] + 0.0001f;
+  }
+}
+
+// A subtree whose root holds at most kThreadMax primitives, by one lane,
+// depth first (at most kThreadMax - 1 splits, so the stack stays below
+// kThreadMax + 1 entries).
+__device__ void sub_tiny(const SahParams& p, const SubTask& t0) {
+  SubTask st[kThreadMax + 1];
+  int sp = 0;
+  st[0] = t0;
+  while (sp >= 0) {
+    const SubTask tk = st[sp--];
+    float mn[3], mx[3];
+    first_offset(tk, mn, mx);
+    Decision d;
+    decide_thread(p, tk.begin, tk.end - tk.begin, tk.depth, mn, mx, d);
+    SubTask l, r;
+    if (sub_write(p, tk, mn, mx, d, l, r)) {
+      if (sp + 2 >= (int)kThreadMax + 1) {
+        atomicOr(&p.cnt->status, kStatusBadIndex);
+        return;
+      }
+      st[++sp] = r;
+      st[++sp] = l;
+    }
+  }
+}
+
+// Appends a subtree of at most kThreadMax primitives to the list that
+// k_sub_tiny finishes, one thread per subtree.
+__device__ __forceinline__ void sub_list_tiny(const SahParams& p, const SubTask& t) {
+  const uint32_t k = atomicAdd(&p.cnt->tiny, 1u);
+  if (k < p.n) reinterpret_cast<SubTask*>(p.tiny)[k] = t;
+  else atomicOr(&p.cnt->status, kStatusBadIndex);
+}
+
+// One subtree by one warp, depth first: tasks of more than kThreadMax
+// primitives by the whole warp; smaller ones are listed for k_sub_tiny.
+// Every write goes to a place fixed by the task's primitive range, so the
+// order in which tasks run does not matter.
+__device__ void sub_warp_tree(const SahParams& p, const Task& root, SubShared& sh) {
+  const int lane = threadIdx.x & 31;
+  int sp = -1;  // warp-uniform
+  const uint32_t rws = root.end - root.begin;
+  if (lane == 0) {
+    const DAabb rb = load_aabb_cg(p.nodes + root.node);
+    SubTask t;
+    t.loc = root.node;
+    t.begin = root.begin;
+    t.end = root.end;
+    t.depth = root.depth;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      t.box[k] = rb.min[k];
+      t.box[3 + k] = rb.max[k];
+    }
+    if (rws <= kThreadMax) sub_list_tiny(p, t);
+    else sh.stack[0] = t;
+  }
+  if (rws > kThreadMax) sp = 0;
   __syncwarp();
+  while (sp >= 0) {
+    const SubTask tk = sh.stack[sp--];
+    float mn[3], mx[3];
+    first_offset(tk, mn, mx);
+    decide_warp(p, tk.begin, tk.end - tk.begin, tk.depth, mn, mx, sh.bins, sh.idx, sh.dec);
+    const Decision d = sh.dec;
+    __syncwarp();
+    SubTask l, r;
+    if (lane == 0) sub_write(p, tk, mn, mx, d, l, r);
+    if (d.split) {
+      const uint32_t nl = d.n_left, nr = (tk.end - tk.begin) - d.n_left;
+      if (sp + 2 >= kSubStack) {
+        if (lane == 0) atomicOr(&p.cnt->status, kStatusBadIndex);
+        return;
+      }
+      // right child first onto the stack: the left one is taken next
+      if (nr <= kThreadMax) {
+        if (lane == 0) sub_list_tiny(p, r);
+      } else {
+        if (lane == 0) sh.stack[sp + 1] = r;
+        ++sp;
+      }
+      if (nl <= kThreadMax) {
+        if (lane == 0) sub_list_tiny(p, l);
+      } else {
+        if (lane == 0) sh.stack[sp + 1] = l;
+        ++sp;
+      }
+    }
+    __syncwarp();
+  }
 }
 
 // ------------------------------------------------------------------ level scan + emit
-__device__ __forceinline__ uint64_t children_value(const Decision& d, const Task& tk) {
+__device__ __forceinline__ uint64_t children_value(const Decision& d, const Task& tk, uint32_t sub_max) {
   if (!d.split) return 0;
   const uint32_t ws = tk.end - tk.begin;
   const uint32_t nl = d.n_left, nr = ws - d.n_left;
-  const uint64_t large = (uint64_t)(nl > kWarpMax) + (uint64_t)(nr > kWarpMax);
+  const uint64_t large = (uint64_t)(nl > sub_max) + (uint64_t)(nr > sub_max);
   return (large << 32) | (uint64_t)(2u - (uint32_t)large);
 }
 
-__device__ __forceinline__ Task level_task(const Level& lv, uint32_t t) {
-  return t < lv.L ? ld_task(lv.large + t) : ld_task(lv.small + (t - lv.L));
-}
+__device__ __forceinline__ Task level_task(const Level& lv, uint32_t t) { return ld_task(lv.large + t); }
 
 template <class T>
 __device__ __forceinline__ T block_scan_incl(T v, T* s_warp, T* total) {
@@ -980,12 +1138,12 @@ __device__ __forceinline__ void segment(uint32_t N, uint32_t& lo, uint32_t& hi) 
 // (scan_vals) and the segment total (scan_sums[block]).
 __device__ void scan_segment(const SahParams& p, const Level& lv, SahShared& sh) {
   uint32_t lo, hi;
-  segment(lv.L + lv.S, lo, hi);
+  segment(lv.L, lo, hi);
   uint64_t carry = 0;
   for (uint32_t base = lo; base < hi; base += kLargeBlock) {
     const uint32_t t = base + threadIdx.x;
     uint64_t v = 0;
-    if (t < hi) v = children_value(ld_dec(p.dec + t), level_task(lv, t));
+    if (t < hi) v = children_value(ld_dec(p.dec + t), level_task(lv, t), p.sub_max);
     uint64_t total;
     const uint64_t incl = block_scan_incl<uint64_t>(v, sh.scan, &total);
     if (t < hi) p.scan_vals[t] = carry + incl - v;
@@ -994,7 +1152,8 @@ __device__ void scan_segment(const SahParams& p, const Level& lv, SahShared& sh)
   if (threadIdx.x == 0) p.scan_sums[blockIdx.x] = carry;
 }
 
-// Node numbering (breadth first) and the next level's task lists.
+// Node numbering (breadth first), the next level's task list and the
+// subtree list.
 __device__ void emit_segment(const SahParams& p, const Level& lv, SahShared& sh, bool advance) {
   // prefix of the block totals before this block, and the level total
   uint64_t before = 0, all = 0;
@@ -1009,7 +1168,7 @@ __device__ void emit_segment(const SahParams& p, const Level& lv, SahShared& sh,
   before = t0;
   all = t1;
   uint32_t lo, hi;
-  segment(lv.L + lv.S, lo, hi);
+  segment(lv.L, lo, hi);
   for (uint32_t t = lo + threadIdx.x; t < hi; t += kLargeBlock) {
     const Decision d = ld_dec(p.dec + t);
     if (!d.split) continue;
@@ -1035,55 +1194,16 @@ __device__ void emit_segment(const SahParams& p, const Level& lv, SahShared& sh,
     store_aabb(p.nodes + child + 1, rb);
     const Task lt{child, tk.begin, tk.begin + d.n_left, tk.depth + 1};
     const Task rt{child + 1, tk.begin + d.n_left, tk.end, tk.depth + 1};
-    if (lt.end - lt.begin > kWarpMax) lv.large_next[li++] = lt;
-    else lv.small_next[si++] = lt;
-    if (rt.end - rt.begin > kWarpMax) lv.large_next[li++] = rt;
-    else lv.small_next[si++] = rt;
+    if (lt.end - lt.begin > p.sub_max) lv.large_next[li++] = lt;
+    else p.subs[lv.sub_base + si++] = lt;
+    if (rt.end - rt.begin > p.sub_max) lv.large_next[li++] = rt;
+    else p.subs[lv.sub_base + si++] = rt;
   }
   if (advance && blockIdx.x == 0 && threadIdx.x == 0) {
     const uint32_t nl = (uint32_t)(all >> 32), ns = (uint32_t)(all & 0xffffffffu);
     p.cnt->node_count = lv.node_base + nl + ns;
     p.cnt->large = nl;
-    p.cnt->small = ns;
-    p.cnt->mq_count = 0;
-    p.cnt->mq_head = 0;
-  }
-}
-
-// Small tasks of the level: up to kThreadMax primitives by one thread each,
-// the rest queued for small_warp_phase. The order in which queued tasks run
-// does not matter: each writes only its own node, index range and decision.
-__device__ void small_thread_phase(const SahParams& p, const Level& lv) {
-  const int lane = threadIdx.x & 31;
-  for (uint32_t base = blockIdx.x * kLargeBlock; base < lv.S; base += gridDim.x * kLargeBlock) {
-    const uint32_t t = base + threadIdx.x;
-    bool big = false;
-    if (t < lv.S) {
-      const Task tk = ld_task(lv.small + t);
-      big = (tk.end - tk.begin) > kThreadMax && tk.depth < kMaxDepth;
-      if (!big) small_task_thread(p, tk, lv.L + t);
-    }
-    const uint32_t m = __ballot_sync(0xffffffffu, big);
-    if (m) {
-      uint32_t qb = 0;
-      if (lane == __ffs(m) - 1) qb = atomicAdd(&p.cnt->mq_count, (uint32_t)__popc(m));
-      qb = __shfl_sync(0xffffffffu, qb, __ffs(m) - 1);
-      if (big) p.mqueue[qb + __popc(m & ((1u << lane) - 1u))] = t;
-    }
-  }
-}
-
-// Every warp takes queued small tasks until the queue is empty.
-__device__ void small_warp_phase(const SahParams& p, const Level& lv, SahShared& sh) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t Q = __ldcg(&p.cnt->mq_count);
-  for (;;) {
-    uint32_t q = 0;
-    if (lane == 0) q = atomicAdd(&p.cnt->mq_head, 1u);
-    q = __shfl_sync(0xffffffffu, q, 0);
-    if (q >= Q) break;
-    const uint32_t t = __ldcg(p.mqueue + q);
-    small_task_warp(p, ld_task(lv.small + t), lv.L + t, &sh.bins[warp][0], &sh.idx[warp][0], sh.dec[warp]);
+    p.cnt->sub = lv.sub_base + ns;
   }
 }
 
@@ -1102,18 +1222,16 @@ __device__ void large_partition_phase(const SahParams& p, const Level& lv, uint3
 __device__ __forceinline__ Level read_level(const SahParams& p, uint32_t level) {
   Level lv;
   lv.L = __ldcg(&p.cnt->large);
-  lv.S = __ldcg(&p.cnt->small);
   lv.node_base = __ldcg(&p.cnt->node_count);
+  lv.sub_base = __ldcg(&p.cnt->sub);
   lv.large = p.large[level & 1];
-  lv.small = p.small[level & 1];
   lv.large_next = p.large[(level + 1) & 1];
-  lv.small_next = p.small[(level + 1) & 1];
   return lv;
 }
 
-// The whole build: one cooperative launch, the levels of the tree one after
-// another, phases separated by grid barriers. Level l reads task lists
-// large[l & 1] / small[l & 1] and writes the other pair.
+// The breadth-first part of the build: one cooperative launch, the levels of
+// the tree one after another, phases separated by grid barriers. Level l
+// reads task list large[l & 1] and writes the other one.
 __global__ void __launch_bounds__(kLargeBlock, 2) k_sah_build(SahParams p) {
   __shared__ SahShared sh;
   const uint32_t G = gridDim.x;
@@ -1121,7 +1239,7 @@ __global__ void __launch_bounds__(kLargeBlock, 2) k_sah_build(SahParams p) {
   uint32_t* status = &p.cnt->status;
   for (uint32_t level = 0;; ++level) {
     const Level lv = read_level(p, level);
-    if (lv.L + lv.S == 0) break;
+    if (lv.L == 0) break;
     if (level > kMaxDepth + 1) {
       if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, kStatusBadIndex);
       break;
@@ -1136,11 +1254,9 @@ __global__ void __launch_bounds__(kLargeBlock, 2) k_sah_build(SahParams p) {
       if (!grid_sync(p.bar, G, status)) return;
       for (uint32_t t = gwarp; t < lv.L; t += nwarps) large_decide(p, lv, t, sh);
     }
-    small_thread_phase(p, lv);
     if (!grid_sync(p.bar, G, status)) return;
-    // large partitions (chunks in ticket order), then queued small tasks
+    // large partitions (chunks in ticket order)
     if (lv.L > 0) large_partition_phase(p, lv, chunks, sh);
-    small_warp_phase(p, lv, sh);
     if (!grid_sync(p.bar, G, status)) return;
     if (lv.L > 0) {
       for (uint32_t c = blockIdx.x; c < chunks; c += G) large_copyback_chunk(p, lv, c);
@@ -1181,17 +1297,10 @@ __global__ void __launch_bounds__(kLargeBlock) k_ph_decide(SahParams p, uint32_t
   const uint32_t gwarp = (blockIdx.x * kLargeBlock + threadIdx.x) >> 5, nwarps = gridDim.x * (kLargeBlock / 32);
   for (uint32_t t = gwarp; t < lv.L; t += nwarps) large_decide(p, lv, t, sh);
 }
-__global__ void __launch_bounds__(kLargeBlock) k_ph_small(SahParams p, uint32_t level) {
-  small_thread_phase(p, read_level(p, level));
-}
 __global__ void __launch_bounds__(kLargeBlock) k_ph_partition(SahParams p, uint32_t level) {
   SahShared& sh = dyn_shared();
   const Level lv = read_level(p, level);
   large_partition_phase(p, lv, __ldcg(&p.cnt->chunks), sh);
-}
-__global__ void __launch_bounds__(kLargeBlock) k_ph_small_warps(SahParams p, uint32_t level) {
-  SahShared& sh = dyn_shared();
-  small_warp_phase(p, read_level(p, level), sh);
 }
 __global__ void __launch_bounds__(kLargeBlock) k_ph_copyback_scan(SahParams p, uint32_t level) {
   SahShared& sh = dyn_shared();
@@ -1220,11 +1329,127 @@ __global__ void k_ph_advance(SahParams p, uint32_t level, uint32_t blocks) {
     const uint32_t nl = (uint32_t)(tot >> 32), ns = (uint32_t)(tot & 0xffffffffu);
     p.cnt->node_count = lv.node_base + nl + ns;
     p.cnt->large = nl;
-    p.cnt->small = ns;
-    p.cnt->mq_count = 0;
-    p.cnt->mq_head = 0;
+    p.cnt->sub = lv.sub_base + ns;
   }
 }
+
+// ---- subtrees and their placement
+__global__ void __launch_bounds__(kSubBlock) k_sub_build(SahParams p) {
+  extern __shared__ __align__(16) unsigned char sub_dyn[];
+  SubShared& sh = reinterpret_cast<SubShared*>(sub_dyn)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const uint32_t S = __ldcg(&p.cnt->sub);
+  for (;;) {
+    uint32_t t = 0;
+    if (lane == 0) t = atomicAdd(&p.cnt->sub_head, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= S) break;
+    sub_warp_tree(p, ld_task(p.subs + t), sh);
+  }
+}
+
+// The listed subtrees of at most kThreadMax primitives, one thread each.
+__global__ void __launch_bounds__(kLargeBlock) k_sub_tiny(SahParams p) {
+  const uint32_t T = __ldcg(&p.cnt->tiny);
+  const SubTask* list = reinterpret_cast<const SubTask*>(p.tiny);
+  for (uint32_t t = blockIdx.x * kLargeBlock + threadIdx.x; t < T && t < p.n; t += gridDim.x * kLargeBlock)
+    sub_tiny(p, list[t]);
+}
+
+constexpr uint32_t kScanTile = 4096;  // split positions per tile: 1024 threads x 4
+
+__global__ void __launch_bounds__(1024) k_tile_sums(const uint32_t* __restrict__ flag, uint32_t n,
+                                                    uint32_t* __restrict__ tile_off) {
+  __shared__ uint32_t s_warp[32];
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * 4u;
+  uint32_t v = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k)
+    if (base + k < n) v += flag[base + k];
+  uint32_t total;
+  block_inclusive_scan<1024>(v, s_warp, &total);
+  if (threadIdx.x == 0) tile_off[blockIdx.x] = total;
+}
+
+// Exclusive offsets of the tiles (one block); the total is the number of
+// splits inside the subtrees.
+__global__ void __launch_bounds__(1024) k_tile_scan(uint32_t* __restrict__ tile_off, uint32_t tiles, Counters* cnt) {
+  __shared__ uint32_t s_warp[32];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < tiles; base += 1024) {
+    const uint32_t t = base + threadIdx.x;
+    const uint32_t v = t < tiles ? tile_off[t] : 0u;
+    uint32_t total;
+    const uint32_t incl = block_inclusive_scan<1024>(v, s_warp, &total);
+    if (t < tiles) tile_off[t] = carry + incl - v;
+    carry += total;
+  }
+  if (threadIdx.x == 0) cnt->sub_splits = carry;
+}
+
+__global__ void __launch_bounds__(1024) k_rank(const uint32_t* __restrict__ flag, uint32_t n,
+                                               const uint32_t* __restrict__ tile_off, uint32_t* __restrict__ rank) {
+  __shared__ uint32_t s_warp[32];
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * 4u;
+  uint32_t f[4], v = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    f[k] = base + k < n ? flag[base + k] : 0u;
+    v += f[k];
+  }
+  uint32_t total;
+  uint32_t x = block_inclusive_scan<1024>(v, s_warp, &total) - v + tile_off[blockIdx.x];
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    if (base + k < n) rank[base + k] = x;
+    x += f[k];
+  }
+}
+
+// The node pair of subtree split m goes to top + 2 rank[m] (top: the nodes
+// of the breadth-first part); interior nodes get their children's final
+// index.
+__global__ void __launch_bounds__(kLargeBlock) k_relocate(SahParams p) {
+  const uint32_t m = blockIdx.x * kLargeBlock + threadIdx.x;
+  if (m == 0 || m >= p.n || !p.sflag[m]) return;
+  const uint32_t top = __ldcg(&p.cnt->node_count);
+  const uint32_t pair = top + 2u * p.srank[m];
+  if (pair + 1u >= 2u * p.n - 1u) {  // past the 2n - 1 nodes
+    atomicOr(&p.cnt->status, kStatusBadIndex);
+    return;
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < 2; ++k) {
+    DAabb nd = load_aabb(p.tnodes + 2u * (m - 1u) + k);
+    if (nd.count < 0) {
+      const uint32_t c = (uint32_t)nd.left_first;
+      if (c == 0 || c >= p.n) {
+        atomicOr(&p.cnt->status, kStatusBadIndex);
+        return;
+      }
+      nd.left_first = (int32_t)(top + 2u * p.srank[c]);
+    }
+    store_aabb(p.nodes + pair + k, nd);
+  }
+}
+
+// Subtree roots (nodes of the breadth-first part) that split.
+__global__ void __launch_bounds__(kLargeBlock) k_fix_roots(SahParams p) {
+  const uint32_t S = __ldcg(&p.cnt->sub), top = __ldcg(&p.cnt->node_count);
+  for (uint32_t t = blockIdx.x * kLargeBlock + threadIdx.x; t < S && t < p.n + 1u; t += gridDim.x * kLargeBlock) {
+    const Task tk = p.subs[t];
+    DAabb nd = load_aabb(p.nodes + tk.node);
+    if (nd.count >= 0) continue;
+    const uint32_t c = (uint32_t)nd.left_first;
+    if (c == 0 || c >= p.n) {
+      atomicOr(&p.cnt->status, kStatusBadIndex);
+      continue;
+    }
+    nd.left_first = (int32_t)(top + 2u * p.srank[c]);
+    store_aabb(p.nodes + tk.node, nd);
+  }
+}
+
 
 __global__ void k_sah_init(SahParams p, const DAabb* world) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1232,21 +1457,23 @@ __global__ void k_sah_init(SahParams p, const DAabb* world) {
   if (i == 0) {
     store_aabb(p.nodes, *world);
     const Task root{0u, 0u, p.n, 0u};
-    if (p.n > kWarpMax) {
+    if (p.n > p.sub_max) {
       p.large[0][0] = root;
       p.cnt->large = 1;
-      p.cnt->small = 0;
+      p.cnt->sub = 0;
     } else {
-      p.small[0][0] = root;
+      p.subs[0] = root;
       p.cnt->large = 0;
-      p.cnt->small = 1;
+      p.cnt->sub = 1;
     }
     p.cnt->node_count = 1;
     p.cnt->status = 0;
     p.cnt->chunks = 0;
     p.cnt->ticket = 0;
-    p.cnt->mq_count = 0;
-    p.cnt->mq_head = 0;
+    p.cnt->sub_head = 0;
+    p.cnt->sub_splits = 0;
+    p.cnt->tiny = 0;
+    p.cnt->tiny_head = 0;
   }
 }
 
@@ -1271,15 +1498,16 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
     pool_free(indices, s);
     return rc;
   };
-  // Small builds run as one cooperative launch with a grid sized to the
-  // problem (fewer blocks make each grid barrier cheaper); large builds
-  // launch the phases separately, which lets each phase run at its own
-  // occupancy, and read the level's counts back between levels.
+  // The breadth-first part of small builds runs as one cooperative launch
+  // with a grid sized to the problem (fewer blocks make each grid barrier
+  // cheaper); large builds launch the phases separately, which lets each
+  // phase run at its own occupancy, and read the level's counts back
+  // between levels.
   const bool coop = n <= kCoopMaxPrims;
   int per_sm = 0;
   if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop ? (const void*)k_sah_build
-                                                                         : (const void*)k_ph_small_warps,
-                                                         kLargeBlock, coop ? 0 : sizeof(SahShared))))
+                                                                         : (const void*)k_ph_partition,
+                                                         kLargeBlock, coop ? 0 : kShSmall)))
     return fail(cuda_rc(e));
   if (per_sm < 1) return fail(DeviceError);
   uint32_t grid = (uint32_t)sm_count() * (uint32_t)per_sm;
@@ -1287,13 +1515,16 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
     const uint32_t want = (n + kCoopPrimsPerBlock - 1) / kCoopPrimsPerBlock;
     if (want < grid) grid = want;
   }
-  const uint32_t large_cap = n / (kWarpMax + 1) + 2;
-  const uint32_t small_cap = n + 1;
-  const uint32_t task_cap = large_cap + small_cap;
+  uint32_t sub_max = n / 2048u;
+  sub_max = sub_max < 32u ? 32u : (sub_max > kWarpMax ? kWarpMax : sub_max);
+  const uint32_t large_cap = n / (sub_max + 1) + 2;
+  const uint32_t sub_cap = n + 1;
   const uint32_t chunk_cap = n / kChunk + large_cap + 2;
-  Scratch<DAabb> world;
-  Scratch<uint32_t> acc, idx_b, bins, chunk_base, chunk_status, mqueue;
-  Scratch<Task> large0, large1, small0, small1;
+  const uint32_t tiles = (n + kScanTile - 1) / kScanTile;
+  Scratch<DAabb> world, tnodes;
+  Scratch<uint32_t> acc, idx_b, bins, chunk_base, chunk_status, sflag, srank, tile_off;
+  Scratch<Task> large0, large1, subs;
+  Scratch<SubTask> tiny;
   Scratch<Decision> dec;
   Scratch<float> tbox;
   Scratch<uint64_t> scan_vals, scan_sums;
@@ -1302,13 +1533,14 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   if ((e = world.alloc(1, s)) || (e = acc.alloc(8, s)) || (e = idx_b.alloc(n, s)) ||
       (e = bins.alloc((size_t)large_cap * kTaskBinWords, s)) || (e = chunk_base.alloc(large_cap + 1, s)) ||
       (e = chunk_status.alloc(chunk_cap, s)) || (e = large0.alloc(large_cap, s)) || (e = large1.alloc(large_cap, s)) ||
-      (e = small0.alloc(small_cap, s)) || (e = small1.alloc(small_cap, s)) || (e = dec.alloc(task_cap, s)) ||
-      (e = tbox.alloc((size_t)large_cap * 6, s)) || (e = scan_vals.alloc(task_cap, s)) ||
-      (e = scan_sums.alloc(grid, s)) || (e = cnt.alloc(1, s)) || (e = mqueue.alloc(small_cap, s)) ||
-      (e = bar.alloc(1, s)))
+      (e = subs.alloc(sub_cap, s)) || (e = dec.alloc(large_cap, s)) || (e = tbox.alloc((size_t)large_cap * 6, s)) ||
+      (e = scan_vals.alloc(large_cap, s)) || (e = scan_sums.alloc(grid, s)) || (e = cnt.alloc(1, s)) ||
+      (e = bar.alloc(1, s)) || (e = tnodes.alloc(2 * (size_t)n, s)) || (e = sflag.alloc(n, s)) ||
+      (e = srank.alloc(n, s)) || (e = tile_off.alloc(tiles + 1, s)) || (e = tiny.alloc(n, s)))
     return fail(cuda_rc(e));
   if ((e = cudaMemsetAsync(chunk_status.ptr, 0, (size_t)chunk_cap * 4, s)) ||
-      (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
+      (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)) ||
+      (e = cudaMemsetAsync(sflag.ptr, 0, (size_t)n * 4, s)))
     return fail(cuda_rc(e));
   if ((e = launch_world_bounds(aabbs, n, world.ptr, acc.ptr, s))) return fail(cuda_rc(e));
 
@@ -1319,11 +1551,12 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   p.idx_a = indices;
   p.idx_b = idx_b.ptr;
   p.n = n;
+  p.sub_max = sub_max;
   p.max_leaf = prims_per_leaf == 0 ? 1u : (uint32_t)(prims_per_leaf > 0xffffffffu ? 0xffffffffu : prims_per_leaf);
   p.large[0] = large0.ptr;
   p.large[1] = large1.ptr;
-  p.small[0] = small0.ptr;
-  p.small[1] = small1.ptr;
+  p.subs = subs.ptr;
+  p.tiny = tiny.ptr;
   p.dec = dec.ptr;
   p.tbox = tbox.ptr;
   p.bins = bins.ptr;
@@ -1331,49 +1564,83 @@ ResultCode build_binned_sah(const DAabb* aabbs, const float4* centers, size_t n_
   p.chunk_status = chunk_status.ptr;
   p.scan_vals = scan_vals.ptr;
   p.scan_sums = scan_sums.ptr;
-  p.mqueue = mqueue.ptr;
+  p.tnodes = tnodes.ptr;
+  p.sflag = sflag.ptr;
+  p.srank = srank.ptr;
+  p.tile_off = tile_off.ptr;
   p.cnt = cnt.ptr;
   p.bar = bar.ptr;
   k_sah_init<<<(n + 255) / 256, 256, 0, s>>>(p, world.ptr);
   Counters h{};
-  if (coop) {
-    void* args[] = {&p};
-    if ((e = cudaLaunchCooperativeKernel((void*)k_sah_build, dim3(grid), dim3(kLargeBlock), args, 0, s)))
-      return fail(cuda_rc(e));
-    if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
-        (e = cudaStreamSynchronize(s)))
-      return fail(cuda_rc(e));
-  } else {
-    h.large = n > kWarpMax ? 1u : 0u;
-    h.small = 1u - h.large;
-    const size_t cap = (size_t)grid;
-    auto blocks = [cap](size_t need) { return (unsigned)(need < 1 ? 1 : (need < cap ? need : cap)); };
-    for (uint32_t level = 0; h.large + h.small > 0; ++level) {
-      if (level > kMaxDepth + 1) return fail(Error);
-      if (h.large) {
+  if (n > sub_max) {
+    if (coop) {
+      // the subtree stage below reads the counts it needs on the device
+      void* args[] = {&p};
+      if ((e = cudaLaunchCooperativeKernel((void*)k_sah_build, dim3(grid), dim3(kLargeBlock), args, 0, s)))
+        return fail(cuda_rc(e));
+    } else {
+      h.large = 1u;
+      const size_t cap = (size_t)grid;
+      auto blocks = [cap](size_t need) { return (unsigned)(need < 1 ? 1 : (need < cap ? need : cap)); };
+      for (uint32_t level = 0; h.large > 0; ++level) {
+        if (level > kMaxDepth + 1) return fail(Error);
         k_ph_prep<<<blocks(((size_t)h.large * 3 * kBins + kLargeBlock - 1) / kLargeBlock), kLargeBlock, kShSmall,
                     s>>>(p, level);
         k_ph_bin<<<grid, kLargeBlock, kShBins, s>>>(p, level);
         k_ph_decide<<<blocks((h.large + 7) / 8), kLargeBlock, kShBins, s>>>(p, level);
+        k_ph_partition<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
+        k_ph_copyback_scan<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
+        k_ph_emit<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
+        k_ph_advance<<<1, kLargeBlock, kShSmall, s>>>(p, level, grid);
+        if ((e = cudaGetLastError())) return fail(cuda_rc(e));
+        if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
+            (e = cudaStreamSynchronize(s)))
+          return fail(cuda_rc(e));
+        if (h.status) break;
       }
-      if (h.small) k_ph_small<<<(h.small + kLargeBlock - 1) / kLargeBlock, kLargeBlock, 0, s>>>(p, level);
-      if (h.large) k_ph_partition<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
-      if (h.small) k_ph_small_warps<<<grid, kLargeBlock, sizeof(SahShared), s>>>(p, level);
-      k_ph_copyback_scan<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
-      k_ph_emit<<<grid, kLargeBlock, kShSmall, s>>>(p, level);
-      k_ph_advance<<<1, kLargeBlock, kShSmall, s>>>(p, level, grid);
-      if ((e = cudaGetLastError())) return fail(cuda_rc(e));
-      if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
-          (e = cudaStreamSynchronize(s)))
-        return fail(cuda_rc(e));
-      if (h.status) break;
     }
+    if (h.status) return fail(h.status & kStatusTimeout ? Timeout : Error);
+    if (h.large > 0) return fail(Error);
   }
-  if (h.status) return fail(h.status & kStatusTimeout ? Timeout : Error);
-  if (h.large + h.small > 0) return fail(Error);
+  // subtrees, then their node pairs after the breadth-first part (the
+  // kernels read the subtree count and the breadth-first node count on the
+  // device)
+  {
+    int sub_per_sm = 0;
+    const size_t sub_smem = (kSubBlock / 32) * sizeof(SubShared);
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sub_per_sm, k_sub_build, kSubBlock, sub_smem)))
+      return fail(cuda_rc(e));
+    if (sub_per_sm < 1) return fail(DeviceError);
+    uint32_t sub_grid = (uint32_t)sm_count() * (uint32_t)sub_per_sm;
+    const uint32_t want = (n / (sub_max > 8u ? 8u : sub_max) + kSubBlock / 32) / (kSubBlock / 32) + 1u;
+    if (want < sub_grid) sub_grid = want;
+    k_sub_build<<<sub_grid, kSubBlock, sub_smem, s>>>(p);
+    {
+      int tiny_per_sm = 0;
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tiny_per_sm, k_sub_tiny, kLargeBlock, 0)))
+        return fail(cuda_rc(e));
+      const uint32_t tiny_grid = (uint32_t)sm_count() * (uint32_t)(tiny_per_sm < 1 ? 1 : tiny_per_sm);
+      k_sub_tiny<<<tiny_grid, kLargeBlock, 0, s>>>(p);
+    }
+    k_tile_sums<<<tiles, 1024, 0, s>>>(sflag.ptr, n, tile_off.ptr);
+    k_tile_scan<<<1, 1024, 0, s>>>(tile_off.ptr, tiles, cnt.ptr);
+    k_rank<<<tiles, 1024, 0, s>>>(sflag.ptr, n, tile_off.ptr, srank.ptr);
+    k_relocate<<<(n + kLargeBlock - 1) / kLargeBlock, kLargeBlock, 0, s>>>(p);
+    const unsigned fix_blocks = (unsigned)((n + kLargeBlock) / kLargeBlock);
+    k_fix_roots<<<fix_blocks < (unsigned)sm_count() * 4u ? fix_blocks : (unsigned)sm_count() * 4u, kLargeBlock, 0,
+                  s>>>(p);
+    if ((e = cudaGetLastError())) return fail(cuda_rc(e));
+    if ((e = cudaMemcpyAsync(&h, cnt.ptr, sizeof(Counters), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+      return fail(cuda_rc(e));
+    if (h.status) return fail(h.status & kStatusTimeout ? Timeout : Error);
+    if (h.large > 0) return fail(Error);  // the breadth-first part did not finish
+  }
+  const uint64_t total = (uint64_t)h.node_count + 2ull * h.sub_splits;
+  if (total > node_cap) return fail(Error);
   out->nodes = nodes;
   out->indices = indices;
-  out->node_count = h.node_count;
+  out->node_count = (uint32_t)total;
   return Ok;
 }
 

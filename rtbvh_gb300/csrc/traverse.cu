@@ -483,8 +483,10 @@ __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RaySta
 // inverse direction beyond kQuantRange, an origin beyond kCompactRange, or a
 // node flagged out of range on the way -- are appended to `deferred` and
 // traced afterwards by k_trace_mbvh over the exact Mbvh.
+// Nine resident blocks per SM (56 registers, 36 warps; a few bytes of
+// spills): measured 4 % faster than the 64-register, 32-warp form.
 template <int STACK>
-__global__ void __launch_bounds__(kBlock) k_trace_compact(TraceArgs a, unsigned int* work, uint32_t* deferred,
+__global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsigned int* work, uint32_t* deferred,
                                                            unsigned int* deferred_count) {
   RayState ray;
   float hu = 0.0f, hv = 0.0f;
