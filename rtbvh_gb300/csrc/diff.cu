@@ -83,40 +83,55 @@ __global__ void __launch_bounds__(kBlock)
   gr[5] = a.t * a.lz;
 }
 
-__device__ __forceinline__ uint32_t lower_bound(const uint32_t* __restrict__ keys, uint32_t n, uint32_t key) {
-  uint32_t lo = 0, hi = n;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi) >> 1;
-    if (__ldg(keys + mid) < key) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
+// Each triangle's range [begin, end) in the sorted (prim, ray) pairs: the
+// first and last position of every run of equal keys (triangles hit by no
+// ray keep begin = end = 0 from the memset).
+__global__ void __launch_bounds__(kBlock) k_bwd_ranges(const uint32_t* __restrict__ keys, uint32_t ray_count,
+                                                       uint32_t prim_count, uint2* __restrict__ range) {
+  const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+  if (k >= ray_count) return;
+  const uint32_t key = __ldg(keys + k);
+  if (key >= prim_count) return;  // rays without a hit sort last
+  if (k == 0 || __ldg(keys + k - 1) != key) range[key].x = k;
+  if (k + 1 == ray_count || __ldg(keys + k + 1) != key) range[key].y = k + 1;
 }
 
-// One thread per triangle sums its rays in ray-index order.
+// One warp per triangle: lane l takes the triangle's rays l, l + 32, ...
+// (in ray-index order within the lane), then the nine sums are reduced
+// across the lanes by a fixed butterfly, so the result is the same on
+// every run.
 __global__ void __launch_bounds__(kBlock)
     k_bwd_vertices(const float* __restrict__ vertices, uint32_t prim_count, const float* __restrict__ rays,
                    const float4* __restrict__ hits, const float* __restrict__ grad_tuv, uint32_t ray_count,
-                   const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                   const uint2* __restrict__ range, const uint32_t* __restrict__ vals,
                    float* __restrict__ grad_vertices) {
-  const uint32_t p = blockIdx.x * kBlock + threadIdx.x;
-  if (p >= prim_count) return;
-  const uint32_t lo = lower_bound(keys, ray_count, p);
-  const uint32_t hi = lower_bound(keys, ray_count, p + 1);
-  float g0x = 0, g0y = 0, g0z = 0, g1x = 0, g1y = 0, g1z = 0, g2x = 0, g2y = 0, g2z = 0;
+  const uint32_t p = (blockIdx.x * kBlock + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (p >= prim_count) return;  // warp-uniform
+  const uint2 rg = range[p];
+  const uint32_t lo = rg.x, hi = rg.y <= ray_count ? rg.y : ray_count;
+  float g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   const float* tri = vertices + 9 * (size_t)p;
-  for (uint32_t k = lo; k < hi; ++k) {
+  for (uint32_t k = lo + (uint32_t)lane; k < hi; k += 32) {
     const uint32_t r = __ldg(vals + k);
     const Adjoint a = adjoint(tri, rays + 6 * (size_t)r, hits[r], grad_tuv + 3 * (size_t)r);
     const float w0 = -(1.0f - a.u - a.v), w1 = -a.u, w2 = -a.v;
-    g0x += w0 * a.lx; g0y += w0 * a.ly; g0z += w0 * a.lz;
-    g1x += w1 * a.lx; g1y += w1 * a.ly; g1z += w1 * a.lz;
-    g2x += w2 * a.lx; g2y += w2 * a.ly; g2z += w2 * a.lz;
+    g[0] += w0 * a.lx; g[1] += w0 * a.ly; g[2] += w0 * a.lz;
+    g[3] += w1 * a.lx; g[4] += w1 * a.ly; g[5] += w1 * a.lz;
+    g[6] += w2 * a.lx; g[7] += w2 * a.ly; g[8] += w2 * a.lz;
   }
-  float* gv = grad_vertices + 9 * (size_t)p;
-  gv[0] = g0x; gv[1] = g0y; gv[2] = g0z;
-  gv[3] = g1x; gv[4] = g1y; gv[5] = g1z;
-  gv[6] = g2x; gv[7] = g2y; gv[8] = g2z;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) g[q] += __shfl_xor_sync(0xffffffffu, g[q], off);
+  }
+  if (lane < 9) {
+    float v = g[0];
+#pragma unroll
+    for (int q = 1; q < 9; ++q)
+      if (lane == q) v = g[q];
+    grad_vertices[9 * (size_t)p + lane] = v;
+  }
 }
 
 }  // namespace
@@ -132,19 +147,25 @@ cudaError_t launch_intersect_backward(const float* vertices, size_t prim_count, 
   }
   const uint32_t n = (uint32_t)prim_count, R = (uint32_t)ray_count;
   Scratch<uint32_t> keys, vals, status;
+  Scratch<uint2> range;
   Scratch<char> temp;
   const size_t tb = radix_sort_temp_bytes(R);
-  if ((e = keys.alloc(R, s)) || (e = vals.alloc(R, s)) || (e = status.alloc(1, s)) || (e = temp.alloc(tb, s)))
+  if ((e = keys.alloc(R, s)) || (e = vals.alloc(R, s)) || (e = status.alloc(1, s)) || (e = temp.alloc(tb, s)) ||
+      (e = range.alloc(n + 1, s)))
     return e;
-  if ((e = cudaMemsetAsync(status.ptr, 0, 4, s))) return e;
+  if ((e = cudaMemsetAsync(status.ptr, 0, 4, s)) || (e = cudaMemsetAsync(range.ptr, 0, (size_t)(n + 1) * 8, s)))
+    return e;
   k_bwd_rays<<<(R + kBlock - 1) / kBlock, kBlock, 0, s>>>(vertices, n, rays, hits, grad_tuv, R, grad_rays, keys.ptr,
                                                          vals.ptr);
   int bits = 1;
   while (bits < 31 && (1u << bits) <= n) ++bits;  // keys are in [0, n]
   if ((e = radix_sort_pairs(keys.ptr, vals.ptr, R, bits, temp.ptr, tb, status.ptr, s))) return e;
   if (n) {
-    k_bwd_vertices<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(vertices, n, rays, hits, grad_tuv, R, keys.ptr,
-                                                               vals.ptr, grad_vertices);
+    k_bwd_ranges<<<(R + kBlock - 1) / kBlock, kBlock, 0, s>>>(keys.ptr, R, n, range.ptr);
+    const size_t threads = (size_t)n * 32;
+    k_bwd_vertices<<<(unsigned)((threads + kBlock - 1) / kBlock), kBlock, 0, s>>>(vertices, n, rays, hits, grad_tuv,
+                                                                                 R, range.ptr, vals.ptr,
+                                                                                 grad_vertices);
   }
   return cudaGetLastError();
 }

@@ -1348,8 +1348,10 @@ __global__ void __launch_bounds__(kSubBlock) k_sub_build(SahParams p) {
   }
 }
 
-// The listed subtrees of at most kThreadMax primitives, one thread each.
-__global__ void __launch_bounds__(kLargeBlock) k_sub_tiny(SahParams p) {
+// The listed subtrees of at most kThreadMax primitives, one thread each
+// (two blocks per SM: 128 registers, 16 bytes of spills, twice the warps of
+// the unbounded 143-register form).
+__global__ void __launch_bounds__(kLargeBlock, 2) k_sub_tiny(SahParams p) {
   const uint32_t T = __ldcg(&p.cnt->tiny);
   const SubTask* list = reinterpret_cast<const SubTask*>(p.tiny);
   for (uint32_t t = blockIdx.x * kLargeBlock + threadIdx.x; t < T && t < p.n; t += gridDim.x * kLargeBlock)
