@@ -133,3 +133,52 @@ def test_batch_tuning_keeps_results(lib):
     with pytest.raises(rb.RtbvhError):
         batch.set_tuning(trace_stack=40)
 
+
+
+def test_batch_config_sized_meshes_match_the_oracle(lib):
+    """Meshes built as the batched workload builds them (perturbed spheres,
+    round(2000 sqrt(n)) incoherent rays each), the largest at the workload's
+    upper size of 200,000 triangles: every mesh's nodes equal the oracle's
+    LOCB build and its hits the oracle's traversal (the same nearest hit;
+    primitive ids shifted by the mesh's offset)."""
+    import math
+    import os
+
+    import oracle
+    from gpu_helpers import assert_same_nearest
+    torch.cuda.set_device(0)
+    rng = np.random.Generator(np.random.PCG64(45))
+    sizes = [200_000, 64, 37_000, 1_500]
+    parts, rays, po, ro = [], [], [0], [0]
+    for m, n in enumerate(sizes):
+        cells = max(2, n // 2)
+        n_lat = max(2, int(round(math.sqrt(cells / 2.0))))
+        n_lon = max(3, int(round(cells / n_lat)))
+        centre = tuple(rng.uniform(-5, 5, size=3))
+        t = scenes.sphere_fast(n_lon, n_lat, radius=1.0, noise=0.05, seed=450000 + m, center=centre)
+        r, _ = scenes.incoherent_rays(int(round(2000 * math.sqrt(len(t)))), seed=455000 + m,
+                                      center=(0.0, 0.0, 0.0), radius=2.0, lo=-1.0, hi=1.0)
+        r[:, :3] += np.asarray(centre, dtype=np.float32)
+        parts.append(t)
+        rays.append(r)
+        po.append(po[-1] + len(t))
+        ro.append(ro[-1] + len(r))
+    tris, allr = np.concatenate(parts), np.concatenate(rays)
+    batch = rb.Batch(to_cuda(tris), po, to_cuda(allr), ro)
+    hits = batch.run().cpu().numpy()
+    assert batch.status() == rb.ResultCode.Ok
+    v = batch.view()
+    nodes = rb.device_copy(v.nodes, (v.node_capacity, 8))
+    threads = os.cpu_count() or 1
+    for m in range(len(sizes)):
+        off, n, nbase = po[m], po[m + 1] - po[m], 2 * po[m] - m
+        mt = tris[off:off + n]
+        a, c = oracle.triangle_prep(mt)
+        on, oi = oracle.build(a, c, "locb", threads=threads)
+        assert np.array_equal(u32(nodes[nbase:nbase + len(on)]), u32(shifted_nodes(on, nbase, off))), m
+        mr = allr[ro[m]:ro[m + 1]]
+        oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, mt.reshape(-1, 9), mr, threads=threads, stats=False)
+        hb = hits[ro[m]:ro[m + 1]].copy()
+        p = rb.hit_prims(hb)
+        hb[:, 3] = np.where(p >= 0, p - off, p).astype(np.int32).view(np.float32)
+        assert_same_nearest(hb, oh, mt, mr)
