@@ -231,7 +231,10 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
 /* Attaches device triangles (prim-id order) to a Bvh (is_mbvh = 0) or Mbvh
  * (is_mbvh = 1) for the fused traversal; they are re-laid in leaf order
  * (v0, v1-v0, v2-v0). Structures built by rtbvh_gpu_create_bvh_from_triangles
- * (and Mbvhs made from them) already carry them. */
+ * (and Mbvhs made from them) already carry them. An Mbvh's closest-hit
+ * traversal tree is rebuilt from the new triangles (see
+ * rtbvh_gpu_traversal_tree), so that its hits stay the reference's walk's
+ * over the unchanged boxes. */
 ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const float *vertices, uintptr_t prim_count,
                                    rtbvh_stream_t stream);
 
@@ -324,10 +327,20 @@ typedef struct RTGpuView {
 ResultCode rtbvh_gpu_view(uint32_t structure_id, int is_mbvh, RTGpuView *view);
 
 /* The Mbvh's closest-hit traversal tree (no counterpart in the reference):
- * a 4-wide collapse of the source Bvh with each slot's own box, `count`
- * nodes with root 0, as exact RTMbvhNode records (`exact`) and as the
- * 64-byte compact records the kernel reads (`compact`). Device pointers,
- * valid until the Mbvh is freed or refitted. */
+ * a 4-wide collapse of the source Bvh, `count` nodes with root 0, as exact
+ * RTMbvhNode records (`exact`) and as the 64-byte compact records the
+ * kernel reads (`compact`). Built when the Mbvh has triangles. When the
+ * Bvh's boxes were built from those triangles by locally-ordered
+ * clustering (or refitted from them), each slot keeps its own box; else
+ * (binned SAH, whose left boxes can miss primitives; triangles attached or
+ * replaced later) each slot box is recomputed from the triangles and the
+ * slots whose box, as the reference's Mbvh tests it, may miss them are
+ * gated: the compact record's flag byte (bits 24-31 of word 3) has bit 1
+ * set on a node reached through a gated slot and bits 4-7 on gated leaf
+ * slots; a ray that passes a gated slot is traced again over the exact
+ * Mbvh in the reference's order. count 0: no tree (closest hit uses the
+ * exact Mbvh). Device pointers, valid until the Mbvh is freed, refitted or
+ * given new triangles. */
 ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode **exact, const void **compact, uint32_t *count);
 
 /* Bvh::refit (src/bvh.rs:176-205) on the GPU from device triangles or device

@@ -33,11 +33,12 @@ struct Entry {
   uint32_t bvh_node_count = 0;    // Mbvh: entries of d_nodes
   uint32_t build_type = 0;        // the crate's BuildType (1 LOCB, 2 binned SAH, 3 spatial; 0 unknown);
                                   // an Mbvh keeps its source Bvh's
-  bool boxes_cover = false;       // every leaf box contains its primitives (see boxes_cover())
+  bool boxes_cover = false;       // every box contains the attached triangles (see boxes_cover())
   DMNode* d_mnodes = nullptr;     // Mbvh
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
   uint32_t wcount = 0;
+  bool q_gates = false;           // Mbvh: escaped triangles are flagged (build_wide_gated)
   uint32_t* d_indices = nullptr;
   float4* d_tris = nullptr;       // 3 per index slot
   float* d_vertices = nullptr;    // prim-id order, 9 floats each
@@ -55,6 +56,7 @@ struct Entry {
     d_qnodes = nullptr;
     d_wnodes = nullptr;
     wcount = 0;
+    q_gates = false;
     d_indices = nullptr;
     d_tris = nullptr;
     d_vertices = nullptr;
@@ -91,25 +93,38 @@ const uint32_t* leaf_check(uint32_t build_type, const uint32_t* indices) {
   return (build_type == 1 || build_type == 2) ? nullptr : indices;
 }
 
-// Leaf boxes contain their primitives for LOCB builds (a leaf is its
-// primitive's box grown by 1e-4, src/builders/locb.rs) and for every tree
-// after a refit (each box recomputed from the primitives,
-// src/bvh.rs:176-205). A binned-SAH build as written sizes a left child's
-// box from bins [0, best_splits[axis].count), which after the longest-axis
-// fallback is not the split (src/builders/binned_sah.rs:236-256), so its
-// leaves need not contain their primitives and only the reference's own
-// walk reproduces its hits: it gets no traversal tree.
+// Boxes contain the triangles they were built from for LOCB builds (a leaf
+// is its primitive's box grown by 1e-4, src/builders/locb.rs) and after a
+// refit from triangles (each box recomputed from them, src/bvh.rs:176-205).
+// A binned-SAH build as written sizes a left child's box from bins
+// [0, best_splits[axis].count), which after the longest-axis fallback is
+// not the split (src/builders/binned_sah.rs:236-256), so its boxes can miss
+// primitives; boxes built from aabbs, and triangles attached or replaced
+// later, promise nothing either.
 bool boxes_cover(uint32_t build_type) { return build_type == 1; }
 
-// build_wide when the leaf boxes contain their primitives, else no tree
-// (closest hit then walks the exact nodes in the reference's order).
-ResultCode build_wide_if(bool cover, const DAabb* nodes, uint32_t node_count, const uint32_t* indices,
-                         uint32_t index_count, cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount) {
-  *wnodes = nullptr;
-  *wq = nullptr;
-  *wcount = 0;
-  if (!cover) return Ok;
-  return build_wide(nodes, node_count, indices, index_count, s, wnodes, wq, wcount);
+// The closest-hit traversal tree of Mbvh entry m, from its own BVH2 nodes
+// and triangles: the plain tree (build_wide) when the boxes contain the
+// triangles, else the tree over boxes from the triangles with escape flags
+// in m's triangle records (build_wide_gated: object-split leaves only,
+// spatial-split trees get none); no tree while m has no triangles. The
+// caller has released m's previous tree and (re)gathered the triangles.
+ResultCode build_traversal_tree(Entry& m, cudaStream_t s) {
+  m.d_wnodes = nullptr;
+  m.d_qnodes = nullptr;
+  m.wcount = 0;
+  m.q_gates = false;
+  if (!m.d_vertices || !m.d_nodes || m.vertex_lower_bound) return Ok;
+  const uint32_t* check = leaf_check(m.build_type, m.d_indices);
+  if (m.boxes_cover)
+    return build_wide(m.d_nodes, m.bvh_node_count, check, m.prim_count, s, &m.d_wnodes, &m.d_qnodes, &m.wcount);
+  if (!m.d_tris) return Ok;
+  uint32_t escaped = 0;
+  const ResultCode rc = build_wide_gated(m.d_nodes, m.bvh_node_count, m.d_indices, m.prim_count, m.d_vertices,
+                                         m.vertex_count, check != nullptr, m.d_tris, s, &m.d_wnodes, &m.d_qnodes,
+                                         &m.wcount, &escaped);
+  m.q_gates = escaped != 0;
+  return rc;
 }
 
 cudaStream_t legacy_stream() {
@@ -183,7 +198,7 @@ ResultCode store_bvh(const BuildOutput& out, uint32_t slots, size_t n, uint32_t 
   e->d_nodes = out.nodes;
   e->d_indices = out.indices;
   e->build_type = build_type;
-  e->boxes_cover = boxes_cover(build_type);
+  e->boxes_cover = boxes_cover(build_type) && d_vertices != nullptr;  // boxes from these triangles
   ResultCode rc;
   cudaError_t err;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s))) {
@@ -735,12 +750,6 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
   if (rc != Ok) return rc;
   cudaError_t err;
-  if ((rc = build_wide_if(cover, d_nodes, node_count, leaf_check(build_type, d_indices), prim_count, s,
-                          &e->d_wnodes, &e->d_qnodes, &e->wcount)) != Ok) {
-    e->release();
-    return rc;
-  }
-
   e->bvh_node_count = node_count;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
       (err = device_alloc(&e->d_indices, prim_count, s)) ||
@@ -761,6 +770,10 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
       e->release();
       return cuda_rc(err);
     }
+  }
+  if ((rc = build_traversal_tree(*e, s)) != Ok) {
+    e->release();
+    return rc;
   }
   if (!(flags & RTBVH_FLAG_NO_HOST_MIRROR)) {
     if ((rc = mirror_mbvh(*e, s)) != Ok) {
@@ -801,7 +814,16 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
   if ((err = cudaMemcpyAsync(e->d_vertices, vertices, 36 * (size_t)prim_count, cudaMemcpyDeviceToDevice, s)) ||
       (err = launch_gather_triangles(e->d_vertices, e->d_indices, e->prim_count, e->d_tris, s)))
     return cuda_rc(err);
-  return Ok;
+  // the boxes promise nothing about these triangles: an Mbvh's traversal
+  // tree is rebuilt from them (gated where the boxes miss them)
+  e->boxes_cover = false;
+  if (!is_mbvh) return Ok;
+  {
+    // the old tree may still be read by traversals on other streams
+    void* const old_arrays[] = {e->d_qnodes, e->d_wnodes};
+    pool_free_now(old_arrays, 2);
+  }
+  return build_traversal_tree(*e, s);
 }
 
 static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
@@ -817,6 +839,7 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
       a.qnodes = e->d_qnodes;
       a.qexact = e->d_wnodes;
       a.q_count = e->wcount;
+      a.q_gates = e->q_gates;
     }
     a.nodes = e->d_nodes;
     a.node_count = e->node_count;
@@ -1084,11 +1107,7 @@ static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, 
   m->d_qnodes = nullptr;
   m->d_wnodes = nullptr;
   m->wcount = 0;
-  // recollapse follows a refit: every box now comes from the primitives
-  m->boxes_cover = true;
-  if ((rc = build_wide_if(true, nodes, node_count, leaf_check(m->build_type, m->d_indices), m->prim_count, s,
-                          &m->d_wnodes, &m->d_qnodes, &m->wcount)) != Ok)
-    return rc;
+  m->q_gates = false;
   if (vertices) {
     if (!m->d_vertices && (err = device_alloc(&m->d_vertices, 9 * n, s))) return cuda_rc(err);
     if (!m->d_tris && (err = device_alloc(&m->d_tris, (size_t)kTriFloat4 * slots, s))) return cuda_rc(err);
@@ -1096,6 +1115,10 @@ static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, 
         (err = launch_gather_triangles(m->d_vertices, m->d_indices, slots, m->d_tris, s)))
       return cuda_rc(err);
   }
+  // recollapse follows a refit: from triangles, every box now contains
+  // them; from boxes, the attached triangles (if any) may lie outside
+  m->boxes_cover = vertices != nullptr;
+  if ((rc = build_traversal_tree(*m, s)) != Ok) return rc;
   if (m->mirrored && (rc = mirror_mbvh(*m, s)) != Ok) return rc;
   return Ok;
 }
@@ -1158,7 +1181,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
   }
   ResultCode rc = refit_bvh(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count, boxes, s);
   if (rc != Ok) return rc;
-  b->boxes_cover = true;
+  b->boxes_cover = vertices != nullptr;
   if (m) {
     if (m->d_nodes && (err = cudaMemcpyAsync(m->d_nodes, b->d_nodes, (size_t)b->node_count * sizeof(DAabb),
                                              cudaMemcpyDeviceToDevice, s)))
@@ -1181,7 +1204,8 @@ ResultCode rtbvh_gpu_refit_noalloc(uint32_t bvh_id, const RTAabb* aabbs, rtbvh_s
   const ResultCode rc = refit_bvh_noalloc(b->d_nodes, b->node_count, b->d_indices, b->prim_count, b->vertex_count,
                                           reinterpret_cast<const DAabb*>(aabbs), b->d_status,
                                           static_cast<cudaStream_t>(stream));
-  if (rc == Ok) b->boxes_cover = true;
+  // boxes from aabbs promise nothing about attached triangles
+  b->boxes_cover = false;
   return rc;
 }
 
@@ -1349,7 +1373,7 @@ ResultCode rtbvh_deserialize_bvh(const uint8_t* buffer, uintptr_t size, uint32_t
   e->node_count = (uint32_t)nn;
   e->prim_count = (uint32_t)ni;
   e->build_type = bt;
-  e->boxes_cover = boxes_cover(bt);
+  e->boxes_cover = false;  // triangles come later (rtbvh_gpu_set_triangles)
   ResultCode rc = upload_entry(*e, hn.data(), nn, hi.data(), ni, s);
   if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_bvh(*e, s);
   if (rc != Ok) {
@@ -1425,9 +1449,7 @@ ResultCode rtbvh_deserialize_mbvh(const uint8_t* buffer, uintptr_t size, uint32_
         (check.size() != nq || std::memcmp(check.data(), hq.data(), nq * 128) != 0))
       rc = InvalidArgument;
   }
-  if (rc == Ok)
-    rc = build_wide_if(e->boxes_cover, e->d_nodes, e->bvh_node_count, leaf_check(e->build_type, e->d_indices),
-                       e->prim_count, s, &e->d_wnodes, &e->d_qnodes, &e->wcount);
+  // no triangles yet: the traversal tree is built when they are attached
   if (rc == Ok && !(flags & RTBVH_FLAG_NO_HOST_MIRROR)) rc = mirror_mbvh(*e, s);
   if (rc != Ok) {
     e->release();

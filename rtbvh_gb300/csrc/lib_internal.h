@@ -65,8 +65,11 @@ cudaError_t launch_world_bounds(const DAabb* aabbs, size_t n, DAabb* world, uint
 cudaError_t launch_morton(const float4* centers, size_t n, const DAabb* world, uint32_t* keys, uint32_t* vals,
                           cudaStream_t s);
 // Leaf-ordered triangles, kTriFloat4 float4 (64 bytes) per index slot:
-// {v0, prim}, {v1 - v0, 0}, {v2 - v0, 0}, {0} for p = indices[k].
+// {v0, prim}, {v1 - v0, flags}, {v2 - v0, 0}, {0} for p = indices[k]. The
+// flags word is 0 when gathered; an Mbvh whose traversal tree was built by
+// build_wide_gated sets kTriEscape there.
 constexpr int kTriFloat4 = 4;
+constexpr uint32_t kTriEscape = 1u;
 cudaError_t launch_gather_triangles(const float* vertices, const uint32_t* indices, size_t n, float4* out,
                                     cudaStream_t s);
 
@@ -124,6 +127,20 @@ cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const 
 // with live_count (device) only the first *live_count of `count` nodes.
 cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,
                                  const uint32_t* live_count = nullptr);
+// The closest-hit traversal tree of a BVH2 whose boxes need not contain the
+// triangles now attached to it (a binned-SAH build, whose left boxes can
+// miss primitives, src/builders/binned_sah.rs:236-256; boxes built from
+// other primitives than the current triangles): the same 4-wide collapse as
+// build_wide over boxes recomputed from the triangles (`vertices`, 9 floats
+// per primitive; leaves index them through `indices`), grown by 1e-4 at the
+// leaves. The leaf-ordered triangle records `tris` get escape flags
+// (kTriEscape): a triangle that lies outside a box the reference's Mbvh
+// tests on the way to it. *escaped receives their number (0: the walk needs
+// no checks). check_leaves: verify that the leaves hold every index slot
+// and every primitive once (no tree otherwise).
+ResultCode build_wide_gated(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                            const float* vertices, uint32_t vertex_count, bool check_leaves, float4* tris,
+                            cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount, uint32_t* escaped);
 
 // Bvh::refit (src/bvh.rs:176-205) bounds, topology kept. Leaves index
 // `indices` (index_count slots), which index `aabbs` (prim_count boxes).
@@ -171,6 +188,9 @@ struct TraceArgs {
   const DQNode* qnodes = nullptr;
   const DMNode* qexact = nullptr;
   uint32_t q_count = 0;
+  // the triangle records carry escape flags (build_wide_gated): rays that
+  // hit an escaped triangle are traced again over mnodes
+  bool q_gates = false;
   const uint32_t* seg_qroot = nullptr;
   // Stack bound of the compact closest-hit walk: 32, 48 or 64 entries (0:
   // 64). A ray that needs more reports prim -2 and kStatusStackOverflow.

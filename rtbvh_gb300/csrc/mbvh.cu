@@ -684,6 +684,19 @@ cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* q
 // parent's box and opens strictly by depth). The tree is an internal
 // acceleration structure: its boxes contain every triangle of their
 // subtrees, so a traversal over it finds the same nearest hit.
+//
+// BVH2s whose boxes need not contain their triangles (a binned-SAH build;
+// triangles attached after the build) get the same collapse over boxes
+// recomputed from the triangles, and their escaped triangles -- those that
+// lie outside a box the reference's Mbvh tests on the way to them -- are
+// flagged (k_escapes). A ray that hits an escaped triangle (t below its
+// current nearest) leaves the walk and is traced again over the exact Mbvh.
+// For every other ray the nearest hit equals the reference's: (1) the
+// walk's nearest triangle T is not escaped, so every box the reference
+// tests on the way to T contains T, and the reference reaches T unless it
+// already holds a nearer hit; (2) a triangle T' nearer than T that the
+// reference reaches lies inside the walk's boxes, so the walk reaches and
+// hits T' too -- it would have kept T' (not escaped) or handed the ray on.
 namespace rtbvh {
 
 namespace {
@@ -791,6 +804,134 @@ __device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next
   const float4* src = reinterpret_cast<const float4*>(&m);
 #pragma unroll
   for (int j = 0; j < 8; ++j) dst[j] = src[j];
+}
+
+// ---- traversal trees over boxes recomputed from the triangles
+__device__ __forceinline__ bool box_contains(const DAabb& outer, const DAabb& inner) {
+  // false on NaN: such a box counts as not containing
+  return outer.min[0] <= inner.min[0] && outer.min[1] <= inner.min[1] && outer.min[2] <= inner.min[2] &&
+         outer.max[0] >= inner.max[0] && outer.max[1] >= inner.max[1] && outer.max[2] >= inner.max[2];
+}
+
+__device__ __forceinline__ bool wide_leaf(const DAabb& b) { return b.count >= 0 || b.left_first < 0; }
+
+__device__ __forceinline__ DAabb triangle_box(const float* __restrict__ v) {
+  DAabb b;
+  for (int a = 0; a < 3; ++a) { b.min[a] = 1e34f; b.max[a] = -1e34f; }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float x = __ldg(v + 3 * j + a);
+      b.min[a] = rs_min(b.min[a], x);
+      b.max[a] = rs_max(b.max[a], x);
+    }
+  return b;
+}
+
+// Traversal boxes recomputed from the triangles: a leaf's box is the union of its
+// triangles' vertex boxes grown by 1e-4 (what Bvh::refit gives a leaf,
+// src/bvh.rs:176-205, from those triangles); an interior node's the union
+// of its children's (no further growth: the union of boxes grown by 1e-4
+// equals the union grown by 1e-4). Bottom-up as in k_refit.
+__global__ void __launch_bounds__(kBlock)
+    k_traversal_boxes(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices,
+                      uint32_t index_count, const float* __restrict__ vertices, uint32_t vertex_count,
+                      const uint32_t* __restrict__ parent, uint32_t* __restrict__ arrive, DAabb* __restrict__ tb,
+                      uint32_t* __restrict__ status) {
+  const uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  const DAabb nd = load_aabb(nodes + c);
+  if (!wide_leaf(nd)) return;  // interior: finished by a child walk
+  DAabb box = nd;
+  for (int a = 0; a < 3; ++a) { box.min[a] = 1e34f; box.max[a] = -1e34f; }
+  if (nd.left_first >= 0) {
+    for (int32_t i = 0; i < nd.count; ++i) {
+      const uint32_t slot = (uint32_t)nd.left_first + (uint32_t)i;
+      if (slot >= index_count) { atomicOr(status, kStatusBadIndex); break; }
+      const uint32_t p = __ldg(indices + slot);
+      if (p >= vertex_count) { atomicOr(status, kStatusBadIndex); break; }
+      const DAabb t = triangle_box(vertices + 9 * (size_t)p);
+      for (int a = 0; a < 3; ++a) { box.min[a] = rs_min(box.min[a], t.min[a]); box.max[a] = rs_max(box.max[a], t.max[a]); }
+    }
+    for (int a = 0; a < 3; ++a) { box.min[a] = box.min[a] - 0.0001f; box.max[a] = box.max[a] + 0.0001f; }
+  }
+  store_aabb(tb + c, box);
+  if (nd.left_first < 0) return;
+  __threadfence();
+  uint32_t x = c;
+  for (uint32_t steps = 0; steps < node_count; ++steps) {
+    const uint32_t p = __ldcg(parent + x);
+    if (p == kNone) break;
+    if (atomicAdd(arrive + p, 1u) == 0u) break;
+    __threadfence();
+    DAabb pn = load_aabb(nodes + p);
+    const uint32_t lf = (uint32_t)pn.left_first;
+    const DAabb l = load_aabb_cg(tb + lf), r = load_aabb_cg(tb + lf + 1);
+    for (int a = 0; a < 3; ++a) {
+      pn.min[a] = rs_min(l.min[a], r.min[a]);
+      pn.max[a] = rs_max(l.max[a], r.max[a]);
+    }
+    store_aabb(tb + p, pn);
+    __threadfence();
+    x = p;
+  }
+}
+
+// Escape flags: the reference's Mbvh reaches a leaf's triangles through
+// slot boxes of the BVH2 nodes at even depth on the way down (depth >= 2;
+// MbvhNode::merge_nodes, src/mbvh_node.rs:297-411, makes quad nodes of the
+// even-depth nodes, whose slots carry their grandchildren's boxes, a leaf
+// among them its own box, and give a leaf child at odd depth its parent's
+// box). A triangle whose box grown by 1e-4 does not lie inside all of
+// those boxes (the root's box taken in too) is escaped: the reference can
+// miss its hits. One thread per leaf walks to the root with the
+// intersections of the boxes at even and at odd distance from the leaf,
+// takes the one of even depth, and sets the flag word (second float4's w)
+// of each of the leaf's triangle records: 1 escaped, 0 not.
+__global__ void __launch_bounds__(kBlock)
+    k_escapes(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices,
+              uint32_t index_count, const float* __restrict__ vertices, uint32_t vertex_count,
+              const uint32_t* __restrict__ parent, float4* __restrict__ tris, uint32_t* __restrict__ escaped,
+              uint32_t* __restrict__ status) {
+  const uint32_t c = blockIdx.x * kBlock + threadIdx.x;
+  if (c >= node_count) return;
+  const DAabb leaf = load_aabb(nodes + c);
+  if (leaf.count <= 0 || leaf.left_first < 0) return;
+  DAabb acc[2];  // [0]: boxes at even distance from the leaf (the leaf itself), [1]: odd
+  acc[0] = leaf;
+  for (int a = 0; a < 3; ++a) { acc[1].min[a] = -3.0e38f; acc[1].max[a] = 3.0e38f; }
+  // a NaN bound on the way (which fmaxf/fminf would drop) flags the leaf
+  bool nan = false;
+  for (int a = 0; a < 3; ++a) nan = nan || !(leaf.min[a] == leaf.min[a]) || !(leaf.max[a] == leaf.max[a]);
+  uint32_t x = c, dist = 0;
+  for (uint32_t steps = 0; steps < node_count; ++steps) {
+    const uint32_t p = __ldg(parent + x);
+    if (p == kNone) break;
+    ++dist;
+    const DAabb b = load_aabb(nodes + p);
+    DAabb& t = acc[dist & 1u];
+    for (int a = 0; a < 3; ++a) {
+      nan = nan || !(b.min[a] == b.min[a]) || !(b.max[a] == b.max[a]);
+      t.min[a] = fmaxf(t.min[a], b.min[a]);
+      t.max[a] = fminf(t.max[a], b.max[a]);
+    }
+    x = p;
+  }
+  const DAabb& tested = acc[dist & 1u];  // the leaf's depth is dist: even depths lie at distance == dist (mod 2)
+  uint32_t n_esc = 0;
+  for (int32_t i = 0; i < leaf.count; ++i) {
+    const uint32_t slot = (uint32_t)leaf.left_first + (uint32_t)i;
+    if (slot >= index_count) { atomicOr(status, kStatusBadIndex); break; }
+    const uint32_t p = __ldg(indices + slot);
+    if (p >= vertex_count) { atomicOr(status, kStatusBadIndex); break; }
+    DAabb t = triangle_box(vertices + 9 * (size_t)p);
+    for (int a = 0; a < 3; ++a) { t.min[a] = t.min[a] - 0.0001f; t.max[a] = t.max[a] + 0.0001f; }
+    const bool esc = nan || !box_contains(tested, t);
+    reinterpret_cast<float*>(tris + (size_t)kTriFloat4 * slot + 1)[3] = __uint_as_float(esc ? kTriEscape : 0u);
+    n_esc += esc ? 1u : 0u;
+  }
+  if (n_esc) atomicAdd(escaped, n_esc);
 }
 
 __global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
@@ -948,20 +1089,32 @@ cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const 
   return launch_quantize_mbvh(wnodes, total_prims, wq, s);
 }
 
-ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                      cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount) {
+namespace {
+
+// build_wide (vertices == nullptr: the BVH2's own boxes, no tree unless they
+// nest) and build_wide_gated (boxes from the triangles, escape flags in
+// `tris`).
+ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                     const uint32_t* box_indices, const float* vertices, uint32_t vertex_count, float4* tris,
+                     cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount, uint32_t* escaped_out) {
   *wnodes_out = nullptr;
   *wq_out = nullptr;
   *wcount = 0;
+  if (escaped_out) *escaped_out = 0;
   if (node_count == 0) return Ok;
+  const bool gated = vertices != nullptr;
   // one traversal node per BVH2 interior node at most, or the root leaf
   const uint32_t capacity = node_count < 3u ? 1u : (node_count + 1u) / 2u;
   cudaError_t e;
-  Scratch<uint32_t> status, qcount, walloc;
+  Scratch<uint32_t> status, qcount, walloc, parent, arrive;
   Scratch<uint2> q0, q1;
   Scratch<GridBarrier> bar;
+  Scratch<DAabb> tb;
   if ((e = status.alloc(4, s)) || (e = qcount.alloc(4, s)) || (e = walloc.alloc(1, s)) || (e = q0.alloc(capacity, s)) ||
       (e = q1.alloc(capacity, s)) || (e = bar.alloc(1, s)))
+    return cuda_rc(e);
+  if (gated &&
+      ((e = parent.alloc(node_count, s)) || (e = arrive.alloc(node_count, s)) || (e = tb.alloc(node_count, s))))
     return cuda_rc(e);
   DMNode* wn = nullptr;
   DQNode* wq = nullptr;
@@ -973,21 +1126,31 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
   if ((e = device_alloc(&wn, capacity, s))) return fail(cuda_rc(e));
   if ((e = cudaMemsetAsync(status.ptr, 0, 16, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
     return fail(cuda_rc(e));
-  // status[1]: not nested, or leaves that are not whole primitives once
-  // each -> no traversal tree (closest hit uses the exact nodes)
-  k_check_nested<<<(node_count + kBlock - 1) / kBlock, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
-  {
+  const unsigned node_blocks = (node_count + kBlock - 1) / kBlock;
+  // status[1]: not nested (own boxes only), or leaves that are not whole
+  // primitives once each -> no traversal tree (closest hit uses the exact
+  // nodes); status[3]: escaped triangles
+  if (!gated) k_check_nested<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
+  if (!gated || indices) {
     Scratch<uint32_t> seen;
     if (indices) {
       if ((e = seen.alloc(index_count, s)) || (e = cudaMemsetAsync(seen.ptr, 0, (size_t)index_count * 4, s)))
         return fail(cuda_rc(e));
-      k_check_leaves<<<(node_count + kBlock - 1) / kBlock, kBlock, 0, s>>>(nodes, node_count, indices, index_count,
-                                                                           seen.ptr, status.ptr + 2, status.ptr + 1);
+      k_check_leaves<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, indices, index_count, seen.ptr, status.ptr + 2,
+                                                    status.ptr + 1);
     }
     uint32_t h[2] = {0, 0};
     if ((e = cudaMemcpyAsync(h, status.ptr + 1, 8, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
       return fail(cuda_rc(e));
     if (h[0] || (indices && h[1] != index_count)) return fail(Ok);
+  }
+  if (gated) {
+    if ((e = cudaMemsetAsync(parent.ptr, 0xff, (size_t)node_count * 4, s))) return fail(cuda_rc(e));
+    k_parents<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, status.ptr);
+    k_traversal_boxes<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, box_indices, index_count, vertices,
+                                                     vertex_count, parent.ptr, arrive.ptr, tb.ptr, status.ptr);
+    k_escapes<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, box_indices, index_count, vertices, vertex_count,
+                                             parent.ptr, tris, status.ptr + 3, status.ptr);
   }
   k_wide_init<<<1, 32, 0, s>>>(q0.ptr, qcount.ptr, walloc.ptr);
   int per_sm = 0;
@@ -998,7 +1161,7 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
   if (grid > useful) grid = useful;
   if (grid < 1) grid = 1;
   WideParams p;
-  p.nodes = nodes;
+  p.nodes = gated ? tb.ptr : nodes;  // tb keeps the topology (count, left_first)
   p.node_count = node_count;
   p.wnodes = wn;
   p.capacity = capacity;
@@ -1011,9 +1174,10 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
   void* args[] = {&p};
   if ((e = cudaLaunchCooperativeKernel((void*)k_wide_collapse, dim3(grid), dim3(kBlock), args, 0, s)))
     return fail(cuda_rc(e));
-  uint32_t h[2] = {0, 0};
+  uint32_t h[3] = {0, 0, 0};
   if ((e = cudaMemcpyAsync(h, walloc.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(h + 2, status.ptr + 3, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
     return fail(cuda_rc(e));
   if (h[1] != 0) return fail((h[1] & kStatusTimeout) ? Timeout : Error);
   if (h[0] == 0 || h[0] > capacity) return fail(Error);
@@ -1022,7 +1186,24 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
   *wnodes_out = wn;
   *wq_out = wq;
   *wcount = h[0];
+  if (escaped_out) *escaped_out = h[2];
   return Ok;
+}
+
+}  // namespace
+
+ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                      cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount) {
+  return wide_impl(nodes, node_count, indices, index_count, nullptr, nullptr, 0, nullptr, s, wnodes_out, wq_out,
+                   wcount, nullptr);
+}
+
+ResultCode build_wide_gated(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                            const float* vertices, uint32_t vertex_count, bool check_leaves, float4* tris,
+                            cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount, uint32_t* escaped) {
+  if (vertices == nullptr || indices == nullptr || tris == nullptr) return Error;
+  return wide_impl(nodes, node_count, check_leaves ? indices : nullptr, index_count, indices, vertices, vertex_count,
+                   tris, s, wnodes, wq, wcount, escaped);
 }
 
 }  // namespace rtbvh

@@ -480,12 +480,13 @@ __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RaySta
 // exactly the same t.
 //
 // Rays the compact walk does not take -- a zero or non-finite component, an
-// inverse direction beyond kQuantRange, an origin beyond kCompactRange, or a
-// node flagged out of range on the way -- are appended to `deferred` and
-// traced afterwards by k_trace_mbvh over the exact Mbvh.
+// inverse direction beyond kQuantRange, an origin beyond kCompactRange, a
+// node flagged out of range on the way or (GATES) a hit on a triangle
+// flagged kTriEscape, see build_wide_gated -- are appended to `deferred`
+// and traced afterwards by k_trace_mbvh over the exact Mbvh.
 // Nine resident blocks per SM (56 registers, 36 warps; a few bytes of
 // spills): measured 4 % faster than the 64-register, 32-warp form.
-template <int STACK>
+template <int STACK, bool GATES>
 __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsigned int* work, uint32_t* deferred,
                                                            unsigned int* deferred_count) {
   RayState ray;
@@ -600,7 +601,13 @@ __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsign
         atomicOr(a.status, kStatusBadIndex);
         active = false;
       } else {
-        for (int32_t j = 0; j < count; ++j) mt_test(a.tris + kTriFloat4 * (size_t)(lf + j), ray, hu, hv, prim);
+        for (int32_t j = 0; j < count; ++j) {
+          const float4* tri = a.tris + kTriFloat4 * (size_t)(lf + j);
+          if (mt_test(tri, ray, hu, hv, prim) && GATES && (__float_as_uint(__ldg(&tri[1].w)) & kTriEscape)) {
+            defer();  // an escaped triangle is hit: its hits are the exact walk's
+            break;
+          }
+        }
       }
     }
     if (active && pend == 0 && next < 0 && sp < 0) finish();
@@ -954,13 +961,21 @@ cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
 // over the exact Mbvh. counters: [0] compact ray counter, [1] deferred rays,
 // [2] exact ray counter (zeroed).
 cudaError_t launch_compact(const TraceArgs& a, cudaStream_t s, unsigned int* counters, uint32_t* deferred) {
-  auto kern = a.stack_limit == 32 ? k_trace_compact<32> : (a.stack_limit == 48 ? k_trace_compact<48> : k_trace_compact<64>);
+  auto kern = a.q_gates ? (a.stack_limit == 32   ? k_trace_compact<32, true>
+                           : a.stack_limit == 48 ? k_trace_compact<48, true>
+                                                 : k_trace_compact<64, true>)
+                        : (a.stack_limit == 32   ? k_trace_compact<32, false>
+                           : a.stack_limit == 48 ? k_trace_compact<48, false>
+                                                 : k_trace_compact<64, false>);
   kern<<<persistent_grid(kern, a), kBlock, 0, s>>>(a, counters, deferred, counters + 1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   TraceArgs b = a;
   b.order = deferred;
   b.ray_count_dev = counters + 1;
+  // few rays, long walks: one ray per lane per refill, so that they spread
+  // over all warps instead of queueing in a few
+  b.ray_batch = 32;
   return launch3<true, false, false>(b, s, counters + 2);
 }
 
