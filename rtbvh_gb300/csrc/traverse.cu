@@ -258,8 +258,14 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   uint32_t r = 0;
   bool active = false, fast = true;
   WarpPool pool;
-  const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
+  uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
   const uint32_t ray_count = a.ray_count_dev ? *a.ray_count_dev : (uint32_t)a.ray_count;
+  if (a.ray_count_dev) {
+    // few rays (deferred by the compact walk): spread them over all warps,
+    // down to one ray per refill, so that their walks run side by side
+    const uint32_t warps = gridDim.x * (kBlock / 32u), even = ray_count / warps;
+    batch = even < 1u ? 1u : (even < batch ? even : batch);
+  }
   auto start_ray = [&](uint32_t rr) {
     r = a.order ? __ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
@@ -973,8 +979,8 @@ cudaError_t launch_compact(const TraceArgs& a, cudaStream_t s, unsigned int* cou
   TraceArgs b = a;
   b.order = deferred;
   b.ray_count_dev = counters + 1;
-  // few rays, long walks: one ray per lane per refill, so that they spread
-  // over all warps instead of queueing in a few
+  // at most 32 rays per refill (the kernel takes fewer when few rays were
+  // deferred)
   b.ray_batch = 32;
   return launch3<true, false, false>(b, s, counters + 2);
 }
