@@ -38,7 +38,7 @@ struct Entry {
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
   uint32_t wcount = 0;
-  bool q_gates = false;           // Mbvh: escaped triangles are flagged (build_wide_gated)
+  bool q_gates = false;           // Mbvh: escaped triangles are flagged (collapse_entry)
   uint32_t* d_indices = nullptr;
   float4* d_tris = nullptr;       // 3 per index slot
   float* d_vertices = nullptr;    // prim-id order, 9 floats each
@@ -103,27 +103,47 @@ const uint32_t* leaf_check(uint32_t build_type, const uint32_t* indices) {
 // later, promise nothing either.
 bool boxes_cover(uint32_t build_type) { return build_type == 1; }
 
-// The closest-hit traversal tree of Mbvh entry m, from its own BVH2 nodes
-// and triangles: the plain tree (build_wide) when the boxes contain the
-// triangles, else the tree over boxes from the triangles with escape flags
-// in m's triangle records (build_wide_gated: object-split leaves only,
-// spatial-split trees get none); no tree while m has no triangles. The
-// caller has released m's previous tree and (re)gathered the triangles.
-ResultCode build_traversal_tree(Entry& m, cudaStream_t s) {
+// The quad nodes (*mnodes, *mcount: Mbvh::construct) and the closest-hit
+// traversal tree of Mbvh entry m, from its own BVH2 nodes and triangles:
+// the plain traversal tree (build_wide over m's boxes) when the boxes
+// contain the triangles, else the tree over boxes recomputed from the
+// triangles with escape flags in m's triangle records (build_mbvh with
+// MbvhTriangles; object-split leaves only, spatial-split trees get none);
+// no traversal tree while m has no triangles. The caller has released m's
+// previous traversal tree and (re)gathered the triangles.
+ResultCode collapse_entry(Entry& m, cudaStream_t s, DMNode** mnodes, uint32_t* mcount) {
   m.d_wnodes = nullptr;
   m.d_qnodes = nullptr;
   m.wcount = 0;
   m.q_gates = false;
-  if (!m.d_vertices || !m.d_nodes || m.vertex_lower_bound) return Ok;
+  if (m.bvh_node_count == 0) {  // Mbvh::default()
+    *mnodes = nullptr;
+    *mcount = 0;
+    return Ok;
+  }
+  if (!m.d_nodes) return Error;
+  const bool tris = m.d_vertices && m.d_tris && !m.vertex_lower_bound;
   const uint32_t* check = leaf_check(m.build_type, m.d_indices);
-  if (m.boxes_cover)
+  ResultCode rc;
+  if (!tris || m.boxes_cover || m.build_type == 3) {
+    if ((rc = build_mbvh(m.d_nodes, m.bvh_node_count, s, mnodes, mcount)) != Ok || !tris) return rc;
     return build_wide(m.d_nodes, m.bvh_node_count, check, m.prim_count, s, &m.d_wnodes, &m.d_qnodes, &m.wcount);
-  if (!m.d_tris) return Ok;
+  }
+  Scratch<DAabb> tb;
+  cudaError_t err;
+  if ((err = tb.alloc(m.bvh_node_count, s))) return cuda_rc(err);
+  MbvhTriangles t;
+  t.indices = m.d_indices;
+  t.index_count = m.prim_count;
+  t.vertices = m.d_vertices;
+  t.vertex_count = m.vertex_count;
+  t.tris = m.d_tris;
+  t.tb = tb.ptr;
   uint32_t escaped = 0;
-  const ResultCode rc = build_wide_gated(m.d_nodes, m.bvh_node_count, m.d_indices, m.prim_count, m.d_vertices,
-                                         m.vertex_count, check != nullptr, m.d_tris, s, &m.d_wnodes, &m.d_qnodes,
-                                         &m.wcount, &escaped);
-  m.q_gates = escaped != 0;
+  if ((rc = build_mbvh(m.d_nodes, m.bvh_node_count, s, mnodes, mcount, &t, &escaped)) != Ok) return rc;
+  // boxes recomputed from the triangles nest by construction
+  rc = build_wide(tb.ptr, m.bvh_node_count, check, m.prim_count, s, &m.d_wnodes, &m.d_qnodes, &m.wcount, true);
+  m.q_gates = escaped != 0 && m.wcount != 0;
   return rc;
 }
 
@@ -747,8 +767,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
   e->build_type = build_type;
   e->boxes_cover = cover;
   e->source_bvh = bvh.id;
-  ResultCode rc = build_mbvh(d_nodes, node_count, s, &e->d_mnodes, &e->node_count);
-  if (rc != Ok) return rc;
+  ResultCode rc;
   cudaError_t err;
   e->bvh_node_count = node_count;
   if ((err = device_alloc(&e->d_status, 4, s)) || (err = cudaMemsetAsync(e->d_status, 0, 16, s)) ||
@@ -771,7 +790,7 @@ ResultCode rtbvh_gpu_create_mbvh(RTBvh bvh, uint32_t flags, rtbvh_stream_t strea
       return cuda_rc(err);
     }
   }
-  if ((rc = build_traversal_tree(*e, s)) != Ok) {
+  if ((rc = collapse_entry(*e, s, &e->d_mnodes, &e->node_count)) != Ok) {
     e->release();
     return rc;
   }
@@ -823,7 +842,13 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
     void* const old_arrays[] = {e->d_qnodes, e->d_wnodes};
     pool_free_now(old_arrays, 2);
   }
-  return build_traversal_tree(*e, s);
+  // the quad nodes come out as they are (same BVH2 nodes); only the
+  // traversal tree and the escape flags are kept
+  DMNode* same = nullptr;
+  uint32_t count = 0;
+  const ResultCode rc = collapse_entry(*e, s, &same, &count);
+  pool_free(same, s);
+  return rc;
 }
 
 static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
@@ -1086,24 +1111,17 @@ ResultCode rtbvh_gpu_traversal_tree(RTMbvh mbvh, const RTMbvhNode** exact, const
 // Re-collapses Mbvh entry m from BVH2 nodes after a refit: fresh quad nodes
 // (same count and topology), a fresh traversal tree, triangles re-laid from
 // `vertices` when given, and the host mirror refreshed.
-static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, const float* vertices,
-                             cudaStream_t s) {
+static ResultCode recollapse(Entry* m, const float* vertices, cudaStream_t s) {
   const size_t n = m->vertex_count, slots = m->prim_count;
-  DMNode* fresh = nullptr;
-  uint32_t count = 0;
   ResultCode rc;
   cudaError_t err;
-  if ((rc = build_mbvh(nodes, node_count, s, &fresh, &count)) != Ok) return rc;
-  if (count != m->node_count) {
-    pool_free(fresh, s);
-    return Error;
-  }
   {
     // the old arrays may still be read by traversals on other streams
     void* const old_arrays[] = {m->d_mnodes, m->d_qnodes, m->d_wnodes};
     pool_free_now(old_arrays, 3);
   }
-  m->d_mnodes = fresh;
+  const uint32_t expected = m->node_count;
+  m->d_mnodes = nullptr;
   m->d_qnodes = nullptr;
   m->d_wnodes = nullptr;
   m->wcount = 0;
@@ -1118,7 +1136,15 @@ static ResultCode recollapse(Entry* m, const DAabb* nodes, uint32_t node_count, 
   // recollapse follows a refit: from triangles, every box now contains
   // them; from boxes, the attached triangles (if any) may lie outside
   m->boxes_cover = vertices != nullptr;
-  if ((rc = build_traversal_tree(*m, s)) != Ok) return rc;
+  DMNode* fresh = nullptr;
+  uint32_t count = 0;
+  if ((rc = collapse_entry(*m, s, &fresh, &count)) != Ok) {
+    pool_free(fresh, s);
+    return rc;
+  }
+  m->d_mnodes = fresh;
+  m->node_count = count;
+  if (count != expected) return Error;  // same topology, same quad count
   if (m->mirrored && (rc = mirror_mbvh(*m, s)) != Ok) return rc;
   return Ok;
 }
@@ -1149,7 +1175,7 @@ ResultCode rtbvh_gpu_refit_mbvh(uint32_t mbvh_id, const float* vertices, const R
   if ((err = refit_boxes(vertices, aabbs, m->vertex_count, d_a, d_c4, &boxes, s))) return cuda_rc(err);
   ResultCode rc = refit_bvh(m->d_nodes, m->bvh_node_count, m->d_indices, m->prim_count, m->vertex_count, boxes, s);
   if (rc != Ok) return rc;
-  return recollapse(m, m->d_nodes, m->bvh_node_count, vertices, s);
+  return recollapse(m, vertices, s);
 }
 
 ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb* aabbs, uint32_t mbvh_id,
@@ -1186,7 +1212,7 @@ ResultCode rtbvh_gpu_refit(uint32_t bvh_id, const float* vertices, const RTAabb*
     if (m->d_nodes && (err = cudaMemcpyAsync(m->d_nodes, b->d_nodes, (size_t)b->node_count * sizeof(DAabb),
                                              cudaMemcpyDeviceToDevice, s)))
       return cuda_rc(err);
-    if ((rc = recollapse(m, b->d_nodes, b->node_count, vertices, s)) != Ok) return rc;
+    if ((rc = recollapse(m, vertices, s)) != Ok) return rc;
   }
   if (b->mirrored && (rc = mirror_bvh(*b, s)) != Ok) return rc;
   return Ok;

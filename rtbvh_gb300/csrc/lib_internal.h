@@ -67,7 +67,7 @@ cudaError_t launch_morton(const float4* centers, size_t n, const DAabb* world, u
 // Leaf-ordered triangles, kTriFloat4 float4 (64 bytes) per index slot:
 // {v0, prim}, {v1 - v0, flags}, {v2 - v0, 0}, {0} for p = indices[k]. The
 // flags word is 0 when gathered; an Mbvh whose traversal tree was built by
-// build_wide_gated sets kTriEscape there.
+// build_mbvh (with triangles) sets kTriEscape there.
 constexpr int kTriFloat4 = 4;
 constexpr uint32_t kTriEscape = 1u;
 cudaError_t launch_gather_triangles(const float* vertices, const uint32_t* indices, size_t n, float4* out,
@@ -105,18 +105,40 @@ ResultCode build_spatial_sah(const DAabb* aabbs, const float4* centers, const fl
                              size_t prims_per_leaf, uint32_t fixes, cudaStream_t s, BuildOutput* out,
                              uint32_t* index_count);
 
-// Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here.
+// Triangles for build_mbvh's escape flags (see build_mbvh): leaves index
+// `indices` (index_count slots), which index `vertices` (vertex_count
+// triangles, 9 floats each); `tris` are the leaf-ordered triangle records
+// (kTriFloat4 float4 per index slot) whose flags word gets kTriEscape or 0;
+// `tb` (node_count entries) receives the traversal boxes.
+struct MbvhTriangles {
+  const uint32_t* indices = nullptr;
+  uint32_t index_count = 0;
+  const float* vertices = nullptr;
+  uint32_t vertex_count = 0;
+  float4* tris = nullptr;
+  DAabb* tb = nullptr;
+};
+// Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here. With
+// `tri` (for BVH2s whose boxes need not contain these triangles: binned-SAH
+// builds, whose left boxes can miss primitives, src/builders/
+// binned_sah.rs:236-256; triangles attached after a build) the same passes
+// also compute every node's box from the triangles into tri->tb (leaf:
+// vertex boxes grown by 1e-4; interior: union of the children) and flag the
+// escaped triangles: those whose grown vertex box does not lie inside every
+// slot box the quad nodes test on the way to them. *escaped receives their
+// number.
 ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes,
-                      uint32_t* mnode_count);
+                      uint32_t* mnode_count, const MbvhTriangles* tri = nullptr, uint32_t* escaped = nullptr);
 // The closest-hit traversal tree: a 4-wide collapse of the BVH2 with tight
 // slot boxes (largest-area child opened first), as exact nodes and compact
 // copies; *wcount nodes, root 0. No tree (*wcount 0, Ok) when a node's box
-// does not contain its children's, or (indices given) when the leaves do not
-// hold each of the index_count slots and each primitive exactly once --
-// spatial-split trees, whose leaf boxes bound fragments -- closest hit then
-// reads the exact nodes in the reference's order.
+// does not contain its children's (checked unless `nested` is known), or
+// (indices given) when the leaves do not hold each of the index_count slots
+// and each primitive exactly once -- spatial-split trees, whose leaf boxes
+// bound fragments -- closest hit then reads the exact nodes in the
+// reference's order.
 ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                      cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount);
+                      cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount, bool nested = false);
 // Traversal trees of a concatenated forest (LOCB meshes): mesh m's tree in
 // nodes [off_m, off_m + n_m) of wnodes (exact) and wq (compact), root off_m;
 // q0/q1 hold total_prims entries each.
@@ -127,20 +149,7 @@ cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const 
 // with live_count (device) only the first *live_count of `count` nodes.
 cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* qnodes, cudaStream_t s,
                                  const uint32_t* live_count = nullptr);
-// The closest-hit traversal tree of a BVH2 whose boxes need not contain the
-// triangles now attached to it (a binned-SAH build, whose left boxes can
-// miss primitives, src/builders/binned_sah.rs:236-256; boxes built from
-// other primitives than the current triangles): the same 4-wide collapse as
-// build_wide over boxes recomputed from the triangles (`vertices`, 9 floats
-// per primitive; leaves index them through `indices`), grown by 1e-4 at the
-// leaves. The leaf-ordered triangle records `tris` get escape flags
-// (kTriEscape): a triangle that lies outside a box the reference's Mbvh
-// tests on the way to it. *escaped receives their number (0: the walk needs
-// no checks). check_leaves: verify that the leaves hold every index slot
-// and every primitive once (no tree otherwise).
-ResultCode build_wide_gated(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                            const float* vertices, uint32_t vertex_count, bool check_leaves, float4* tris,
-                            cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount, uint32_t* escaped);
+
 
 // Bvh::refit (src/bvh.rs:176-205) bounds, topology kept. Leaves index
 // `indices` (index_count slots), which index `aabbs` (prim_count boxes).
@@ -188,8 +197,8 @@ struct TraceArgs {
   const DQNode* qnodes = nullptr;
   const DMNode* qexact = nullptr;
   uint32_t q_count = 0;
-  // the triangle records carry escape flags (build_wide_gated): rays that
-  // hit an escaped triangle are traced again over mnodes
+  // the triangle records carry escape flags (build_mbvh with triangles):
+  // rays that hit an escaped triangle are traced again over mnodes
   bool q_gates = false;
   const uint32_t* seg_qroot = nullptr;
   // Stack bound of the compact closest-hit walk: 32, 48 or 64 entries (0:

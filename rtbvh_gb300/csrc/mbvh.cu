@@ -26,6 +26,32 @@ namespace {
 constexpr int kBlock = 256;
 constexpr uint32_t kNone = 0xffffffffu;
 
+__device__ __forceinline__ bool box_contains(const DAabb& outer, const DAabb& inner) {
+  // false on NaN: such a box counts as not containing
+  return outer.min[0] <= inner.min[0] && outer.min[1] <= inner.min[1] && outer.min[2] <= inner.min[2] &&
+         outer.max[0] >= inner.max[0] && outer.max[1] >= inner.max[1] && outer.max[2] >= inner.max[2];
+}
+
+// Vertex box of triangle p (9 floats), grown by 1e-4: what Bvh::refit
+// (src/bvh.rs:176-205) gives a leaf of that one triangle.
+__device__ __forceinline__ DAabb grown_triangle_box(const float* __restrict__ vertices, uint32_t p) {
+  const float* v = vertices + 9 * (size_t)p;
+  DAabb b;
+  for (int a = 0; a < 3; ++a) { b.min[a] = 1e34f; b.max[a] = -1e34f; }
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float x = __ldg(v + 3 * j + a);
+      b.min[a] = rs_min(b.min[a], x);
+      b.max[a] = rs_max(b.max[a], x);
+    }
+  for (int a = 0; a < 3; ++a) { b.min[a] = b.min[a] - 0.0001f; b.max[a] = b.max[a] + 0.0001f; }
+  b.count = 0;
+  b.left_first = 0;
+  return b;
+}
+
 __global__ void __launch_bounds__(kBlock)
     k_parents(const DAabb* __restrict__ nodes, uint32_t node_count, uint32_t* __restrict__ parent,
               uint32_t* __restrict__ arrive, uint32_t* __restrict__ status) {
@@ -44,15 +70,40 @@ __global__ void __launch_bounds__(kBlock)
   }
 }
 
+// With TRIS, the same walk also computes every node's traversal box `tb`
+// from the triangles: a leaf's is the union of its triangles' vertex boxes
+// grown by 1e-4, an interior node's the union of its children's (the union
+// of boxes grown by 1e-4 is the union grown by 1e-4); count/left_first are
+// copied from `nodes`.
+template <bool TRIS>
 __global__ void __launch_bounds__(kBlock)
     k_counts_bottom_up(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ parent,
-                       uint32_t* __restrict__ arrive, uint32_t* __restrict__ cnt_e, uint32_t* __restrict__ cnt_o) {
+                       uint32_t* __restrict__ arrive, uint32_t* __restrict__ cnt_e, uint32_t* __restrict__ cnt_o,
+                       MbvhTriangles tri, uint32_t* __restrict__ status) {
   uint32_t c = blockIdx.x * kBlock + threadIdx.x;
   if (c >= node_count) return;
   DAabb nd = load_aabb(nodes + c);
   if (nd.count < 0) return;  // walks start at leaves
   cnt_e[c] = 0;
   cnt_o[c] = 0;
+  if (TRIS) {
+    DAabb box = nd;
+    for (int a = 0; a < 3; ++a) { box.min[a] = 1e34f; box.max[a] = -1e34f; }
+    if (nd.left_first >= 0) {
+      for (int a = 0; a < 3; ++a) { box.min[a] = 1e34f - 0.0001f; box.max[a] = -1e34f + 0.0001f; }
+      for (int32_t i = 0; i < nd.count; ++i) {
+        const uint32_t slot = (uint32_t)nd.left_first + (uint32_t)i;
+        const uint32_t p = slot < tri.index_count ? __ldg(tri.indices + slot) : kNone;
+        if (p >= tri.vertex_count) {
+          atomicOr(status, kStatusBadIndex);
+          break;
+        }
+        const DAabb t = grown_triangle_box(tri.vertices, p);
+        for (int a = 0; a < 3; ++a) { box.min[a] = rs_min(box.min[a], t.min[a]); box.max[a] = rs_max(box.max[a], t.max[a]); }
+      }
+    }
+    store_aabb(tri.tb + c, box);
+  }
   __threadfence();
   uint32_t x = c;
   for (uint32_t steps = 0; steps < node_count; ++steps) {
@@ -60,11 +111,20 @@ __global__ void __launch_bounds__(kBlock)
     if (p == kNone) break;
     if (atomicAdd(arrive + p, 1u) == 0u) break;  // first arrival: the sibling finishes p
     __threadfence();
-    uint32_t lf = (uint32_t)load_aabb(nodes + p).left_first;
+    DAabb pn = load_aabb(nodes + p);
+    uint32_t lf = (uint32_t)pn.left_first;
     uint32_t e = 1u + __ldcg(cnt_o + lf) + __ldcg(cnt_o + lf + 1);
     uint32_t o = __ldcg(cnt_e + lf) + __ldcg(cnt_e + lf + 1);
     cnt_e[p] = e;
     cnt_o[p] = o;
+    if (TRIS) {
+      const DAabb l = load_aabb_cg(tri.tb + lf), r = load_aabb_cg(tri.tb + lf + 1);
+      for (int a = 0; a < 3; ++a) {
+        pn.min[a] = rs_min(l.min[a], r.min[a]);
+        pn.max[a] = rs_max(l.max[a], r.max[a]);
+      }
+      store_aabb(tri.tb + p, pn);
+    }
     __threadfence();
     x = p;
   }
@@ -80,6 +140,11 @@ struct CollapseParams {
   uint32_t* qcount;  // 3 rotating counters
   GridBarrier* bar;
   uint32_t* status;
+  // escape flags only: triangles, per quad node the intersection of the
+  // slot boxes on the way to it, the count of escaped triangles
+  MbvhTriangles tri;
+  DAabb* ibox;
+  uint32_t* escaped;
 };
 
 __device__ __forceinline__ void set_slot_box(DMNode& m, int i, const DAabb& b) {
@@ -87,8 +152,54 @@ __device__ __forceinline__ void set_slot_box(DMNode& m, int i, const DAabb& b) {
   m.max_x[i] = b.max[0]; m.max_y[i] = b.max[1]; m.max_z[i] = b.max[2];
 }
 
+// Escape flags of quad node mi's slots (TRIS): an interior slot hands its
+// child quad the intersection of the slot boxes on the way to it; a leaf
+// slot's triangles are escaped when their vertex box grown by 1e-4 is not
+// inside that intersection -- the reference's walk tests these boxes
+// before it yields the triangle (src/iter_indices.rs:264-313), so it can
+// miss the triangle's hits. Flags go to the flags word of each leaf-ordered
+// triangle record (kTriEscape).
+__device__ void mark_escapes(const CollapseParams& p, uint32_t mi, const DMNode& m) {
+  const DAabb in = load_aabb_cg(p.ibox + mi);
+  uint32_t n_esc = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int32_t ch = m.children[i], cnt = m.counts[i];
+    if (cnt < 0 && ch < 0) continue;  // empty slot
+    const float smin[3] = {m.min_x[i], m.min_y[i], m.min_z[i]}, smax[3] = {m.max_x[i], m.max_y[i], m.max_z[i]};
+    DAabb box;
+    bool nan = false;
+    for (int a = 0; a < 3; ++a) {
+      nan = nan || !(smin[a] == smin[a]) || !(smax[a] == smax[a]);
+      box.min[a] = fmaxf(in.min[a], smin[a]);
+      box.max[a] = fminf(in.max[a], smax[a]);
+    }
+    if (nan)  // a NaN bound: nothing below counts as inside
+      for (int a = 0; a < 3; ++a) { box.min[a] = 3.0e38f; box.max[a] = -3.0e38f; }
+    box.count = 0;
+    box.left_first = 0;
+    if (cnt < 0) {
+      if ((uint32_t)ch < p.m_total) store_aabb(p.ibox + ch, box);
+      continue;
+    }
+    for (int32_t j = 0; j < cnt; ++j) {
+      const uint32_t slot = (uint32_t)ch + (uint32_t)j;
+      const uint32_t prim = slot < p.tri.index_count ? __ldg(p.tri.indices + slot) : kNone;
+      if (prim >= p.tri.vertex_count) {
+        atomicOr(p.status, kStatusBadIndex);
+        break;
+      }
+      const bool esc = !box_contains(box, grown_triangle_box(p.tri.vertices, prim));
+      reinterpret_cast<float*>(p.tri.tris + (size_t)kTriFloat4 * slot + 1)[3] = __uint_as_float(esc ? kTriEscape : 0u);
+      n_esc += esc ? 1u : 0u;
+    }
+  }
+  if (n_esc) atomicAdd(p.escaped, n_esc);
+}
+
 // merge_nodes(mi, c) without the recursion: fills quad node mi and appends
 // its interior slots (bvh node, quad index) to `next`.
+template <bool TRIS>
 __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint2* next, uint32_t* next_count) {
   const DAabb cur = load_aabb(p.nodes + c);
   DMNode m;
@@ -161,11 +272,13 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
     const float4* src = reinterpret_cast<const float4*>(&m);
 #pragma unroll
     for (int k = 0; k < 8; ++k) dst[k] = src[k];
+    if (TRIS) mark_escapes(p, mi, m);
   } else {
     atomicOr(p.status, kStatusBadIndex);
   }
 }
 
+template <bool TRIS>
 __global__ void __launch_bounds__(kBlock) k_collapse(CollapseParams p) {
   const uint32_t G = gridDim.x;
   const uint32_t tid = blockIdx.x * kBlock + threadIdx.x, nthreads = G * kBlock;
@@ -178,7 +291,7 @@ __global__ void __launch_bounds__(kBlock) k_collapse(CollapseParams p) {
     uint32_t* next_count = p.qcount + ((level + 1) % 3);
     for (uint32_t k = tid; k < size; k += nthreads) {
       uint2 item = __ldcg(q + k);
-      emit_quad(p, item.x, item.y, next, next_count);
+      emit_quad<TRIS>(p, item.x, item.y, next, next_count);
     }
     if (tid == 0) p.qcount[(level + 2) % 3] = 0;
     if (!grid_sync(p.bar, G, p.status)) return;
@@ -195,6 +308,17 @@ __global__ void k_collapse_init(const uint32_t* cnt_e, const DAabb* nodes, uint2
     DAabb r = *nodes;
     uint32_t t = r.count < 0 ? cnt_e[0] : 1u;
     *m_total_out = t;
+  }
+}
+
+// The root quad's slots are the first boxes on every way down.
+__global__ void k_ibox_init(DAabb* ibox) {
+  if (threadIdx.x == 0) {
+    DAabb b;
+    for (int a = 0; a < 3; ++a) { b.min[a] = -3.0e38f; b.max[a] = 3.0e38f; }
+    b.count = 0;
+    b.left_first = 0;
+    store_aabb(ibox, b);
   }
 }
 
@@ -282,7 +406,7 @@ __global__ void __launch_bounds__(kBlock) k_collapse_segments(SegCollapseParams 
       uint2* qout = p.queue[cur ^ 1] + base;
       for (uint32_t k = threadIdx.x; k < size; k += kBlock) {
         const uint2 item = qin[k];
-        emit_quad(p.c, item.x, item.y, qout, &s_count[cur ^ 1]);
+        emit_quad<false>(p.c, item.x, item.y, qout, &s_count[cur ^ 1]);
       }
       __syncthreads();
       if (threadIdx.x == 0) s_count[cur] = 0;
@@ -347,10 +471,13 @@ __global__ void __launch_bounds__(kBlock)
 }  // namespace
 
 ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, DMNode** mnodes_out,
-                      uint32_t* mnode_count) {
+                      uint32_t* mnode_count, const MbvhTriangles* tri, uint32_t* escaped_out) {
   *mnodes_out = nullptr;
   *mnode_count = 0;
+  if (escaped_out) *escaped_out = 0;
   if (node_count == 0) return Ok;  // Mbvh::default()
+  const bool with_tris = tri != nullptr;
+  if (with_tris && (!tri->indices || !tri->vertices || !tri->tris || !tri->tb)) return Error;
   cudaError_t e;
   Scratch<uint32_t> parent, arrive, cnt_e, cnt_o, status, mtot;
   if ((e = parent.alloc(node_count, s)) || (e = arrive.alloc(node_count, s)) || (e = cnt_e.alloc(node_count, s)) ||
@@ -359,9 +486,17 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   if ((e = cudaMemsetAsync(parent.ptr, 0xff, (size_t)node_count * 4, s)) ||
       (e = cudaMemsetAsync(status.ptr, 0, 16, s)))
     return cuda_rc(e);
+  // unreachable nodes keep an empty leaf box (never read by a collapse)
+  if (with_tris && (e = cudaMemsetAsync(tri->tb, 0, (size_t)node_count * sizeof(DAabb), s))) return cuda_rc(e);
   const unsigned blocks = (node_count + kBlock - 1) / kBlock;
   k_parents<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, status.ptr);
-  k_counts_bottom_up<<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, cnt_e.ptr, cnt_o.ptr);
+  const MbvhTriangles none;
+  if (with_tris)
+    k_counts_bottom_up<true><<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, cnt_e.ptr,
+                                                       cnt_o.ptr, *tri, status.ptr);
+  else
+    k_counts_bottom_up<false><<<blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, cnt_e.ptr,
+                                                        cnt_o.ptr, none, status.ptr);
   Scratch<uint2> q0, q1;
   Scratch<uint32_t> qcount;
   Scratch<GridBarrier> bar;
@@ -375,14 +510,20 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   if (h[1] != 0) return Error;
   const uint32_t m_total = h[0];
   if (m_total == 0 || m_total > node_count) return Error;
+  Scratch<DAabb> ibox;
+  if (with_tris) {
+    if ((e = ibox.alloc(m_total, s))) return cuda_rc(e);
+    k_ibox_init<<<1, 32, 0, s>>>(ibox.ptr);
+  }
   DMNode* mnodes = nullptr;
   if ((e = device_alloc(&mnodes, m_total, s))) return cuda_rc(e);
   if ((e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s))) {
     pool_free(mnodes, s);
     return cuda_rc(e);
   }
+  auto kern = with_tris ? k_collapse<true> : k_collapse<false>;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collapse, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
   unsigned grid = (unsigned)(sm_count() * per_sm);
   const unsigned useful = (m_total + kBlock - 1) / kBlock;
@@ -399,22 +540,26 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   p.qcount = qcount.ptr;
   p.bar = bar.ptr;
   p.status = status.ptr;
+  if (with_tris) p.tri = *tri;
+  p.ibox = ibox.ptr;
+  p.escaped = status.ptr + 2;
   void* args[] = {&p};
-  if ((e = cudaLaunchCooperativeKernel((void*)k_collapse, dim3(grid), dim3(kBlock), args, 0, s))) {
+  if ((e = cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kBlock), args, 0, s))) {
     pool_free(mnodes, s);
     return cuda_rc(e);
   }
-  uint32_t st = 0;
-  if ((e = cudaMemcpyAsync(&st, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
+  uint32_t st[3] = {0, 0, 0};
+  if ((e = cudaMemcpyAsync(st, status.ptr, 12, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
     pool_free(mnodes, s);
     return cuda_rc(e);
   }
-  if (st != 0) {
+  if (st[0] != 0) {
     pool_free(mnodes, s);
-    return (st & kStatusTimeout) ? Timeout : Error;
+    return (st[0] & kStatusTimeout) ? Timeout : Error;
   }
   *mnodes_out = mnodes;
   *mnode_count = m_total;
+  if (escaped_out) *escaped_out = st[2];
   return Ok;
 }
 
@@ -518,7 +663,8 @@ cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, co
   if ((e = cudaMemsetAsync(parent, 0xff, (size_t)node_count * 4, s))) return e;
   const unsigned nb = (node_count + kBlock - 1) / kBlock;
   k_parents<<<nb, kBlock, 0, s>>>(nodes, node_count, parent, arrive, status);
-  k_counts_bottom_up<<<nb, kBlock, 0, s>>>(nodes, node_count, parent, arrive, cnt_e, cnt_o);
+  k_counts_bottom_up<false><<<nb, kBlock, 0, s>>>(nodes, node_count, parent, arrive, cnt_e, cnt_o, MbvhTriangles(),
+                                                  status);
   k_seg_mbase<<<1, 1024, 0, s>>>(nodes, cnt_e, prim_off, mesh_count, mbase);
   SegCollapseParams p;
   p.c.nodes = nodes;
@@ -531,6 +677,8 @@ cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, co
   p.c.qcount = nullptr;
   p.c.bar = nullptr;
   p.c.status = status;
+  p.c.ibox = nullptr;
+  p.c.escaped = nullptr;
   p.prim_off = prim_off;
   p.order = order;
   p.mbase = mbase;
@@ -687,16 +835,17 @@ cudaError_t launch_quantize_mbvh(const DMNode* mnodes, uint32_t count, DQNode* q
 //
 // BVH2s whose boxes need not contain their triangles (a binned-SAH build;
 // triangles attached after the build) get the same collapse over boxes
-// recomputed from the triangles, and their escaped triangles -- those that
-// lie outside a box the reference's Mbvh tests on the way to them -- are
-// flagged (k_escapes). A ray that hits an escaped triangle (t below its
-// current nearest) leaves the walk and is traced again over the exact Mbvh.
-// For every other ray the nearest hit equals the reference's: (1) the
-// walk's nearest triangle T is not escaped, so every box the reference
-// tests on the way to T contains T, and the reference reaches T unless it
-// already holds a nearer hit; (2) a triangle T' nearer than T that the
-// reference reaches lies inside the walk's boxes, so the walk reaches and
-// hits T' too -- it would have kept T' (not escaped) or handed the ray on.
+// recomputed from the triangles (build_mbvh with MbvhTriangles computes
+// them), and their escaped triangles -- those that lie outside a box the
+// reference's Mbvh tests on the way to them -- are flagged (mark_escapes).
+// A ray that hits an escaped triangle (t below its current nearest) leaves
+// the walk and is traced again over the exact Mbvh. For every other ray the
+// nearest hit equals the reference's: (1) the walk's nearest triangle T is
+// not escaped, so every box the reference tests on the way to T contains
+// T, and the reference reaches T unless it already holds a nearer hit; (2)
+// a triangle T' nearer than T that the reference reaches lies inside the
+// walk's boxes, so the walk reaches and hits T' too -- it would have kept
+// T' (not escaped) or handed the ray on.
 namespace rtbvh {
 
 namespace {
@@ -804,134 +953,6 @@ __device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next
   const float4* src = reinterpret_cast<const float4*>(&m);
 #pragma unroll
   for (int j = 0; j < 8; ++j) dst[j] = src[j];
-}
-
-// ---- traversal trees over boxes recomputed from the triangles
-__device__ __forceinline__ bool box_contains(const DAabb& outer, const DAabb& inner) {
-  // false on NaN: such a box counts as not containing
-  return outer.min[0] <= inner.min[0] && outer.min[1] <= inner.min[1] && outer.min[2] <= inner.min[2] &&
-         outer.max[0] >= inner.max[0] && outer.max[1] >= inner.max[1] && outer.max[2] >= inner.max[2];
-}
-
-__device__ __forceinline__ bool wide_leaf(const DAabb& b) { return b.count >= 0 || b.left_first < 0; }
-
-__device__ __forceinline__ DAabb triangle_box(const float* __restrict__ v) {
-  DAabb b;
-  for (int a = 0; a < 3; ++a) { b.min[a] = 1e34f; b.max[a] = -1e34f; }
-#pragma unroll
-  for (int j = 0; j < 3; ++j)
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float x = __ldg(v + 3 * j + a);
-      b.min[a] = rs_min(b.min[a], x);
-      b.max[a] = rs_max(b.max[a], x);
-    }
-  return b;
-}
-
-// Traversal boxes recomputed from the triangles: a leaf's box is the union of its
-// triangles' vertex boxes grown by 1e-4 (what Bvh::refit gives a leaf,
-// src/bvh.rs:176-205, from those triangles); an interior node's the union
-// of its children's (no further growth: the union of boxes grown by 1e-4
-// equals the union grown by 1e-4). Bottom-up as in k_refit.
-__global__ void __launch_bounds__(kBlock)
-    k_traversal_boxes(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices,
-                      uint32_t index_count, const float* __restrict__ vertices, uint32_t vertex_count,
-                      const uint32_t* __restrict__ parent, uint32_t* __restrict__ arrive, DAabb* __restrict__ tb,
-                      uint32_t* __restrict__ status) {
-  const uint32_t c = blockIdx.x * kBlock + threadIdx.x;
-  if (c >= node_count) return;
-  const DAabb nd = load_aabb(nodes + c);
-  if (!wide_leaf(nd)) return;  // interior: finished by a child walk
-  DAabb box = nd;
-  for (int a = 0; a < 3; ++a) { box.min[a] = 1e34f; box.max[a] = -1e34f; }
-  if (nd.left_first >= 0) {
-    for (int32_t i = 0; i < nd.count; ++i) {
-      const uint32_t slot = (uint32_t)nd.left_first + (uint32_t)i;
-      if (slot >= index_count) { atomicOr(status, kStatusBadIndex); break; }
-      const uint32_t p = __ldg(indices + slot);
-      if (p >= vertex_count) { atomicOr(status, kStatusBadIndex); break; }
-      const DAabb t = triangle_box(vertices + 9 * (size_t)p);
-      for (int a = 0; a < 3; ++a) { box.min[a] = rs_min(box.min[a], t.min[a]); box.max[a] = rs_max(box.max[a], t.max[a]); }
-    }
-    for (int a = 0; a < 3; ++a) { box.min[a] = box.min[a] - 0.0001f; box.max[a] = box.max[a] + 0.0001f; }
-  }
-  store_aabb(tb + c, box);
-  if (nd.left_first < 0) return;
-  __threadfence();
-  uint32_t x = c;
-  for (uint32_t steps = 0; steps < node_count; ++steps) {
-    const uint32_t p = __ldcg(parent + x);
-    if (p == kNone) break;
-    if (atomicAdd(arrive + p, 1u) == 0u) break;
-    __threadfence();
-    DAabb pn = load_aabb(nodes + p);
-    const uint32_t lf = (uint32_t)pn.left_first;
-    const DAabb l = load_aabb_cg(tb + lf), r = load_aabb_cg(tb + lf + 1);
-    for (int a = 0; a < 3; ++a) {
-      pn.min[a] = rs_min(l.min[a], r.min[a]);
-      pn.max[a] = rs_max(l.max[a], r.max[a]);
-    }
-    store_aabb(tb + p, pn);
-    __threadfence();
-    x = p;
-  }
-}
-
-// Escape flags: the reference's Mbvh reaches a leaf's triangles through
-// slot boxes of the BVH2 nodes at even depth on the way down (depth >= 2;
-// MbvhNode::merge_nodes, src/mbvh_node.rs:297-411, makes quad nodes of the
-// even-depth nodes, whose slots carry their grandchildren's boxes, a leaf
-// among them its own box, and give a leaf child at odd depth its parent's
-// box). A triangle whose box grown by 1e-4 does not lie inside all of
-// those boxes (the root's box taken in too) is escaped: the reference can
-// miss its hits. One thread per leaf walks to the root with the
-// intersections of the boxes at even and at odd distance from the leaf,
-// takes the one of even depth, and sets the flag word (second float4's w)
-// of each of the leaf's triangle records: 1 escaped, 0 not.
-__global__ void __launch_bounds__(kBlock)
-    k_escapes(const DAabb* __restrict__ nodes, uint32_t node_count, const uint32_t* __restrict__ indices,
-              uint32_t index_count, const float* __restrict__ vertices, uint32_t vertex_count,
-              const uint32_t* __restrict__ parent, float4* __restrict__ tris, uint32_t* __restrict__ escaped,
-              uint32_t* __restrict__ status) {
-  const uint32_t c = blockIdx.x * kBlock + threadIdx.x;
-  if (c >= node_count) return;
-  const DAabb leaf = load_aabb(nodes + c);
-  if (leaf.count <= 0 || leaf.left_first < 0) return;
-  DAabb acc[2];  // [0]: boxes at even distance from the leaf (the leaf itself), [1]: odd
-  acc[0] = leaf;
-  for (int a = 0; a < 3; ++a) { acc[1].min[a] = -3.0e38f; acc[1].max[a] = 3.0e38f; }
-  // a NaN bound on the way (which fmaxf/fminf would drop) flags the leaf
-  bool nan = false;
-  for (int a = 0; a < 3; ++a) nan = nan || !(leaf.min[a] == leaf.min[a]) || !(leaf.max[a] == leaf.max[a]);
-  uint32_t x = c, dist = 0;
-  for (uint32_t steps = 0; steps < node_count; ++steps) {
-    const uint32_t p = __ldg(parent + x);
-    if (p == kNone) break;
-    ++dist;
-    const DAabb b = load_aabb(nodes + p);
-    DAabb& t = acc[dist & 1u];
-    for (int a = 0; a < 3; ++a) {
-      nan = nan || !(b.min[a] == b.min[a]) || !(b.max[a] == b.max[a]);
-      t.min[a] = fmaxf(t.min[a], b.min[a]);
-      t.max[a] = fminf(t.max[a], b.max[a]);
-    }
-    x = p;
-  }
-  const DAabb& tested = acc[dist & 1u];  // the leaf's depth is dist: even depths lie at distance == dist (mod 2)
-  uint32_t n_esc = 0;
-  for (int32_t i = 0; i < leaf.count; ++i) {
-    const uint32_t slot = (uint32_t)leaf.left_first + (uint32_t)i;
-    if (slot >= index_count) { atomicOr(status, kStatusBadIndex); break; }
-    const uint32_t p = __ldg(indices + slot);
-    if (p >= vertex_count) { atomicOr(status, kStatusBadIndex); break; }
-    DAabb t = triangle_box(vertices + 9 * (size_t)p);
-    for (int a = 0; a < 3; ++a) { t.min[a] = t.min[a] - 0.0001f; t.max[a] = t.max[a] + 0.0001f; }
-    const bool esc = nan || !box_contains(tested, t);
-    reinterpret_cast<float*>(tris + (size_t)kTriFloat4 * slot + 1)[3] = __uint_as_float(esc ? kTriEscape : 0u);
-    n_esc += esc ? 1u : 0u;
-  }
-  if (n_esc) atomicAdd(escaped, n_esc);
 }
 
 __global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
@@ -1089,32 +1110,20 @@ cudaError_t launch_wide_segments(const DAabb* nodes, uint32_t node_count, const 
   return launch_quantize_mbvh(wnodes, total_prims, wq, s);
 }
 
-namespace {
-
-// build_wide (vertices == nullptr: the BVH2's own boxes, no tree unless they
-// nest) and build_wide_gated (boxes from the triangles, escape flags in
-// `tris`).
-ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                     const uint32_t* box_indices, const float* vertices, uint32_t vertex_count, float4* tris,
-                     cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount, uint32_t* escaped_out) {
+ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
+                      cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount, bool nested) {
   *wnodes_out = nullptr;
   *wq_out = nullptr;
   *wcount = 0;
-  if (escaped_out) *escaped_out = 0;
   if (node_count == 0) return Ok;
-  const bool gated = vertices != nullptr;
   // one traversal node per BVH2 interior node at most, or the root leaf
   const uint32_t capacity = node_count < 3u ? 1u : (node_count + 1u) / 2u;
   cudaError_t e;
-  Scratch<uint32_t> status, qcount, walloc, parent, arrive;
+  Scratch<uint32_t> status, qcount, walloc;
   Scratch<uint2> q0, q1;
   Scratch<GridBarrier> bar;
-  Scratch<DAabb> tb;
   if ((e = status.alloc(4, s)) || (e = qcount.alloc(4, s)) || (e = walloc.alloc(1, s)) || (e = q0.alloc(capacity, s)) ||
       (e = q1.alloc(capacity, s)) || (e = bar.alloc(1, s)))
-    return cuda_rc(e);
-  if (gated &&
-      ((e = parent.alloc(node_count, s)) || (e = arrive.alloc(node_count, s)) || (e = tb.alloc(node_count, s))))
     return cuda_rc(e);
   DMNode* wn = nullptr;
   DQNode* wq = nullptr;
@@ -1127,11 +1136,10 @@ ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* in
   if ((e = cudaMemsetAsync(status.ptr, 0, 16, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
     return fail(cuda_rc(e));
   const unsigned node_blocks = (node_count + kBlock - 1) / kBlock;
-  // status[1]: not nested (own boxes only), or leaves that are not whole
-  // primitives once each -> no traversal tree (closest hit uses the exact
-  // nodes); status[3]: escaped triangles
-  if (!gated) k_check_nested<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
-  if (!gated || indices) {
+  // status[1]: not nested, or leaves that are not whole primitives once
+  // each -> no traversal tree (closest hit uses the exact nodes)
+  if (!nested || indices) {
+    if (!nested) k_check_nested<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
     Scratch<uint32_t> seen;
     if (indices) {
       if ((e = seen.alloc(index_count, s)) || (e = cudaMemsetAsync(seen.ptr, 0, (size_t)index_count * 4, s)))
@@ -1144,14 +1152,6 @@ ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* in
       return fail(cuda_rc(e));
     if (h[0] || (indices && h[1] != index_count)) return fail(Ok);
   }
-  if (gated) {
-    if ((e = cudaMemsetAsync(parent.ptr, 0xff, (size_t)node_count * 4, s))) return fail(cuda_rc(e));
-    k_parents<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, parent.ptr, arrive.ptr, status.ptr);
-    k_traversal_boxes<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, box_indices, index_count, vertices,
-                                                     vertex_count, parent.ptr, arrive.ptr, tb.ptr, status.ptr);
-    k_escapes<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, box_indices, index_count, vertices, vertex_count,
-                                             parent.ptr, tris, status.ptr + 3, status.ptr);
-  }
   k_wide_init<<<1, 32, 0, s>>>(q0.ptr, qcount.ptr, walloc.ptr);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wide_collapse, kBlock, 0);
@@ -1161,7 +1161,7 @@ ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* in
   if (grid > useful) grid = useful;
   if (grid < 1) grid = 1;
   WideParams p;
-  p.nodes = gated ? tb.ptr : nodes;  // tb keeps the topology (count, left_first)
+  p.nodes = nodes;
   p.node_count = node_count;
   p.wnodes = wn;
   p.capacity = capacity;
@@ -1174,10 +1174,9 @@ ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* in
   void* args[] = {&p};
   if ((e = cudaLaunchCooperativeKernel((void*)k_wide_collapse, dim3(grid), dim3(kBlock), args, 0, s)))
     return fail(cuda_rc(e));
-  uint32_t h[3] = {0, 0, 0};
+  uint32_t h[2] = {0, 0};
   if ((e = cudaMemcpyAsync(h, walloc.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaMemcpyAsync(h + 2, status.ptr + 3, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
     return fail(cuda_rc(e));
   if (h[1] != 0) return fail((h[1] & kStatusTimeout) ? Timeout : Error);
   if (h[0] == 0 || h[0] > capacity) return fail(Error);
@@ -1186,24 +1185,7 @@ ResultCode wide_impl(const DAabb* nodes, uint32_t node_count, const uint32_t* in
   *wnodes_out = wn;
   *wq_out = wq;
   *wcount = h[0];
-  if (escaped_out) *escaped_out = h[2];
   return Ok;
-}
-
-}  // namespace
-
-ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                      cudaStream_t s, DMNode** wnodes_out, DQNode** wq_out, uint32_t* wcount) {
-  return wide_impl(nodes, node_count, indices, index_count, nullptr, nullptr, 0, nullptr, s, wnodes_out, wq_out,
-                   wcount, nullptr);
-}
-
-ResultCode build_wide_gated(const DAabb* nodes, uint32_t node_count, const uint32_t* indices, uint32_t index_count,
-                            const float* vertices, uint32_t vertex_count, bool check_leaves, float4* tris,
-                            cudaStream_t s, DMNode** wnodes, DQNode** wq, uint32_t* wcount, uint32_t* escaped) {
-  if (vertices == nullptr || indices == nullptr || tris == nullptr) return Error;
-  return wide_impl(nodes, node_count, check_leaves ? indices : nullptr, index_count, indices, vertices, vertex_count,
-                   tris, s, wnodes, wq, wcount, escaped);
 }
 
 }  // namespace rtbvh

@@ -488,7 +488,7 @@ __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RaySta
 // Rays the compact walk does not take -- a zero or non-finite component, an
 // inverse direction beyond kQuantRange, an origin beyond kCompactRange, a
 // node flagged out of range on the way or (GATES) a hit on a triangle
-// flagged kTriEscape, see build_wide_gated -- are appended to `deferred`
+// flagged kTriEscape, see build_mbvh -- are appended to `deferred`
 // and traced afterwards by k_trace_mbvh over the exact Mbvh.
 // Nine resident blocks per SM (56 registers, 36 warps; a few bytes of
 // spills): measured 4 % faster than the 64-register, 32-warp form.

@@ -402,9 +402,10 @@ def _escaped(m):
 
 def _escaped_reference(nodes, idx, tris):
     """The escape flags restated: a triangle is escaped when its vertex box
-    grown by 1e-4 does not lie inside every box at even depth on the way to
-    its leaf (the slot boxes the reference's Mbvh tests,
-    src/mbvh_node.rs:297-411, with the root's box)."""
+    grown by 1e-4 does not lie inside every slot box the reference's Mbvh
+    tests on the way to its leaf (src/mbvh_node.rs:297-411: the boxes of the
+    BVH2 nodes at even depth >= 2 on the way down; a leaf at depth 1 sits in
+    a slot with the root's box)."""
     ni, nf = nodes.view(np.int32), nodes.view(np.float32)
     cnt, lf = ni[:, 3], ni[:, 7]
     big = np.float32(3e38)
@@ -413,8 +414,10 @@ def _escaped_reference(nodes, idx, tris):
     e = np.float32(1e-4)
     while stack:
         x, d, lo, hi = stack.pop()
-        if d % 2 == 0:
+        if d % 2 == 0 and d >= 2:
             lo, hi = np.maximum(lo, nf[x, 0:3]), np.minimum(hi, nf[x, 4:7])
+        if cnt[x] >= 0 and d <= 1:
+            lo, hi = np.maximum(lo, nf[0, 0:3]), np.minimum(hi, nf[0, 4:7])
         if cnt[x] >= 0:
             ids = idx[lf[x]:lf[x] + cnt[x]]
             t = tris[ids]
