@@ -37,6 +37,7 @@ sys.path.insert(0, ROOT)
 N_TRIS = 1_000_000
 N_RAYS = 16_777_216
 SCENE_SEED, RAY_SEED = 2, 3
+CLUSTER_TRIS, CLUSTER_CAMERA = 10_000_000, 4096  # clustered spheres: triangles, camera width
 METRIC = "closest-hit Mrays/s (1M-tri incoherent LOCB+MBVH, 16.7M rays)"
 B_IN, B_OUT, B_NODE, B_TRI = 24, 16, 128, 40  # algorithmic bytes: ray in, hit out, quad node, triangle (36 + index 4)
 # algorithmic build bytes per primitive: triangle in 36, box 32, Morton code 4,
@@ -60,12 +61,16 @@ def make_scene():
 
 def apply_size_overrides(args):
     """--rays/--tris shrink the workload for profiling captures only; the
-    benchmark line is always taken at the full size."""
-    global N_RAYS, N_TRIS, METRIC
+    benchmark line is always taken at the full size. With --only
+    clustered_10M_binned_sah they set the clustered scene's triangle count
+    and its camera (the square image with about --rays pixels)."""
+    global N_RAYS, N_TRIS, METRIC, CLUSTER_TRIS, CLUSTER_CAMERA
     if args.rays:
         N_RAYS = args.rays
+        CLUSTER_CAMERA = max(16, math.isqrt(args.rays))
     if args.tris:
         N_TRIS = args.tris
+        CLUSTER_TRIS = args.tris
     if args.rays or args.tris:
         METRIC = METRIC + f" [reduced: {N_TRIS} tris, {N_RAYS} rays]"
 
@@ -636,7 +641,7 @@ def workload_clustered(with_stats=True):
 
     import rtbvh_gb300 as rb
     from rtbvh_gb300 import scenes
-    tris = scenes.clustered(10_000_000)
+    tris = scenes.clustered(CLUSTER_TRIS)
     d_tris = torch.from_numpy(tris).cuda()
     del tris
     sah_ms = _cuda_time(lambda: rb.Builder(primitives=rb.Triangles(d_tris)).construct_binned_sah(host_mirror=False),
@@ -644,7 +649,7 @@ def workload_clustered(with_stats=True):
     bvh = rb.Builder(primitives=rb.Triangles(d_tris)).construct_binned_sah(host_mirror=False)
     mbvh_ms = _cuda_time(lambda: rb.Mbvh.construct(bvh, host_mirror=False), reps=3, warmup=1)
     m = rb.Mbvh.construct(bvh, host_mirror=False)
-    primary = torch.from_numpy(scenes.camera_rays(4096, 4096)).cuda()
+    primary = torch.from_numpy(scenes.camera_rays(CLUSTER_CAMERA, CLUSTER_CAMERA)).cuda()
     ph, _ = m.intersect(primary)
     primary_hits = int((ph[:, 3].contiguous().view(torch.int32) >= 0).sum())
     sec = secondary_rays(primary, ph, d_tris, per_hit=3)
