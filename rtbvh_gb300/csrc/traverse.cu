@@ -395,9 +395,18 @@ __device__ __forceinline__ void sort_slots(float (&key)[4], int32_t (&ch)[4]) {
 }
 
 // Key of slot i (interior slots only) and its bit in the leaf mask.
+//
+// A slot whose box lies wholly behind the origin (exit t below 0) is
+// skipped as well, which the reference's test does not do: every box of a
+// traversal tree contains its triangles grown by 1e-4, so a triangle hit at
+// t > 1e-4 (the triangle test's lower bound) lies inside its boxes with that
+// margin, and the box's computed exit t stays above 0 (the slab rounding is
+// below the margin, see kCompactRange). The cull removes no box that holds
+// a hit; it saves the walks of rays that start inside the scene (secondary
+// rays) through the boxes behind them.
 __device__ __forceinline__ void slot_key(float tn, float tx, float t, int32_t child, int32_t count, int i,
                                          float& key, uint32_t& leaves) {
-  const bool hit = tx >= tn && tn < t && child >= 0;
+  const bool hit = tx >= tn && tx >= 0.0f && tn < t && child >= 0;
   key = (hit && count < 0) ? tn : __int_as_float(0x7f800000);
   leaves |= (hit && count >= 0) ? 1u << i : 0u;
 }

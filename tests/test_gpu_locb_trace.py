@@ -303,6 +303,46 @@ def test_compact_nodes_same_nearest_hit(name, kind):
     assert (rb.hit_prims(hits) >= 0).sum() > 0
 
 
+@pytest.mark.parametrize("name", ["incoherent_20k", "sphere"])
+@pytest.mark.parametrize("kind", ["locb", "sah"])
+def test_compact_nodes_rays_from_inside_the_scene(name, kind):
+    """Rays that start inside the scene: the compact walk skips slot boxes
+    that lie behind the origin, which the reference's test keeps. Origins
+    uniform in the scene box with uniform directions, and secondary rays
+    leaving the primary hit points 1e-4 off the surface in random
+    directions (some back into the surface), against the exact-node walk and
+    the oracle."""
+    tris = scene(name)
+    g = gpu_build(tris, kind)
+    m = rb.Mbvh.construct(g)
+    rng = np.random.default_rng(21)
+    lo, hi = tris.reshape(-1, 3).min(0), tris.reshape(-1, 3).max(0)
+    n = 32768
+    o = rng.uniform(lo, hi, size=(n, 3))
+    d = rng.normal(size=(n, 3))
+    inside = np.concatenate([o, d / np.linalg.norm(d, axis=1, keepdims=True)], 1).astype(np.float32)
+    prim_rays, _ = rays_for(name, count=n)
+    ph = m.intersect(to_cuda(prim_rays))[0].cpu().numpy()
+    hit = rb.hit_prims(ph) >= 0
+    p = prim_rays[hit, :3].astype(np.float64) + prim_rays[hit, 3:] * ph[hit, :1]
+    tri = tris[rb.hit_prims(ph)[hit]].astype(np.float64)
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm *= -np.sign(np.einsum("ij,ij->i", nrm, prim_rays[hit, 3:]))[:, None]
+    sd = rng.normal(size=p.shape)
+    sd /= np.linalg.norm(sd, axis=1, keepdims=True)
+    second = np.concatenate([p + 1e-4 * nrm, sd], 1).astype(np.float32)
+    rays = np.concatenate([inside, second])
+    hits = m.intersect(to_cuda(rays))[0].cpu().numpy()
+    exact = m.intersect(to_cuda(rays), exact_nodes=True)[0].cpu().numpy()
+    assert m.status() == rb.ResultCode.Ok
+    assert_same_nearest(hits, exact, tris, rays)
+    on, oi = oracle_build(tris, kind)
+    oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, stats=False)
+    assert_same_nearest(hits, oh, tris, rays)
+    assert (rb.hit_prims(hits) >= 0).sum() > n // 4
+
+
 def test_compact_nodes_out_of_range_values():
     """Triangles far outside the quantisable range put their quad nodes on
     the exact path; rays with huge origins trace the exact nodes entirely.
