@@ -163,7 +163,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int nblocks
           ok = 0;
           break;
         }
-        __nanosleep(256);
+        __nanosleep(32);
       }
     }
     __threadfence();

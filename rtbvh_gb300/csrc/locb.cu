@@ -14,9 +14,11 @@
 //      unmerged nodes (next level) and children (final node array).
 // Node positions follow the reference exactly (locb.rs:178-215), so the
 // output is bit-identical to the reference's node array. Levels of at most
-// kTailNodes nodes are finished by block 0 alone with block barriers.
+// kTailNodes nodes are finished by k_locb_tail: one block of 1024 threads
+// with the whole level in shared memory and block barriers only.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "lib_internal.h"
 
@@ -35,7 +37,7 @@ struct LocbParams {
   uint32_t* blocksum;
   GridBarrier* bar;
   uint32_t* status;
-  uint32_t* info;  // [0] levels run
+  uint32_t* info;  // levels run, then begin, end and level buffer of the first tail level
   uint32_t n;
 };
 
@@ -236,11 +238,124 @@ __global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
     ++levels;
   }
 
-  // ---------------------------------------------------------------- tail (block 0)
-  if (blockIdx.x != 0) return;
-  if (!locb_block_finish(p.lvl, p.final_nodes, p.nb, begin, end, cur, levels, s_box, s_flag, s_warp, p.status))
+  // the last kTailNodes nodes: k_locb_tail
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    p.info[0] = levels;
+    p.info[1] = begin;
+    p.info[2] = end;
+    p.info[3] = (uint32_t)cur;
+  }
+}
+
+// The clustering levels of the last kTailNodes (or fewer) nodes in ONE block
+// of kTailBlock threads, the whole level held in shared memory: per level the
+// nearest neighbours, the merge flags and their prefix, and the placement of
+// parents (next level, shared memory) and children (final node array) with
+// the arithmetic of nn_tile / scatter_tile, so the nodes are the same bits.
+// The level comes from p.info (written by k_locb_levels) or, for builds with
+// no wide level, from the arguments.
+constexpr int kTailBlock = 1024;
+constexpr size_t kTailSmem = 2 * kTailNodes * sizeof(DAabb) + 2 * kTailNodes * sizeof(uint32_t);
+
+__global__ void __launch_bounds__(kTailBlock) k_locb_tail(LocbParams p, bool from_info, uint32_t begin0,
+                                                          uint32_t end0) {
+  extern __shared__ __align__(16) unsigned char tail_smem[];
+  __shared__ uint32_t s_warp[kTailBlock / 32];
+  DAabb* x = reinterpret_cast<DAabb*>(tail_smem);
+  DAabb* y = x + kTailNodes;
+  uint32_t* s_nb = reinterpret_cast<uint32_t*>(y + kTailNodes);
+  uint32_t* s_incl = s_nb + kTailNodes;
+  const uint32_t tid = threadIdx.x;
+  uint32_t levels = from_info ? __ldcg(p.info) : 0u;
+  uint32_t begin = from_info ? __ldcg(p.info + 1) : begin0;
+  uint32_t end = from_info ? __ldcg(p.info + 2) : end0;
+  const int cur = from_info ? (int)__ldcg(p.info + 3) : 0;
+  if (end <= begin || end - begin > kTailNodes || end > 2u * p.n - 1u || (cur != 0 && cur != 1)) {
+    if (tid == 0) atomicOr(p.status, kStatusBadIndex);
     return;
-  if (threadIdx.x == 0) {
+  }
+  for (uint32_t i = tid; i < end - begin; i += kTailBlock) x[i] = load_aabb_cg(p.lvl[cur] + begin + i);
+  __syncthreads();
+  while (end - begin > 1) {
+    const uint32_t m = end - begin;
+    // 1. nearest neighbour in [max(0, i - 14), min(m, i + 15)), first minimum wins
+    for (uint32_t i = tid; i < m; i += kTailBlock) {
+      const uint32_t sb = i > (uint32_t)kRadius ? i - kRadius : 0u;
+      const uint32_t se = min(i + kRadius + 1, m);
+      const SBox bi = to_sbox(x[i]);
+      float best = 3.40282347e+38f;
+      int32_t best_j = -1;
+      for (uint32_t j = sb; j < i; ++j) {
+        const float d = union_half_area(to_sbox(x[j]), bi);
+        if (d < best) { best = d; best_j = (int32_t)j; }
+      }
+      for (uint32_t j = i + 1; j < se; ++j) {
+        const float d = union_half_area(bi, to_sbox(x[j]));
+        if (d < best) { best = d; best_j = (int32_t)j; }
+      }
+      if (best_j < 0) {
+        atomicOr(p.status, kStatusNoNeighbour);
+        best_j = (int32_t)i;
+      }
+      s_nb[i] = (uint32_t)best_j;
+    }
+    __syncthreads();
+    // 2. merge flags (i < j, nb[j] == i) and their inclusive prefix, two per thread
+    const uint32_t i0 = 2u * tid, i1 = i0 + 1u;
+    const uint32_t f0 = (i0 < m && i0 < s_nb[i0] && s_nb[s_nb[i0]] == i0) ? 1u : 0u;
+    const uint32_t f1 = (i1 < m && i1 < s_nb[i1] && s_nb[s_nb[i1]] == i1) ? 1u : 0u;
+    uint32_t mc;
+    const uint32_t incl = block_inclusive_scan<kTailBlock>(f0 + f1, s_warp, &mc);
+    if (i0 < m) s_incl[i0] = incl - f1;
+    if (i1 < m) s_incl[i1] = incl;
+    if (mc == 0) {
+      if (tid == 0) atomicOr(p.status, kStatusNoMerge);
+      return;  // block-uniform
+    }
+    __syncthreads();
+    // 3. parents of merged pairs and unmerged nodes to the next level (begin - mc ...),
+    //    merged pairs' children to the final node array (locb.rs:178-215)
+    const uint32_t unmerged_begin = begin - mc, children_begin = end - 2u * mc;
+    for (uint32_t i = tid; i < m; i += kTailBlock) {
+      const uint32_t j = s_nb[i];
+      const uint32_t merged_i = s_incl[i];
+      if (s_nb[j] == i) {
+        if (i < j) {
+          const uint32_t pos = unmerged_begin + j - s_incl[j];
+          const uint32_t fc = children_begin + (merged_i - 1u) * 2u;
+          const DAabb a = x[i], b = x[j];
+          DAabb par;
+#pragma unroll
+          for (int ax = 0; ax < 3; ++ax) {
+            par.min[ax] = rs_min(b.min[ax], a.min[ax]);
+            par.max[ax] = rs_max(b.max[ax], a.max[ax]);
+          }
+          par.count = -1;
+          par.left_first = (int32_t)fc;
+          if (pos >= unmerged_begin && pos < end - 2u * mc && fc + 1 < end) {
+            y[pos - unmerged_begin] = par;
+            store_aabb(p.final_nodes + fc, a);
+            store_aabb(p.final_nodes + fc + 1, b);
+          } else {
+            atomicOr(p.status, kStatusBadIndex);
+          }
+        }
+      } else {
+        const uint32_t pos = unmerged_begin + i - merged_i;
+        if (pos >= unmerged_begin && pos < end - 2u * mc) y[pos - unmerged_begin] = x[i];
+        else atomicOr(p.status, kStatusBadIndex);
+      }
+    }
+    __syncthreads();
+    DAabb* t = x;
+    x = y;
+    y = t;
+    begin -= mc;
+    end -= 2u * mc;
+    ++levels;
+  }
+  if (tid == 0) {
+    store_aabb(p.final_nodes + begin, x[0]);
     p.info[0] = levels;
     p.info[1] = begin;
   }
@@ -483,6 +598,7 @@ ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n_, cuda
   if ((e = blocksum.alloc(grid, s)) || (e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s)))
     return fail(cuda_rc(e));
 
+  if ((e = cudaMemsetAsync(info.ptr, 0, 4 * sizeof(uint32_t), s))) return fail(cuda_rc(e));
   LocbParams p;
   p.lvl[0] = lvl0.ptr;
   p.lvl[1] = lvl1.ptr;
@@ -493,9 +609,18 @@ ResultCode build_locb(const DAabb* aabbs, const float4* centers, size_t n_, cuda
   p.status = status.ptr;
   p.info = info.ptr;
   p.n = n;
-  void* args[] = {&p};
-  if ((e = cudaLaunchCooperativeKernel((void*)k_locb_levels, dim3(grid), dim3(kBlock), args, 0, s)))
-    return fail(cuda_rc(e));
+  const bool wide = n > kTailNodes;  // levels above kTailNodes nodes in the cooperative launch
+  if (wide) {
+    void* args[] = {&p};
+    if ((e = cudaLaunchCooperativeKernel((void*)k_locb_levels, dim3(grid), dim3(kBlock), args, 0, s)))
+      return fail(cuda_rc(e));
+  }
+  static std::once_flag tail_attr;
+  std::call_once(tail_attr, [] {
+    cudaFuncSetAttribute(k_locb_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailSmem);
+  });
+  k_locb_tail<<<1, kTailBlock, kTailSmem, s>>>(p, wide, n - 1u, node_count);
+  if ((e = cudaGetLastError())) return fail(cuda_rc(e));
   uint32_t h_status = 0;
   if ((e = cudaMemcpyAsync(&h_status, status.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
       (e = cudaStreamSynchronize(s)))

@@ -340,7 +340,7 @@ def test_compact_nodes_rays_from_inside_the_scene(name, kind):
     on, oi = oracle_build(tris, kind)
     oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, stats=False)
     assert_same_nearest(hits, oh, tris, rays)
-    assert (rb.hit_prims(hits) >= 0).sum() > n // 4
+    assert (rb.hit_prims(hits) >= 0).sum() > len(rays) // 20
 
 
 def test_compact_nodes_out_of_range_values():
