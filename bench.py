@@ -204,6 +204,33 @@ def nearest_hit_parity(gpu, ref, tris, rays):
             "ties_proven": ties, "uv_mismatch_same_prim": uv_bad}
 
 
+B_QNODE, B_QTRI, B_XNODE = 64, 64, 128  # bytes the default walk reads: compact node, triangle record, exact node
+
+
+def own_walk_roofline(mbvh, d_rays, ref_stats, ms, peak, peak_kind):
+    """Roofline of the default walk over the bytes it reads itself: per ray
+    24 in + 16 out, 64 per traversal-tree node visit and 64 per triangle
+    record, counted by the walk's own statistics (RTBVH_TRACE_WALK_STATS);
+    rays it hands on to the exact walk add that walk's 128-byte node visits
+    and 64-byte triangle records (its counts are the reference iterator's)."""
+    import torch
+    _, w = mbvh.intersect(d_rays, walk_stats=True)
+    w = w.to(torch.int64)
+    n = w.shape[0]
+    handed = w[:, 2] != 0
+    wv, wt = float(w[:, 0].sum()), float(w[:, 1].sum())
+    xb = 0.0
+    if bool(handed.any()):
+        xb = float(B_XNODE * ref_stats[handed, 0].sum() + B_QTRI * ref_stats[handed, 1].sum())
+    own = n * (B_IN + B_OUT) + B_QNODE * wv + B_QTRI * wt + xb
+    ach = own / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "unit": "GB/s", "achieved": round(ach, 1), "peak": peak, "frac": round(ach / peak, 3),
+            "peak_source": peak_kind, "bytes_per_ray": round(own / n, 1), "mean_node_visits": round(wv / n, 3),
+            "mean_tri_tests": round(wt / n, 3), "rays_handed_to_exact_walk": int(handed.sum()),
+            "bytes": "24 ray + 16 hit + 64 per compact node + 64 per triangle record (+ 128 per exact node of "
+                     "handed-on rays)"}
+
+
 def replica_value(total_ms, rays_per_step, steps, world_size, dist=None, device="cpu"):
     """Replicas (no exchange between ranks): every rank traces its own copy
     of the workload. Returns (whole-job Mrays/s = all ranks' rays / the
@@ -331,6 +358,7 @@ def run_gpu(args):
 
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / (ms * 1e-3) / 1e9
+    roofline_own = own_walk_roofline(mbvh, d_rays, st, ms, peak, peak_kind)
     traffic = None
     tp = os.path.join(ROOT, "profiles", "trace_mbvh_traffic.json")
     if os.path.exists(tp):
@@ -381,9 +409,13 @@ def run_gpu(args):
                          "peak_source": peak_kind,
                          "bytes_per_ray": round(alg_bytes / N_RAYS, 1),
                          "mean_node_visits": round(visits / N_RAYS, 3),
-                         "mean_tri_tests": round(tests / N_RAYS, 3)},
+                         "mean_tri_tests": round(tests / N_RAYS, 3),
+                         "bytes": "24 ray + 16 hit + 128 per quad node + 40 per triangle, visit counts of the "
+                                  "reference's iterator over its Mbvh"},
+            "roofline_own_walk": roofline_own,
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
+            # per step: the compact walk and the exact-node pass over the rays it hands on
+            "gpu_launches": 2 * args.steps,
             "clocks": clk.summary(),
             "build_ms": {"locb": round(statistics.median(build_ms), 3), "mbvh": round(statistics.median(mbvh_ms), 3)},
             "any_hit": {"value": round(ws * N_RAYS / (any_ms * 1e-3) / 1e6, 2), "unit": "Mrays/s",
@@ -676,6 +708,7 @@ def workload_clustered(with_stats=True):
         out["roofline"] = {"bytes_per_ray": round(bpr, 1), "mean_node_visits": round(nv, 3),
                            "mean_tri_tests": round(nt, 3), "achieved_gbs": round(ach, 1),
                            "frac": round(ach / peak, 3), "peak_source": kind}
+        out["roofline_own_walk"] = own_walk_roofline(m, allr, st, ms, peak, kind)
     if m.status() != rb.ResultCode.Ok:
         raise RuntimeError("clustered traversal reported an error")
     return out

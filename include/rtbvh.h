@@ -186,6 +186,16 @@ typedef void *rtbvh_stream_t;
  * triangles are hit at exactly the same t either may be reported. This flag
  * reads the exact 128-byte nodes in the reference's visit order instead. */
 #define RTBVH_TRACE_EXACT_NODES 8u
+/* MBVH closest hit over the compact nodes (the default walk) with per-ray
+ * counts of that walk in `stats` (3 per ray): traversal-tree node visits,
+ * triangle tests, and 1 if the ray was handed on to the exact-node walk
+ * (its hit is that walk's; its counts cover the compact part only). These
+ * are this library's own work per ray, not the reference iterator's (for
+ * those use RTBVH_TRACE_STATS). Hits are those of the call without the
+ * flag. InvalidArgument with RTBVH_TRACE_STATS, _ANY_HIT, _EXACT_NODES or
+ * _REORDER, on a Bvh, or on an Mbvh without a traversal tree; Error if
+ * stats is NULL. The host-buffer entry ignores it. */
+#define RTBVH_TRACE_WALK_STATS 16u
 
 /* Builder::construct_binned_sah / construct_locally_ordered_clustered on
  * device triangles (src/bvh.rs:87-137, with aabbs = Triangle::aabb and

@@ -154,6 +154,7 @@ void free_mbvh(RTMbvh bvh);
 #define RTBVH_TRACE_STATS 2u
 #define RTBVH_TRACE_REORDER 4u
 #define RTBVH_TRACE_EXACT_NODES 8u
+#define RTBVH_TRACE_WALK_STATS 16u
 #define RTBVH_SPATIAL_FIX_CLIP 1u
 #define RTBVH_SPATIAL_FIX_EXIT_BIN 2u
 #define RTBVH_SPATIAL_FIX_SWEEP_BOX 4u

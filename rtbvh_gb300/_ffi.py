@@ -37,6 +37,7 @@ TRACE_ANY_HIT = 1
 TRACE_STATS = 2
 TRACE_REORDER = 4
 TRACE_EXACT_NODES = 8
+TRACE_WALK_STATS = 16
 
 # RTBVH_SPATIAL_FIX_*: corrections of the reference's spatial-split builder.
 SPATIAL_FIX_CLIP = 1

@@ -287,16 +287,19 @@ class Mbvh:
         return np.frombuffer(buf, dtype=np.uint32).copy()
 
     def intersect(self, rays, t_max=None, any_hit=False, stats=False, stream=None, reorder=False,
-                  exact_nodes=False):
+                  exact_nodes=False, walk_stats=False):
         """GPU MbvhIndexIterator + triangle test for a batch of rays.
         rays: (R, 6) float32 (CUDA tensor or array). Returns (hits (R,4)
         float32 CUDA tensor [t, u, v, prim bits], stats (R,3) int32 or None).
         reorder: trace in (origin, direction)-sorted order (same results).
         exact_nodes: closest hit over the exact 128-byte quad nodes in the
         reference's visit order (default: compact nodes, same nearest hit,
-        either triangle where two are hit at exactly the same t)."""
+        either triangle where two are hit at exactly the same t).
+        walk_stats: closest hit of the default walk with its own per-ray
+        counts as stats: traversal-tree node visits, triangle tests, 1 if
+        the ray was handed on to the exact walk."""
         return _trace(self._lib.rtbvh_gpu_intersect_mbvh, self._h, rays, t_max, any_hit, stats, stream, reorder,
-                      exact_nodes)
+                      exact_nodes, walk_stats)
 
     def intersect_packets(self, rays, t=None, stats=False, stream=None):
         """GPU MbvhPacketIndexIterator + packet triangle test (the reference's
@@ -387,15 +390,16 @@ class Mbvh:
             pass
 
 
-def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False, exact_nodes=False):
+def _trace(fn, handle, rays, t_max, any_hit, stats, stream, reorder=False, exact_nodes=False, walk_stats=False):
     r = _cuda_f32(rays, 6)
     n = r.shape[0]
     tm = _cuda_f32(t_max).reshape(-1) if t_max is not None else None
     hits = torch.empty((n, 4), dtype=torch.float32, device=r.device)
-    st = torch.empty((n, 3), dtype=torch.int32, device=r.device) if stats else None
+    st = torch.empty((n, 3), dtype=torch.int32, device=r.device) if (stats or walk_stats) else None
     flags = (_ffi.TRACE_ANY_HIT if any_hit else 0) | (_ffi.TRACE_STATS if stats else 0)
     flags |= _ffi.TRACE_REORDER if reorder else 0
     flags |= _ffi.TRACE_EXACT_NODES if exact_nodes else 0
+    flags |= _ffi.TRACE_WALK_STATS if walk_stats else 0
     check(fn(handle, _ptr(r), _ptr(tm), n, _ptr(hits), flags, _ptr(st), _stream(stream)), "intersect")
     return hits, st
 

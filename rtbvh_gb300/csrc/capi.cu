@@ -854,6 +854,10 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
 static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const float* t_max, uintptr_t ray_count,
                                float* hits, uint32_t flags, uint32_t* stats, cudaStream_t s) {
   TraceArgs a;
+  const bool walk_stats = (flags & RTBVH_TRACE_WALK_STATS) != 0;
+  if (walk_stats && (!mbvh || (flags & (RTBVH_TRACE_STATS | RTBVH_TRACE_ANY_HIT | RTBVH_TRACE_EXACT_NODES |
+                                        RTBVH_TRACE_REORDER))))
+    return InvalidArgument;
   {
     std::lock_guard<std::mutex> lock(g_mu);
     Entry* e = lookup(id, mbvh);
@@ -866,6 +870,7 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
       a.q_count = e->wcount;
       a.q_gates = e->q_gates;
     }
+    if (walk_stats && (a.qnodes == nullptr || a.q_count == 0)) return InvalidArgument;
     a.nodes = e->d_nodes;
     a.node_count = e->node_count;
     a.tris = e->d_tris;
@@ -878,7 +883,9 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
   a.t_max = t_max;
   a.ray_count = ray_count;
   a.hits = reinterpret_cast<float4*>(hits);
+  if (walk_stats && stats == nullptr) return Error;
   a.stats = (flags & RTBVH_TRACE_STATS) ? stats : nullptr;
+  a.walk_stats = walk_stats ? stats : nullptr;
   a.any_hit = (flags & RTBVH_TRACE_ANY_HIT) != 0;
   a.reorder = (flags & RTBVH_TRACE_REORDER) != 0;
   cudaError_t err = mbvh ? launch_trace_mbvh(a, s) : launch_trace_bvh(a, s);
@@ -1029,7 +1036,7 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
     float* dh = static_cast<float*>(const_cast<void*>(mapped_host(hits)));
     const float* dt = t_max ? static_cast<const float*>(mapped_host(t_max)) : nullptr;
     if (dr && dh && (t_max == nullptr || dt)) {
-      ResultCode rc = trace_common(mbvh.id, true, dr, dt, ray_count, dh, flags & ~RTBVH_TRACE_STATS, nullptr,
+      ResultCode rc = trace_common(mbvh.id, true, dr, dt, ray_count, dh, flags & ~(RTBVH_TRACE_STATS | RTBVH_TRACE_WALK_STATS), nullptr,
                                    streams[0]);
       if ((e = cudaStreamSynchronize(streams[0]))) return cuda_rc(e);
       return rc;
@@ -1056,7 +1063,7 @@ ResultCode rtbvh_intersect_mbvh_batch(RTMbvh mbvh, const float* rays, const floa
     if (t_max && (e = cudaMemcpyAsync(d_tmax[k].ptr, t_max + c0, 4 * cnt, cudaMemcpyHostToDevice, s)))
       return cuda_rc(e);
     rc = trace_common(mbvh.id, true, d_rays[k].ptr, t_max ? d_tmax[k].ptr : nullptr, cnt,
-                      reinterpret_cast<float*>(d_hits[k].ptr), flags & ~RTBVH_TRACE_STATS, nullptr, s);
+                      reinterpret_cast<float*>(d_hits[k].ptr), flags & ~(RTBVH_TRACE_STATS | RTBVH_TRACE_WALK_STATS), nullptr, s);
     if (rc != Ok) break;
     if ((e = cudaMemcpyAsync(hits + 4 * c0, d_hits[k].ptr, 16 * cnt, cudaMemcpyDeviceToHost, s))) return cuda_rc(e);
     c0 += cnt;

@@ -204,6 +204,9 @@ struct TraceArgs {
   // Stack bound of the compact closest-hit walk: 32, 48 or 64 entries (0:
   // 64). A ray that needs more reports prim -2 and kStatusStackOverflow.
   uint32_t stack_limit = 0;
+  // Optional per-ray counts of the compact closest-hit walk (3 per ray:
+  // traversal-tree node visits, triangle tests, 1 if handed to the exact walk).
+  uint32_t* walk_stats = nullptr;
   // Internal: the ray count is read from this device word (at most ray_count).
   const unsigned int* ray_count_dev = nullptr;
 };

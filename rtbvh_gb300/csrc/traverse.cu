@@ -501,12 +501,16 @@ __device__ __forceinline__ void slot_keys_exact(const DMNode* node, const RaySta
 // and traced afterwards by k_trace_mbvh over the exact Mbvh.
 // Nine resident blocks per SM (56 registers, 36 warps; a few bytes of
 // spills): measured 4 % faster than the 64-register, 32-warp form.
-template <int STACK, bool GATES>
+//
+// WSTATS: per-ray counts of this walk in a.walk_stats (traversal-tree node
+// visits, triangle tests, 1 if the ray was handed to the exact walk).
+template <int STACK, bool GATES, bool WSTATS>
 __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsigned int* work, uint32_t* deferred,
                                                            unsigned int* deferred_count) {
   RayState ray;
   float hu = 0.0f, hv = 0.0f;
   int32_t prim = -1;
+  uint32_t w_visits = 0, w_tests = 0;
   int32_t stack[STACK];
   int sp = -1;
   int32_t next = -1;
@@ -519,12 +523,21 @@ __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsign
   WarpPool pool;
   const uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
   const uint32_t ray_count = (uint32_t)a.ray_count;
+  auto write_stats = [&](uint32_t handed_on) {
+    if (WSTATS) {
+      a.walk_stats[3 * (size_t)r + 0] = w_visits;
+      a.walk_stats[3 * (size_t)r + 1] = w_tests;
+      a.walk_stats[3 * (size_t)r + 2] = handed_on;
+    }
+  };
   auto finish = [&]() {
     a.hits[r] = make_float4(ray.t, hu, hv, __int_as_float(prim));
+    write_stats(0u);
     active = false;
   };
   auto defer = [&]() {
     deferred[atomicAdd(deferred_count, 1u)] = r;
+    write_stats(1u);
     active = false;
   };
   auto start_ray = [&](uint32_t rr) {
@@ -535,6 +548,7 @@ __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsign
     sp = -1;
     pend = 0;
     next = 0;
+    w_visits = w_tests = 0;
     if (a.node_count == 0) {
       finish();
       return;
@@ -578,6 +592,7 @@ __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsign
         float h0[8], h1[8];
         ld8(qn, h0);
         ld8(qn + 8, h1);
+        if (WSTATS) ++w_visits;
         const uint32_t flags = __float_as_uint(h0[3]) >> 24;
         if (flags & kQFlagOutOfRange) {
           defer();
@@ -618,6 +633,7 @@ __global__ void __launch_bounds__(kBlock, 9) k_trace_compact(TraceArgs a, unsign
       } else {
         for (int32_t j = 0; j < count; ++j) {
           const float4* tri = a.tris + kTriFloat4 * (size_t)(lf + j);
+          if (WSTATS) ++w_tests;
           if (mt_test(tri, ray, hu, hv, prim) && GATES && (__float_as_uint(__ldg(&tri[1].w)) & kTriEscape)) {
             defer();  // an escaped triangle is hit: its hits are the exact walk's
             break;
@@ -975,13 +991,18 @@ cudaError_t launch3(const TraceArgs& a, cudaStream_t s, unsigned int* work) {
 // Closest hit through the compact traversal tree, then the rays it deferred
 // over the exact Mbvh. counters: [0] compact ray counter, [1] deferred rays,
 // [2] exact ray counter (zeroed).
+template <bool WSTATS>
+auto compact_kernel(const TraceArgs& a) {
+  return a.q_gates ? (a.stack_limit == 32   ? k_trace_compact<32, true, WSTATS>
+                      : a.stack_limit == 48 ? k_trace_compact<48, true, WSTATS>
+                                            : k_trace_compact<64, true, WSTATS>)
+                   : (a.stack_limit == 32   ? k_trace_compact<32, false, WSTATS>
+                      : a.stack_limit == 48 ? k_trace_compact<48, false, WSTATS>
+                                            : k_trace_compact<64, false, WSTATS>);
+}
+
 cudaError_t launch_compact(const TraceArgs& a, cudaStream_t s, unsigned int* counters, uint32_t* deferred) {
-  auto kern = a.q_gates ? (a.stack_limit == 32   ? k_trace_compact<32, true>
-                           : a.stack_limit == 48 ? k_trace_compact<48, true>
-                                                 : k_trace_compact<64, true>)
-                        : (a.stack_limit == 32   ? k_trace_compact<32, false>
-                           : a.stack_limit == 48 ? k_trace_compact<48, false>
-                                                 : k_trace_compact<64, false>);
+  auto kern = a.walk_stats ? compact_kernel<true>(a) : compact_kernel<false>(a);
   kern<<<persistent_grid(kern, a), kBlock, 0, s>>>(a, counters, deferred, counters + 1);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;

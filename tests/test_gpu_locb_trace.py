@@ -558,3 +558,50 @@ def test_moved_triangles_keep_the_reference_hits():
     m.attach_triangles(to_cuda(tris))
     assert not _escaped(m).any()
 
+
+
+@pytest.mark.parametrize("name,kind", [("incoherent_300k", "locb"), ("sphere", "sah")])
+def test_walk_stats_of_the_compact_walk(name, kind):
+    """RTBVH_TRACE_WALK_STATS: the default walk's own per-ray counts. The
+    hits equal the call without the flag bit for bit; every ray taken by the
+    compact walk visits the root, every reported hit of that walk comes from
+    a triangle test; rays handed on to the exact walk are flagged (none on an
+    LOCB tree, some on the binned-SAH sphere whose boxes miss triangles); on
+    the LOCB tree the walk visits fewer nodes and tests fewer triangles than
+    the reference's iterator (RTBVH_TRACE_STATS) on average."""
+    tris = scene(name)
+    m = rb.Mbvh.construct(gpu_build(tris, kind))
+    rays = scenes.camera_rays(1024, 1024) if name == "sphere" else rays_for(name, count=262144)[0]
+    d_rays = to_cuda(rays)
+    plain = m.intersect(d_rays)[0].cpu().numpy()
+    hits, ws = m.intersect(d_rays, walk_stats=True)
+    hits, ws = hits.cpu().numpy(), ws.cpu().numpy()
+    assert m.status() == rb.ResultCode.Ok
+    assert np.array_equal(u32(hits), u32(plain))
+    own = ws[:, 2] == 0
+    assert set(np.unique(ws[:, 2]).tolist()) <= {0, 1}
+    assert (ws[own, 0] >= 1).all()
+    hit = rb.hit_prims(hits) >= 0
+    assert (ws[own & hit, 1] >= 1).all()
+    handed = int((~own).sum())
+    if kind == "locb":
+        assert handed == 0
+    else:
+        assert 0 < handed < len(rays) // 50
+    if kind == "locb":
+        # the traversal tree of an LOCB build is the tighter one
+        _, ref = m.intersect(d_rays, stats=True)
+        ref = ref.cpu().numpy()
+        assert ws[:, 0].mean() < ref[:, 0].mean()
+        assert ws[:, 1].mean() < ref[:, 1].mean()
+    lib = _ffi.load()
+    st = torch.empty((len(rays), 3), dtype=torch.int32, device="cuda")
+    h = torch.empty((len(rays), 4), dtype=torch.float32, device="cuda")
+    for extra in (_ffi.TRACE_STATS, _ffi.TRACE_ANY_HIT, _ffi.TRACE_EXACT_NODES, _ffi.TRACE_REORDER):
+        rc = lib.rtbvh_gpu_intersect_mbvh(m.handle, ctypes.c_void_p(d_rays.data_ptr()), None, len(rays),
+                                          ctypes.c_void_p(h.data_ptr()), _ffi.TRACE_WALK_STATS | extra,
+                                          ctypes.c_void_p(st.data_ptr()), None)
+        assert rc == rb.ResultCode.InvalidArgument
+    rc = lib.rtbvh_gpu_intersect_mbvh(m.handle, ctypes.c_void_p(d_rays.data_ptr()), None, len(rays),
+                                      ctypes.c_void_p(h.data_ptr()), _ffi.TRACE_WALK_STATS, None, None)
+    assert rc == rb.ResultCode.Error
