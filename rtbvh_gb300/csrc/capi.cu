@@ -37,6 +37,7 @@ struct Entry {
   DMNode* d_mnodes = nullptr;     // Mbvh
   DQNode* d_qnodes = nullptr;     // Mbvh: closest-hit traversal tree, compact nodes
   DMNode* d_wnodes = nullptr;     // Mbvh: the same tree, exact nodes
+  DTBox* d_tboxes = nullptr;      // Mbvh with q_gates: subtree boxes of d_mnodes (from the triangles)
   uint32_t wcount = 0;
   bool q_gates = false;           // Mbvh: escaped triangles are flagged (collapse_entry)
   uint32_t* d_indices = nullptr;
@@ -49,12 +50,13 @@ struct Entry {
   std::vector<uint32_t> h_indices;
 
   void release() {
-    void* const arrays[] = {d_nodes, d_mnodes, d_qnodes, d_wnodes, d_indices, d_tris, d_vertices, d_status};
-    pool_free_now(arrays, 8);
+    void* const arrays[] = {d_nodes, d_mnodes, d_qnodes, d_wnodes, d_tboxes, d_indices, d_tris, d_vertices, d_status};
+    pool_free_now(arrays, 9);
     d_nodes = nullptr;
     d_mnodes = nullptr;
     d_qnodes = nullptr;
     d_wnodes = nullptr;
+    d_tboxes = nullptr;
     wcount = 0;
     q_gates = false;
     d_indices = nullptr;
@@ -114,6 +116,7 @@ bool boxes_cover(uint32_t build_type) { return build_type == 1; }
 ResultCode collapse_entry(Entry& m, cudaStream_t s, DMNode** mnodes, uint32_t* mcount) {
   m.d_wnodes = nullptr;
   m.d_qnodes = nullptr;
+  m.d_tboxes = nullptr;
   m.wcount = 0;
   m.q_gates = false;
   if (m.bvh_node_count == 0) {  // Mbvh::default()
@@ -139,11 +142,16 @@ ResultCode collapse_entry(Entry& m, cudaStream_t s, DMNode** mnodes, uint32_t* m
   t.vertex_count = m.vertex_count;
   t.tris = m.d_tris;
   t.tb = tb.ptr;
+  t.tboxes_out = &m.d_tboxes;
   uint32_t escaped = 0;
   if ((rc = build_mbvh(m.d_nodes, m.bvh_node_count, s, mnodes, mcount, &t, &escaped)) != Ok) return rc;
   // boxes recomputed from the triangles nest by construction
   rc = build_wide(tb.ptr, m.bvh_node_count, check, m.prim_count, s, &m.d_wnodes, &m.d_qnodes, &m.wcount, true);
   m.q_gates = escaped != 0 && m.wcount != 0;
+  if (!m.q_gates) {  // no ray is handed on for an escape: the subtree boxes would go unused
+    pool_free(m.d_tboxes, s);
+    m.d_tboxes = nullptr;
+  }
   return rc;
 }
 
@@ -839,8 +847,8 @@ ResultCode rtbvh_gpu_set_triangles(uint32_t structure_id, int is_mbvh, const flo
   if (!is_mbvh) return Ok;
   {
     // the old tree may still be read by traversals on other streams
-    void* const old_arrays[] = {e->d_qnodes, e->d_wnodes};
-    pool_free_now(old_arrays, 2);
+    void* const old_arrays[] = {e->d_qnodes, e->d_wnodes, e->d_tboxes};
+    pool_free_now(old_arrays, 3);
   }
   // the quad nodes come out as they are (same BVH2 nodes); only the
   // traversal tree and the escape flags are kept
@@ -869,6 +877,7 @@ static ResultCode trace_common(uint32_t id, bool mbvh, const float* rays, const 
       a.qexact = e->d_wnodes;
       a.q_count = e->wcount;
       a.q_gates = e->q_gates;
+      a.tboxes = e->q_gates ? e->d_tboxes : nullptr;
     }
     if (walk_stats && (a.qnodes == nullptr || a.q_count == 0)) return InvalidArgument;
     a.nodes = e->d_nodes;
@@ -1124,13 +1133,14 @@ static ResultCode recollapse(Entry* m, const float* vertices, cudaStream_t s) {
   cudaError_t err;
   {
     // the old arrays may still be read by traversals on other streams
-    void* const old_arrays[] = {m->d_mnodes, m->d_qnodes, m->d_wnodes};
-    pool_free_now(old_arrays, 3);
+    void* const old_arrays[] = {m->d_mnodes, m->d_qnodes, m->d_wnodes, m->d_tboxes};
+    pool_free_now(old_arrays, 4);
   }
   const uint32_t expected = m->node_count;
   m->d_mnodes = nullptr;
   m->d_qnodes = nullptr;
   m->d_wnodes = nullptr;
+  m->d_tboxes = nullptr;
   m->wcount = 0;
   m->q_gates = false;
   if (vertices) {

@@ -62,6 +62,17 @@ struct alignas(64) DQNode {
   int16_t counts[4];
 };
 static_assert(sizeof(DQNode) == 64, "DQNode must be 64 bytes");
+// The boxes of a quad node's four slots computed from their subtrees'
+// triangles (each triangle's vertex box grown by 1e-4, united up the
+// subtree), for the exact-order walk of binned-SAH trees, whose own slot
+// boxes can miss triangles: a slot whose subtree box the ray cannot enter
+// below its current t holds no hit. Slots with a bound beyond
+// kCompactRange (or a NaN) get the infinite box, which every finite ray
+// enters. Three 256-bit loads.
+struct alignas(32) DTBox {
+  float min_x[4], max_x[4], min_y[4], max_y[4], min_z[4], max_z[4];
+};
+static_assert(sizeof(DTBox) == 96, "DTBox must be 96 bytes");
 constexpr uint32_t kQFlagExact = 1u;
 constexpr uint32_t kQFlagOutOfRange = 2u;
 constexpr float kQuantRange = 1e18f;  // larger inverse-direction components use the exact nodes

@@ -109,7 +109,9 @@ ResultCode build_spatial_sah(const DAabb* aabbs, const float4* centers, const fl
 // `indices` (index_count slots), which index `vertices` (vertex_count
 // triangles, 9 floats each); `tris` are the leaf-ordered triangle records
 // (kTriFloat4 float4 per index slot) whose flags word gets kTriEscape or 0;
-// `tb` (node_count entries) receives the traversal boxes.
+// `tb` (node_count entries) receives the traversal boxes; with
+// `tboxes_out`, build_mbvh also allocates the quad nodes' subtree boxes
+// (DTBox per quad node, from `tb`) and stores them there.
 struct MbvhTriangles {
   const uint32_t* indices = nullptr;
   uint32_t index_count = 0;
@@ -117,6 +119,7 @@ struct MbvhTriangles {
   uint32_t vertex_count = 0;
   float4* tris = nullptr;
   DAabb* tb = nullptr;
+  DTBox** tboxes_out = nullptr;
 };
 // Mbvh::construct (src/bvh.rs:381-404). mnodes is allocated here. With
 // `tri` (for BVH2s whose boxes need not contain these triangles: binned-SAH
@@ -204,6 +207,10 @@ struct TraceArgs {
   // Stack bound of the compact closest-hit walk: 32, 48 or 64 entries (0:
   // 64). A ray that needs more reports prim -2 and kStatusStackOverflow.
   uint32_t stack_limit = 0;
+  // Optional subtree boxes of the quad nodes (mnodes): the exact-order pass
+  // over the rays the compact walk hands on also skips slots whose subtree
+  // box the ray cannot enter below its current t.
+  const DTBox* tboxes = nullptr;
   // Optional per-ray counts of the compact closest-hit walk (3 per ray:
   // traversal-tree node visits, triangle tests, 1 if handed to the exact walk).
   uint32_t* walk_stats = nullptr;

@@ -145,6 +145,7 @@ struct CollapseParams {
   MbvhTriangles tri;
   DAabb* ibox;
   uint32_t* escaped;
+  DTBox* tboxes;  // optional (TRIS): subtree boxes of every quad node's slots
 };
 
 __device__ __forceinline__ void set_slot_box(DMNode& m, int i, const DAabb& b) {
@@ -211,6 +212,7 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
   }
   int32_t nodes_[4] = {-1, -1, -1, -1};
   int32_t leafs[4] = {-1, -1, -1, -1};
+  int32_t sub[4] = {-1, -1, -1, -1};  // BVH2 node under each slot (TRIS: its box from the triangles)
   if (cur.left_first >= 0) {
     const uint32_t lf = (uint32_t)cur.left_first;
 #pragma unroll
@@ -224,6 +226,7 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
           if (cn.count >= 0) {
             nodes_[s0] = (int32_t)clf;
             leafs[s0] = cn.count;
+            sub[s0] = (int32_t)child;
           } else if (clf + 1 < p.node_count) {
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
@@ -235,6 +238,7 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
                 nodes_[s0 + k] = (int32_t)(clf + k);
               }
               set_slot_box(m, s0 + k, g);
+              sub[s0 + k] = (int32_t)(clf + k);
             }
           } else {
             atomicOr(p.status, kStatusBadIndex);
@@ -273,6 +277,25 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
 #pragma unroll
     for (int k = 0; k < 8; ++k) dst[k] = src[k];
     if (TRIS) mark_escapes(p, mi, m);
+    if (TRIS && p.tboxes) {
+      DTBox t;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        bool ok = sub[i] >= 0 && (uint32_t)sub[i] < p.node_count;
+        DAabb b = cur;
+        if (ok) b = load_aabb_cg(p.tri.tb + sub[i]);
+        for (int a = 0; a < 3; ++a)  // false for NaN
+          ok = ok && fabsf(b.min[a]) <= kCompactRange && fabsf(b.max[a]) <= kCompactRange;
+        const float inf = __int_as_float(0x7f800000);
+        t.min_x[i] = ok ? b.min[0] : -inf; t.max_x[i] = ok ? b.max[0] : inf;
+        t.min_y[i] = ok ? b.min[1] : -inf; t.max_y[i] = ok ? b.max[1] : inf;
+        t.min_z[i] = ok ? b.min[2] : -inf; t.max_z[i] = ok ? b.max[2] : inf;
+      }
+      float4* td = reinterpret_cast<float4*>(p.tboxes + mi);
+      const float4* ts = reinterpret_cast<const float4*>(&t);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) td[k] = ts[k];
+    }
   } else {
     atomicOr(p.status, kStatusBadIndex);
   }
@@ -516,9 +539,18 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
     k_ibox_init<<<1, 32, 0, s>>>(ibox.ptr);
   }
   DMNode* mnodes = nullptr;
+  DTBox* tboxes = nullptr;
   if ((e = device_alloc(&mnodes, m_total, s))) return cuda_rc(e);
-  if ((e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s))) {
+  if (with_tris && tri->tboxes_out && (e = device_alloc(&tboxes, m_total, s))) {
     pool_free(mnodes, s);
+    return cuda_rc(e);
+  }
+  auto drop = [&]() {
+    pool_free(mnodes, s);
+    pool_free(tboxes, s);
+  };
+  if ((e = cudaMemsetAsync(bar.ptr, 0, sizeof(GridBarrier), s))) {
+    drop();
     return cuda_rc(e);
   }
   auto kern = with_tris ? k_collapse<true> : k_collapse<false>;
@@ -543,22 +575,24 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   if (with_tris) p.tri = *tri;
   p.ibox = ibox.ptr;
   p.escaped = status.ptr + 2;
+  p.tboxes = tboxes;
   void* args[] = {&p};
   if ((e = cudaLaunchCooperativeKernel((void*)kern, dim3(grid), dim3(kBlock), args, 0, s))) {
-    pool_free(mnodes, s);
+    drop();
     return cuda_rc(e);
   }
   uint32_t st[3] = {0, 0, 0};
   if ((e = cudaMemcpyAsync(st, status.ptr, 12, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
-    pool_free(mnodes, s);
+    drop();
     return cuda_rc(e);
   }
   if (st[0] != 0) {
-    pool_free(mnodes, s);
+    drop();
     return (st[0] & kStatusTimeout) ? Timeout : Error;
   }
   *mnodes_out = mnodes;
   *mnode_count = m_total;
+  if (with_tris && tri->tboxes_out) *tri->tboxes_out = tboxes;
   if (escaped_out) *escaped_out = st[2];
   return Ok;
 }
@@ -679,6 +713,7 @@ cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, co
   p.c.status = status;
   p.c.ibox = nullptr;
   p.c.escaped = nullptr;
+  p.c.tboxes = nullptr;
   p.prim_off = prim_off;
   p.order = order;
   p.mbase = mbase;

@@ -238,11 +238,41 @@ __device__ __forceinline__ uint32_t ray_mesh(const TraceArgs& a, uint32_t r) {
   return lo;
 }
 
+// Hit mask of a quad node's subtree boxes (DTBox): slot i is set when the
+// ray can enter its box at some t in [0, r.t). Finite rays within the
+// compact walk's range only (the rounding argument of kCompactRange: a box
+// that holds a triangle hit at t > 1e-4 passes).
+__device__ __forceinline__ uint32_t subtree_mask(const DTBox* box, const RayState& r) {
+  const float* q = reinterpret_cast<const float*>(box);
+  float vx[8], vy[8], vz[8];
+  ld8(q, vx);
+  ld8(q + 8, vy);
+  ld8(q + 16, vz);
+  uint32_t m = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float tx0 = (vx[i] - r.ox) * r.ix, tx1 = (vx[4 + i] - r.ox) * r.ix;
+    const float ty0 = (vy[i] - r.oy) * r.iy, ty1 = (vy[4 + i] - r.oy) * r.iy;
+    const float tz0 = (vz[i] - r.oz) * r.iz, tz1 = (vz[4 + i] - r.oz) * r.iz;
+    const float tn = fmaxf(fminf(tx0, tx1), fmaxf(fminf(ty0, ty1), fminf(tz0, tz1)));
+    const float tx = fminf(fmaxf(tx0, tx1), fminf(fmaxf(ty0, ty1), fmaxf(tz0, tz1)));
+    if (tx >= tn && tx >= 0.0f && tn < r.t) m |= 1u << i;
+  }
+  return m;
+}
+
 // Persistent MBVH traversal over the exact quad nodes with per-lane ray
 // refill. Each loop iteration visits one quad node per lane; a ray's
 // node/triangle order is the reference's. With ray_count_dev the number of
 // rays is read from the device (the rays the compact kernel deferred).
-template <bool ANY_HIT, bool STATS>
+//
+// TCULL (closest hit over a binned-SAH tree's quad nodes with a.tboxes):
+// a slot whose subtree box (from the triangles) the ray cannot enter below
+// its current t is skipped. The reference would walk that subtree and
+// accept no hit in it (every triangle lies inside the subtree box), so t
+// and the order of all later tests are unchanged: the hit is the
+// reference's bit for bit (the node counts are not, so STATS never culls).
+template <bool ANY_HIT, bool STATS, bool TCULL = false>
 __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int* work) {
   RayState ray;
   float hu = 0.0f, hv = 0.0f;
@@ -256,7 +286,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
   int sp = -1;
   int32_t next = -1;
   uint32_t r = 0;
-  bool active = false, fast = true;
+  bool active = false, fast = true, cull = false;
   WarpPool pool;
   uint32_t batch = a.ray_batch ? a.ray_batch : kPoolBatch;
   const uint32_t ray_count = a.ray_count_dev ? *a.ray_count_dev : (uint32_t)a.ray_count;
@@ -270,6 +300,17 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     r = a.order ? __ldg(a.order + rr) : rr;
     ray = load_ray(a.rays, r, a.t_max);
     fast = finite_ray(ray);
+    if (TCULL && a.node_count > 0) {
+      // |x| <= bound is false for NaN and infinities. Only rays that start
+      // inside the scene's root box: boxes behind them are most of what the
+      // cull saves; for rays from outside it costs more than it saves
+      const DAabb root = load_aabb(a.nodes);
+      cull = fabsf(ray.ox) <= kCompactRange && fabsf(ray.oy) <= kCompactRange && fabsf(ray.oz) <= kCompactRange &&
+             fabsf(ray.dx) <= 3.0e38f && fabsf(ray.dy) <= 3.0e38f && fabsf(ray.dz) <= 3.0e38f &&
+             fabsf(ray.ix) <= kQuantRange && fabsf(ray.iy) <= kQuantRange && fabsf(ray.iz) <= kQuantRange &&
+             ray.ox >= root.min[0] && ray.oy >= root.min[1] && ray.oz >= root.min[2] && ray.ox <= root.max[0] &&
+             ray.oy <= root.max[1] && ray.oz <= root.max[2];
+    }
     hu = hv = 0.0f;
     prim = -1;
     visits = tests = max_depth = 0;
@@ -320,6 +361,7 @@ __global__ void __launch_bounds__(kBlock) k_trace_mbvh(TraceArgs a, unsigned int
     bool done = false;
     if (fast) quad_intersect<true>(a.mnodes + current, ray, mask, ids, children, counts);
     else quad_intersect<false>(a.mnodes + current, ray, mask, ids, children, counts);
+    if (TCULL && cull) mask &= subtree_mask(a.tboxes + current, ray);
     if (STATS) ++visits;
 #pragma unroll 1
     for (int i = 0; i < 4; ++i) {
@@ -1012,6 +1054,11 @@ cudaError_t launch_compact(const TraceArgs& a, cudaStream_t s, unsigned int* cou
   // at most 32 rays per refill (the kernel takes fewer when few rays were
   // deferred)
   b.ray_batch = 32;
+  if (b.tboxes) {
+    auto cull_kern = k_trace_mbvh<false, false, true>;
+    cull_kern<<<persistent_grid(cull_kern, b), kBlock, 0, s>>>(b, counters + 2);
+    return cudaGetLastError();
+  }
   return launch3<true, false, false>(b, s, counters + 2);
 }
 

@@ -588,6 +588,10 @@ def test_walk_stats_of_the_compact_walk(name, kind):
         assert handed == 0
     else:
         assert 0 < handed < len(rays) // 50
+        # the pass over handed-on rays skips subtrees without a hit but keeps
+        # the reference's order: its hits are the exact walk's, bit for bit
+        exact = m.intersect(d_rays, exact_nodes=True)[0].cpu().numpy()
+        assert np.array_equal(u32(hits[~own]), u32(exact[~own]))
     if kind == "locb":
         # the traversal tree of an LOCB build is the tighter one
         _, ref = m.intersect(d_rays, stats=True)
