@@ -4,14 +4,19 @@
 // Morton codes of the centres -> stable radix sort -> leaves (sorted boxes
 // + 1e-4) -> clustering levels until one node is left.
 //
-// All clustering levels run in ONE cooperative launch. A level of m nodes
-// [begin, end) does, with a grid barrier after each phase:
-//   1. nearest neighbour of every node inside the window
-//      [max(begin, i-14), min(end, i+15)) by the half area of the union,
-//      first (lowest index) minimum wins -- boxes staged in shared memory;
-//   2. per-block counts of the merge flags (i < j, nb[j] == i);
-//   3. the inclusive prefix of the flags and the scatter of parents,
+// The clustering levels above kTailNodes nodes run in ONE cooperative
+// launch. A level of m nodes [begin, end) does, with a grid barrier after
+// each phase:
+//   A. for a contiguous chunk per block: the nearest neighbour of every
+//      node inside the window [max(begin, i-14), min(end, i+15)) by the
+//      half area of the union, first (lowest index) minimum wins -- boxes
+//      staged in shared memory, the neighbours of a 14-node halo on either
+//      side recomputed -- so the block knows its nodes' merge flags
+//      (i < j, nb[j] == i) and counts them at once;
+//   B. the prefix of the blocks' counts and the scatter of parents,
 //      unmerged nodes (next level) and children (final node array).
+// (The segmented builds of many meshes use the three-phase form of the
+// same level: nn_tile, the flag count, scatter_tile.)
 // Node positions follow the reference exactly (locb.rs:178-215), so the
 // output is bit-identical to the reference's node array. Levels of at most
 // kTailNodes nodes are finished by k_locb_tail: one block of 1024 threads
@@ -185,9 +190,133 @@ __device__ bool locb_block_finish(DAabb* const lvl[2], DAabb* final_nodes, uint3
   return true;
 }
 
+// Merge state of node i of a wide level, kept in the top bits of its nb word
+// (neighbour indices are below 2^30): kPairHead when i < nb[i] and
+// nb[nb[i]] == i (i heads a merged pair: the merge flag of locb.rs:159-167),
+// kPairTail when nb[i] < i and nb[nb[i]] == i.
+constexpr uint32_t kPairHead = 1u << 30;
+constexpr uint32_t kPairTail = 2u << 30;
+constexpr uint32_t kNbMask = (1u << 30) - 1u;
+constexpr int kHalo = 2 * kRadius;  // boxes a sub-tile stages on each side
+
+// Phase A for the sub-tile [s0, s1) of a block's chunk of the level
+// [begin, end): the nearest neighbours of the nodes [s0 - 14, s1 + 14) --
+// the sub-tile and the halo its merge states depend on, with nn_tile's
+// window and tie rule; the boxes [s0 - 28, s1 + 28) staged in shared
+// memory -- then each sub-tile node's neighbour and merge state go to nb.
+// Returns the thread's count of pair heads.
+__device__ uint32_t nn_state_tile(const DAabb* in, uint32_t* nb, uint32_t begin, uint32_t end, uint32_t s0,
+                                  uint32_t s1, SBox* s_box, uint16_t* s_nb, uint32_t* status) {
+  const int64_t base = (int64_t)s0 - kHalo;  // s_box[k] holds node base + k
+  const int span = kBlock + 2 * kHalo;
+  for (int k = threadIdx.x; k < span; k += kBlock) {
+    const int64_t idx = base + k;
+    if (idx >= (int64_t)begin && idx < (int64_t)end) s_box[k] = to_sbox(load_aabb_cg(in + idx));
+  }
+  __syncthreads();
+  // nodes [n0, n1): s_nb[x - (s0 - 14)] = neighbour of x, as an index into s_box
+  const uint32_t n0 = s0 > begin + kRadius ? s0 - kRadius : begin;
+  const uint32_t n1 = min(s1 + kRadius, end);
+  for (uint32_t x = n0 + threadIdx.x; x < n1; x += kBlock) {
+    const uint32_t sb = (x > begin + kRadius) ? x - kRadius : begin;
+    const uint32_t se = min(x + kRadius + 1, end);
+    const SBox bx = s_box[x - base];
+    float best = 3.40282347e+38f;
+    int64_t best_j = -1;
+    for (uint32_t j = sb; j < x; ++j) {
+      const float d = union_half_area(s_box[j - base], bx);
+      if (d < best) { best = d; best_j = j; }
+    }
+    for (uint32_t j = x + 1; j < se; ++j) {
+      const float d = union_half_area(bx, s_box[j - base]);
+      if (d < best) { best = d; best_j = j; }
+    }
+    if (best_j < 0) {
+      atomicOr(status, kStatusNoNeighbour);
+      best_j = x;
+    }
+    s_nb[x - (s0 - kRadius)] = (uint16_t)(best_j - base);
+  }
+  __syncthreads();
+  uint32_t heads = 0;
+  const uint32_t i = s0 + threadIdx.x;
+  if (i < s1) {
+    const int64_t rel = (int64_t)s0 - kRadius - base;  // s_nb index of node v: v - base - rel
+    const uint32_t j = (uint32_t)(base + s_nb[i - base - rel]);
+    const uint32_t jj = (uint32_t)(base + s_nb[j - base - rel]);
+    uint32_t state = 0;
+    if (jj == i && i < j) state = kPairHead;
+    else if (jj == i && j < i) state = kPairTail;
+    nb[i] = j | state;
+    heads = state == kPairHead ? 1u : 0u;
+  }
+  __syncthreads();
+  return heads;
+}
+
+// Phase B for the sub-tile [s0, s1): the prefix of the pair heads (carry:
+// heads before s0 in the level) and the placement of scatter_tile, from the
+// nb words phase A left (heads up to 14 nodes past s1 may belong to the next
+// block's chunk). Returns the carry for the next sub-tile.
+__device__ uint32_t place_tile(const DAabb* in, DAabb* out, DAabb* final_nodes, const uint32_t* nb, uint32_t begin,
+                               uint32_t end, uint32_t s0, uint32_t s1, uint32_t carry, uint32_t mc, uint32_t* s_word,
+                               uint32_t* s_warp, uint32_t* status) {
+  for (int k = threadIdx.x; k < kBlock + kRadius; k += kBlock) {
+    const uint32_t idx = s0 + k;
+    s_word[k] = idx < end ? __ldcg(nb + idx) : 0u;
+  }
+  __syncthreads();
+  const uint32_t i = s0 + threadIdx.x;
+  const uint32_t w = i < s1 ? s_word[threadIdx.x] : 0u;
+  uint32_t tile_total;
+  const uint32_t incl = block_inclusive_scan<kBlock>((w & kPairHead) ? 1u : 0u, s_warp, &tile_total) + carry;
+  const uint32_t unmerged_begin = begin - mc;
+  const uint32_t children_begin = end - 2u * mc;
+  if (i < s1) {
+    const uint32_t merged_i = incl;
+    if (w & kPairHead) {
+      const uint32_t j = w & kNbMask;
+      uint32_t merged_j = merged_i;
+      for (uint32_t k = i + 1; k <= j; ++k) merged_j += (s_word[k - s0] & kPairHead) ? 1u : 0u;
+      const uint32_t pos = unmerged_begin + j - begin - merged_j;
+      const uint32_t fc = children_begin + (merged_i - 1u) * 2u;
+      const DAabb a = load_aabb_cg(in + i), b = load_aabb_cg(in + j);
+      DAabb par;
+#pragma unroll
+      for (int ax = 0; ax < 3; ++ax) {
+        par.min[ax] = rs_min(b.min[ax], a.min[ax]);
+        par.max[ax] = rs_max(b.max[ax], a.max[ax]);
+      }
+      par.count = -1;
+      par.left_first = (int32_t)fc;
+      if (j < end && pos < end && fc + 1 < end) {
+        store_aabb(out + pos, par);
+        store_aabb(final_nodes + fc, a);
+        store_aabb(final_nodes + fc + 1, b);
+      } else {
+        atomicOr(status, kStatusBadIndex);
+      }
+    } else if (!(w & kPairTail)) {
+      const uint32_t pos = unmerged_begin + i - begin - merged_i;
+      if (pos < end) store_aabb(out + pos, load_aabb_cg(in + i));
+      else atomicOr(status, kStatusBadIndex);
+    }
+  }
+  __syncthreads();
+  return carry + tile_total;
+}
+
+// The clustering levels above kTailNodes nodes. Per level, two phases with
+// a grid barrier after each: (A) every block takes a contiguous chunk of
+// the level and computes the nearest neighbours of its nodes and of a
+// 14-node halo on either side (the halo is recomputed, not waited for), so
+// it knows its nodes' merge states and counts its pair heads at once; (B)
+// the prefix of the blocks' counts and the placement of parents, unmerged
+// nodes and children (locb.rs:178-215).
 __global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
-  __shared__ SBox s_box[kBlock + 2 * kRadius];
-  __shared__ uint32_t s_flag[kBlock + kRadius];
+  __shared__ SBox s_box[kBlock + 2 * kHalo];
+  __shared__ uint16_t s_nb[kBlock + 2 * kRadius];
+  __shared__ uint32_t s_word[kBlock + kRadius];
   __shared__ uint32_t s_warp[kBlock / 32];
   const uint32_t node_count = 2u * p.n - 1u;
   uint32_t begin = p.n - 1u, end = node_count;
@@ -200,15 +329,12 @@ __global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
     const uint32_t m = end - begin;
     const DAabb* in = p.lvl[cur];
     DAabb* out = p.lvl[cur ^ 1];
-    for (uint32_t tile = blockIdx.x; (size_t)tile * kBlock < m; tile += G)
-      nn_tile(in, p.nb, begin, end, begin + tile * kBlock, s_box, p.status);
-    if (!grid_sync(p.bar, G, p.status)) return;
-
     const uint32_t chunk = (m + G - 1) / G;
     const uint32_t c0 = min(begin + blockIdx.x * chunk, end);
     const uint32_t c1 = min(c0 + chunk, end);
     uint32_t local = 0;
-    for (uint32_t i = c0 + threadIdx.x; i < c1; i += kBlock) local += merge_flag(p.nb, i);
+    for (uint32_t s0 = c0; s0 < c1; s0 += kBlock)
+      local += nn_state_tile(in, p.nb, begin, end, s0, min(s0 + kBlock, c1), s_box, s_nb, p.status);
     uint32_t tot;
     block_inclusive_scan<kBlock>(local, s_warp, &tot);
     if (threadIdx.x == 0) p.blocksum[blockIdx.x] = tot;
@@ -230,7 +356,8 @@ __global__ void __launch_bounds__(kBlock) k_locb_levels(LocbParams p) {
     }
     uint32_t carry = pre_tot;
     for (uint32_t s0 = c0; s0 < c1; s0 += kBlock)
-      carry = scatter_tile(in, out, p.final_nodes, p.nb, begin, end, s0, c1, carry, mc, s_flag, s_warp, p.status);
+      carry = place_tile(in, out, p.final_nodes, p.nb, begin, end, s0, min(s0 + kBlock, c1), carry, mc, s_word,
+                         s_warp, p.status);
     if (!grid_sync(p.bar, G, p.status)) return;
     begin -= mc;
     end -= 2u * mc;
