@@ -146,6 +146,9 @@ struct CollapseParams {
   DAabb* ibox;
   uint32_t* escaped;
   DTBox* tboxes;  // optional (TRIS): subtree boxes of every quad node's slots
+  // optional: the quad count, read on the device; m_total then holds the
+  // capacity of mnodes / ibox / tboxes
+  const uint32_t* m_total_dev;
 };
 
 __device__ __forceinline__ void set_slot_box(DMNode& m, int i, const DAabb& b) {
@@ -303,6 +306,16 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
 
 template <bool TRIS>
 __global__ void __launch_bounds__(kBlock) k_collapse(CollapseParams p) {
+  if (p.m_total_dev) {
+    // every block reads the same word (written before the launch), so all
+    // of them return here together or none does
+    const uint32_t mt = __ldcg(p.m_total_dev);
+    if (mt == 0 || mt > p.m_total) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(p.status, kStatusBadIndex);
+      return;
+    }
+    p.m_total = mt;
+  }
   const uint32_t G = gridDim.x;
   const uint32_t tid = blockIdx.x * kBlock + threadIdx.x, nthreads = G * kBlock;
   for (uint32_t level = 0; level < p.m_total + 1; ++level) {
@@ -526,22 +539,19 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   if ((e = qcount.alloc(4, s)) || (e = bar.alloc(1, s))) return cuda_rc(e);
   if ((e = q0.alloc(node_count, s)) || (e = q1.alloc(node_count, s))) return cuda_rc(e);
   k_collapse_init<<<1, 32, 0, s>>>(cnt_e.ptr, nodes, q0.ptr, qcount.ptr, mtot.ptr);
-  uint32_t h[2] = {0, 0};
-  if ((e = cudaMemcpyAsync(h, mtot.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
-    return cuda_rc(e);
-  if (h[1] != 0) return Error;
-  const uint32_t m_total = h[0];
-  if (m_total == 0 || m_total > node_count) return Error;
+  // The quad count stays on the device (the collapse reads it); arrays are
+  // sized by its bound: quad nodes are interior BVH2 nodes, at most
+  // (node_count - 1) / 2 of a binary tree, or the root leaf.
+  const uint32_t m_cap = (node_count + 1u) / 2u;
   Scratch<DAabb> ibox;
   if (with_tris) {
-    if ((e = ibox.alloc(m_total, s))) return cuda_rc(e);
+    if ((e = ibox.alloc(m_cap, s))) return cuda_rc(e);
     k_ibox_init<<<1, 32, 0, s>>>(ibox.ptr);
   }
   DMNode* mnodes = nullptr;
   DTBox* tboxes = nullptr;
-  if ((e = device_alloc(&mnodes, m_total, s))) return cuda_rc(e);
-  if (with_tris && tri->tboxes_out && (e = device_alloc(&tboxes, m_total, s))) {
+  if ((e = device_alloc(&mnodes, m_cap, s))) return cuda_rc(e);
+  if (with_tris && tri->tboxes_out && (e = device_alloc(&tboxes, m_cap, s))) {
     pool_free(mnodes, s);
     return cuda_rc(e);
   }
@@ -558,7 +568,7 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
   unsigned grid = (unsigned)(sm_count() * per_sm);
-  const unsigned useful = (m_total + kBlock - 1) / kBlock;
+  const unsigned useful = (m_cap + kBlock - 1) / kBlock;
   if (grid > useful) grid = useful;
   if (grid < 1) grid = 1;
   CollapseParams p;
@@ -566,7 +576,8 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
   p.node_count = node_count;
   p.cnt_e = cnt_e.ptr;
   p.mnodes = mnodes;
-  p.m_total = m_total;
+  p.m_total = m_cap;
+  p.m_total_dev = mtot.ptr;
   p.queue[0] = q0.ptr;
   p.queue[1] = q1.ptr;
   p.qcount = qcount.ptr;
@@ -581,8 +592,9 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
     drop();
     return cuda_rc(e);
   }
-  uint32_t st[3] = {0, 0, 0};
-  if ((e = cudaMemcpyAsync(st, status.ptr, 12, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
+  uint32_t st[4] = {0, 0, 0, 0};
+  if ((e = cudaMemcpyAsync(st, status.ptr, 12, cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaMemcpyAsync(st + 3, mtot.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s))) {
     drop();
     return cuda_rc(e);
   }
@@ -590,6 +602,7 @@ ResultCode build_mbvh(const DAabb* nodes, uint32_t node_count, cudaStream_t s, D
     drop();
     return (st[0] & kStatusTimeout) ? Timeout : Error;
   }
+  const uint32_t m_total = st[3];  // checked on the device: 1 .. m_cap
   *mnodes_out = mnodes;
   *mnode_count = m_total;
   if (with_tris && tri->tboxes_out) *tri->tboxes_out = tboxes;
@@ -714,6 +727,7 @@ cudaError_t launch_collapse_segments(const DAabb* nodes, uint32_t node_count, co
   p.c.ibox = nullptr;
   p.c.escaped = nullptr;
   p.c.tboxes = nullptr;
+  p.c.m_total_dev = nullptr;
   p.prim_off = prim_off;
   p.order = order;
   p.mbase = mbase;
@@ -895,6 +909,12 @@ struct WideParams {
   uint32_t* qcount;   // 3 rotating counters
   GridBarrier* bar;
   uint32_t* status;
+  // optional checks run before the launch: the tree is not collapsed when
+  // check[0] != 0 (boxes that do not nest, or duplicate leaf slots) or,
+  // with expect_seen != UINT32_MAX, when check[1] (primitives seen in
+  // leaves) differs from it
+  const uint32_t* check;
+  uint32_t expect_seen;
 };
 
 // Traversal node wi from BVH2 node c. Interior slots get indices from
@@ -991,6 +1011,10 @@ __device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next
 }
 
 __global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
+  if (p.check) {  // the same words for every block: all return or none
+    const uint32_t bad = __ldcg(p.check), seen = __ldcg(p.check + 1);
+    if (bad || (p.expect_seen != kNone && seen != p.expect_seen)) return;
+  }
   const uint32_t G = gridDim.x;
   const uint32_t tid = blockIdx.x * kBlock + threadIdx.x, nthreads = G * kBlock;
   WideCtx ctx;
@@ -1172,20 +1196,18 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
     return fail(cuda_rc(e));
   const unsigned node_blocks = (node_count + kBlock - 1) / kBlock;
   // status[1]: not nested, or leaves that are not whole primitives once
-  // each -> no traversal tree (closest hit uses the exact nodes)
-  if (!nested || indices) {
+  // each -> no traversal tree (closest hit uses the exact nodes); the
+  // collapse reads the verdict on the device and does nothing then
+  const bool checked = !nested || indices;
+  Scratch<uint32_t> seen;
+  if (checked) {
     if (!nested) k_check_nested<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, status.ptr + 1);
-    Scratch<uint32_t> seen;
     if (indices) {
       if ((e = seen.alloc(index_count, s)) || (e = cudaMemsetAsync(seen.ptr, 0, (size_t)index_count * 4, s)))
         return fail(cuda_rc(e));
       k_check_leaves<<<node_blocks, kBlock, 0, s>>>(nodes, node_count, indices, index_count, seen.ptr, status.ptr + 2,
                                                     status.ptr + 1);
     }
-    uint32_t h[2] = {0, 0};
-    if ((e = cudaMemcpyAsync(h, status.ptr + 1, 8, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
-      return fail(cuda_rc(e));
-    if (h[0] || (indices && h[1] != index_count)) return fail(Ok);
   }
   k_wide_init<<<1, 32, 0, s>>>(q0.ptr, qcount.ptr, walloc.ptr);
   int per_sm = 0;
@@ -1206,17 +1228,22 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
   p.qcount = qcount.ptr;
   p.bar = bar.ptr;
   p.status = status.ptr;
+  p.check = checked ? status.ptr + 1 : nullptr;
+  p.expect_seen = indices ? index_count : kNone;
   void* args[] = {&p};
   if ((e = cudaLaunchCooperativeKernel((void*)k_wide_collapse, dim3(grid), dim3(kBlock), args, 0, s)))
     return fail(cuda_rc(e));
-  uint32_t h[2] = {0, 0};
+  // compact nodes for the live part of the tree (the node count is read on
+  // the device), then one readback for everything
+  if ((e = device_alloc(&wq, capacity, s))) return fail(cuda_rc(e));
+  if ((e = launch_quantize_mbvh(wn, capacity, wq, s, walloc.ptr))) return fail(cuda_rc(e));
+  uint32_t h[4] = {0, 0, 0, 0};
   if ((e = cudaMemcpyAsync(h, walloc.ptr, 4, cudaMemcpyDeviceToHost, s)) ||
-      (e = cudaMemcpyAsync(h + 1, status.ptr, 4, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
+      (e = cudaMemcpyAsync(h + 1, status.ptr, 12, cudaMemcpyDeviceToHost, s)) || (e = cudaStreamSynchronize(s)))
     return fail(cuda_rc(e));
+  if (checked && (h[2] || (indices && h[3] != index_count))) return fail(Ok);
   if (h[1] != 0) return fail((h[1] & kStatusTimeout) ? Timeout : Error);
   if (h[0] == 0 || h[0] > capacity) return fail(Error);
-  if ((e = device_alloc(&wq, h[0], s))) return fail(cuda_rc(e));
-  if ((e = launch_quantize_mbvh(wn, h[0], wq, s))) return fail(cuda_rc(e));
   *wnodes_out = wn;
   *wq_out = wq;
   *wcount = h[0];
