@@ -151,6 +151,25 @@ struct CollapseParams {
   const uint32_t* m_total_dev;
 };
 
+// Warp-aggregated reservation of n consecutive entries from *counter: every
+// lane of the warp calls it (n = 0 for nothing), one atomic per warp; the
+// lane's first entry is returned. The top-down passes append to one queue
+// counter per level, whose atomics would otherwise serialise.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t n) {
+  const int lane = threadIdx.x & 31;
+  uint32_t incl = n;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(counter, total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return base + incl - n;
+}
+
 __device__ __forceinline__ void set_slot_box(DMNode& m, int i, const DAabb& b) {
   m.min_x[i] = b.min[0]; m.min_y[i] = b.min[1]; m.min_z[i] = b.min[2];
   m.max_x[i] = b.max[0]; m.max_y[i] = b.max[1]; m.max_z[i] = b.max[2];
@@ -202,9 +221,12 @@ __device__ void mark_escapes(const CollapseParams& p, uint32_t mi, const DMNode&
 }
 
 // merge_nodes(mi, c) without the recursion: fills quad node mi and appends
-// its interior slots (bvh node, quad index) to `next`.
-template <bool TRIS>
-__device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint2* next, uint32_t* next_count) {
+// its interior slots (bvh node, quad index) to `next`. AGG: called by all
+// lanes of a warp (`valid` false for lanes without an item), the queue
+// entries reserved once per warp.
+template <bool TRIS, bool AGG>
+__device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint2* next, uint32_t* next_count,
+                          bool valid = true) {
   const DAabb cur = load_aabb(p.nodes + c);
   DMNode m;
 #pragma unroll
@@ -250,6 +272,14 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
       }
     }
   }
+  uint32_t n_int = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) n_int += (nodes_[i] >= 0 && leafs[i] < 0) ? 1u : 0u;
+  if (!valid) n_int = 0;
+  uint32_t qslot = 0;
+  if (AGG) qslot = warp_reserve(next_count, n_int);
+  else if (n_int) qslot = atomicAdd(next_count, n_int);
+  if (!valid) return;
   uint32_t next_index = mi + 1u;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -259,15 +289,16 @@ __device__ void emit_quad(const CollapseParams& p, uint32_t c, uint32_t mi, uint
       m.children[i] = node;
       m.counts[i] = count;
       continue;
-    } else if (node == -1) {
+    } else if (node < 0) {
+      if (node != -1) atomicOr(p.status, kStatusBadIndex);
       continue;
     }
     const uint32_t g = (uint32_t)node;
     const uint32_t idx = next_index;
     next_index += __ldg(p.cnt_e + g);
+    const uint32_t slot = qslot++;
     if (idx < p.m_total) {
       m.children[i] = (int32_t)idx;
-      uint32_t slot = atomicAdd(next_count, 1u);
       if (slot < p.m_total) next[slot] = make_uint2(g, idx);
       else atomicOr(p.status, kStatusBadIndex);
     } else {
@@ -325,9 +356,12 @@ __global__ void __launch_bounds__(kBlock) k_collapse(CollapseParams p) {
     const uint2* q = p.queue[level & 1];
     uint2* next = p.queue[(level + 1) & 1];
     uint32_t* next_count = p.qcount + ((level + 1) % 3);
-    for (uint32_t k = tid; k < size; k += nthreads) {
-      uint2 item = __ldcg(q + k);
-      emit_quad<TRIS>(p, item.x, item.y, next, next_count);
+    // warp-uniform loop: every lane takes part in the queue reservation
+    for (uint32_t k0 = tid - (threadIdx.x & 31u); k0 < size; k0 += nthreads) {
+      const uint32_t k = k0 + (threadIdx.x & 31u);
+      const bool valid = k < size;
+      const uint2 item = valid ? __ldcg(q + k) : make_uint2(0u, 0u);
+      emit_quad<TRIS, true>(p, item.x, item.y, next, next_count, valid);
     }
     if (tid == 0) p.qcount[(level + 2) % 3] = 0;
     if (!grid_sync(p.bar, G, p.status)) return;
@@ -442,7 +476,7 @@ __global__ void __launch_bounds__(kBlock) k_collapse_segments(SegCollapseParams 
       uint2* qout = p.queue[cur ^ 1] + base;
       for (uint32_t k = threadIdx.x; k < size; k += kBlock) {
         const uint2 item = qin[k];
-        emit_quad<false>(p.c, item.x, item.y, qout, &s_count[cur ^ 1]);
+        emit_quad<false, false>(p.c, item.x, item.y, qout, &s_count[cur ^ 1]);
       }
       __syncthreads();
       if (threadIdx.x == 0) s_count[cur] = 0;
@@ -929,12 +963,18 @@ struct WideCtx {
   uint32_t* status;
 };
 
-__device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next, uint32_t* next_count) {
+// AGG: called by all lanes of a warp (`valid` false for lanes without an
+// item), node indices and queue entries reserved once per warp.
+template <bool AGG>
+__device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next, uint32_t* next_count,
+                          bool valid = true) {
   uint32_t slot[4];
   DAabb box[4];
   int ns = 0;
+  bool ok = valid;
   const DAabb cur = load_aabb(p.nodes + c);
-  if (cur.count >= 0 || cur.left_first < 0) {
+  if (!ok) {
+  } else if (cur.count >= 0 || cur.left_first < 0) {
     slot[0] = c;
     box[0] = cur;
     ns = 1;
@@ -970,17 +1010,23 @@ __device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next
     }
   } else {
     atomicOr(p.status, kStatusBadIndex);
-    return;
+    ok = false;
   }
   uint32_t n_int = 0;
-  for (int i = 0; i < ns; ++i) n_int += (box[i].count < 0 && box[i].left_first >= 0) ? 1u : 0u;
-  uint32_t base = 0;
-  if (n_int) {
+  if (ok)
+    for (int i = 0; i < ns; ++i) n_int += (box[i].count < 0 && box[i].left_first >= 0) ? 1u : 0u;
+  uint32_t base = 0, qbase = 0;
+  if (AGG) {
+    base = warp_reserve(p.alloc, n_int);
+    qbase = warp_reserve(next_count, n_int);
+  } else if (n_int) {
     base = atomicAdd(p.alloc, n_int);
-    if (base + n_int > p.alloc_end) {
-      atomicOr(p.status, kStatusBadIndex);
-      return;
-    }
+    qbase = atomicAdd(next_count, n_int);
+  }
+  if (!ok) return;
+  if (n_int && base + n_int > p.alloc_end) {
+    atomicOr(p.status, kStatusBadIndex);
+    return;
   }
   DMNode m;
   uint32_t k = 0;
@@ -996,10 +1042,10 @@ __device__ void emit_wide(const WideCtx& p, uint32_t c, uint32_t wi, uint2* next
       m.children[i] = b.left_first;
       m.counts[i] = b.count;
     } else {
+      const uint32_t q = qbase + k;
       const uint32_t child = base + k++;
       m.children[i] = (int32_t)child;
       m.counts[i] = -1;
-      const uint32_t q = atomicAdd(next_count, 1u);
       if (q < p.next_cap) next[q] = make_uint2(slot[i], child);
       else atomicOr(p.status, kStatusBadIndex);
     }
@@ -1032,9 +1078,12 @@ __global__ void __launch_bounds__(kBlock) k_wide_collapse(WideParams p) {
     const uint2* q = p.queue[level & 1];
     uint2* next = p.queue[(level + 1) & 1];
     uint32_t* next_count = p.qcount + ((level + 1) % 3);
-    for (uint32_t k = tid; k < size; k += nthreads) {
-      const uint2 item = __ldcg(q + k);
-      emit_wide(ctx, item.x, item.y, next, next_count);
+    // warp-uniform loop: every lane takes part in the reservations
+    for (uint32_t k0 = tid - (threadIdx.x & 31u); k0 < size; k0 += nthreads) {
+      const uint32_t k = k0 + (threadIdx.x & 31u);
+      const bool valid = k < size;
+      const uint2 item = valid ? __ldcg(q + k) : make_uint2(0u, 0u);
+      emit_wide<true>(ctx, item.x, item.y, next, next_count, valid);
     }
     if (tid == 0) p.qcount[(level + 2) % 3] = 0;
     if (!grid_sync(p.bar, G, p.status)) return;
@@ -1145,7 +1194,7 @@ __global__ void __launch_bounds__(kBlock)
       uint2* qout = (cur ? q0 : q1) + off;
       for (uint32_t k = threadIdx.x; k < size; k += kBlock) {
         const uint2 item = qin[k];
-        emit_wide(ctx, item.x, item.y, qout, &s_count[cur ^ 1]);
+        emit_wide<false>(ctx, item.x, item.y, qout, &s_count[cur ^ 1]);
       }
       __syncthreads();
       if (threadIdx.x == 0) s_count[cur] = 0;
