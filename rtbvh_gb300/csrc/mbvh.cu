@@ -26,6 +26,16 @@ namespace {
 constexpr int kBlock = 256;
 constexpr uint32_t kNone = 0xffffffffu;
 
+// Arrival at a parent in the bottom-up walks: atomic add with acquire and
+// release semantics at device scope. The release publishes this thread's
+// writes for its child; the second arrival's acquire makes the sibling's
+// writes visible to it (one instruction where fence + add + fence were).
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t* p) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
 __device__ __forceinline__ bool box_contains(const DAabb& outer, const DAabb& inner) {
   // false on NaN: such a box counts as not containing
   return outer.min[0] <= inner.min[0] && outer.min[1] <= inner.min[1] && outer.min[2] <= inner.min[2] &&
@@ -104,13 +114,11 @@ __global__ void __launch_bounds__(kBlock)
     }
     store_aabb(tri.tb + c, box);
   }
-  __threadfence();
   uint32_t x = c;
   for (uint32_t steps = 0; steps < node_count; ++steps) {
     uint32_t p = __ldcg(parent + x);
     if (p == kNone) break;
-    if (atomicAdd(arrive + p, 1u) == 0u) break;  // first arrival: the sibling finishes p
-    __threadfence();
+    if (arrive_acq_rel(arrive + p) == 0u) break;  // first arrival: the sibling finishes p
     DAabb pn = load_aabb(nodes + p);
     uint32_t lf = (uint32_t)pn.left_first;
     uint32_t e = 1u + __ldcg(cnt_o + lf) + __ldcg(cnt_o + lf + 1);
@@ -125,7 +133,6 @@ __global__ void __launch_bounds__(kBlock)
       }
       store_aabb(tri.tb + p, pn);
     }
-    __threadfence();
     x = p;
   }
 }
@@ -516,13 +523,11 @@ __global__ void __launch_bounds__(kBlock)
   }
   store_aabb(nodes + c, box);
   if (nd.left_first < 0) return;
-  __threadfence();
   uint32_t x = c;
   for (uint32_t steps = 0; steps < node_count; ++steps) {
     uint32_t p = __ldcg(parent + x);
     if (p == kNone) break;
-    if (atomicAdd(arrive + p, 1u) == 0u) break;
-    __threadfence();
+    if (arrive_acq_rel(arrive + p) == 0u) break;
     DAabb pn = load_aabb_cg(nodes + p);
     const uint32_t lf = (uint32_t)pn.left_first;
     DAabb l = load_aabb_cg(nodes + lf), r = load_aabb_cg(nodes + lf + 1);
@@ -533,7 +538,6 @@ __global__ void __launch_bounds__(kBlock)
       pn.max[a] = mx + 0.0001f;
     }
     store_aabb(nodes + p, pn);
-    __threadfence();
     x = p;
   }
 }
