@@ -33,6 +33,10 @@ _Static_assert(sizeof(ResultCode) == 4 && sizeof(BvhType) == 4, "enums are 32-bi
 _Static_assert(Ok == 0 && Error == 1 && NoPrimitives == 2 && InequalAabbsAndPrimitives == 3 && Nan == 4,
                "ResultCode values");
 _Static_assert(LocallyOrderedClustered == 0 && BinnedSAH == 1, "BvhType values");
+/* this library's trace flags: distinct bits */
+_Static_assert(RTBVH_TRACE_ANY_HIT == 1u && RTBVH_TRACE_STATS == 2u && RTBVH_TRACE_REORDER == 4u &&
+                   RTBVH_TRACE_EXACT_NODES == 8u && RTBVH_TRACE_WALK_STATS == 16u,
+               "trace flags");
 
 static int failures = 0;
 #define CHECK(cond)                                                  \

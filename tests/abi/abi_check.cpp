@@ -37,6 +37,9 @@ static_assert(std::is_same<std::underlying_type<BvhType>::type, uint32_t>::value
 static_assert(sizeof(ResultCode) == 4, "ResultCode is a C enum");
 static_assert(static_cast<int>(ResultCode::Nan) == 4 && static_cast<uint32_t>(BvhType::BinnedSAH) == 1, "values");
 static_assert(std::is_standard_layout<RTAabb>::value && std::is_trivially_copyable<RTMbvhNode>::value, "POD");
+static_assert(RTBVH_TRACE_ANY_HIT == 1u && RTBVH_TRACE_STATS == 2u && RTBVH_TRACE_REORDER == 4u &&
+                  RTBVH_TRACE_EXACT_NODES == 8u && RTBVH_TRACE_WALK_STATS == 16u,
+              "trace flags, the same bits as rtbvh.h");
 
 static int failures = 0;
 #define CHECK(cond)                                                               \

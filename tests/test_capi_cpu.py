@@ -218,3 +218,13 @@ def test_host_callback_traversal_matches_oracle_on_teapot(lib, golden):
                                 d.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(t), None, cb)
         assert rc == 0
         assert np.float32(t.value) == want[r, 0]
+
+
+def test_python_flag_constants_equal_the_header():
+    """The ctypes layer's flag constants are the values include/rtbvh.h
+    defines (RTBVH_TRACE_* and RTBVH_FLAG_NO_HOST_MIRROR)."""
+    header = open(os.path.join(os.path.dirname(__file__), "..", "include", "rtbvh.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define (RTBVH_\w+) (\d+)u", header)}
+    for name in ("ANY_HIT", "STATS", "REORDER", "EXACT_NODES", "WALK_STATS"):
+        assert getattr(_ffi, "TRACE_" + name) == defs["RTBVH_TRACE_" + name]
+    assert _ffi.FLAG_NO_HOST_MIRROR == defs["RTBVH_FLAG_NO_HOST_MIRROR"]
