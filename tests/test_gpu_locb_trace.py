@@ -343,6 +343,40 @@ def test_compact_nodes_rays_from_inside_the_scene(name, kind):
     assert (rb.hit_prims(hits) >= 0).sum() > len(rays) // 20
 
 
+def test_handed_on_pass_with_far_triangles_and_inside_origins():
+    """A binned-SAH tree (its rays that hit escaped triangles are handed to
+    the exact walk, which skips subtrees by their triangle boxes) where some
+    triangles lie far beyond the compact range: their subtree boxes are the
+    infinite box and must never be skipped. Rays start inside the scene box
+    (the skip applies to them) or far outside it (it does not). Handed-on
+    rays get the exact walk's hits bit for bit; all rays the oracle's
+    nearest hit."""
+    tris = scene("incoherent_20k").copy()
+    far = np.random.default_rng(6).choice(len(tris), 50, replace=False)
+    tris[far] *= np.float32(1e19)
+    g = gpu_build(tris, "sah")
+    m = rb.Mbvh.construct(g)
+    rng = np.random.default_rng(23)
+    n = 65536
+    o = rng.uniform(0.0, 1.0, size=(n, 3))
+    o[:256] = rng.uniform(-1e3, 1e3, size=(256, 3))  # beyond the compact range: exact walk, no skip
+    d = rng.normal(size=(n, 3))
+    rays = np.concatenate([o, d / np.linalg.norm(d, axis=1, keepdims=True)], 1).astype(np.float32)
+    d_rays = to_cuda(rays)
+    hits, ws = m.intersect(d_rays, walk_stats=True)
+    hits, ws = hits.cpu().numpy(), ws.cpu().numpy()
+    exact = m.intersect(d_rays, exact_nodes=True)[0].cpu().numpy()
+    assert m.status() == rb.ResultCode.Ok
+    handed = ws[:, 2] != 0
+    assert handed.sum() >= 256
+    assert np.array_equal(u32(hits[handed]), u32(exact[handed]))
+    assert_same_nearest(hits, exact, tris, rays)
+    on, oi = oracle_build(tris, "sah")
+    oh, _, _ = oracle.trace("mbvh", oracle.mbvh(on), oi, tris.reshape(-1, 9), rays, stats=False)
+    assert_same_nearest(hits, oh, tris, rays)
+    assert (rb.hit_prims(hits) >= 0).sum() > n // 20
+
+
 def test_compact_nodes_out_of_range_values():
     """Triangles far outside the quantisable range put their quad nodes on
     the exact path; rays with huge origins trace the exact nodes entirely.
