@@ -470,7 +470,7 @@ void rtbvh_gpu_batch_free(RTBatch batch);
 /* Launch parameters of a batch; 0 in a field means the default. */
 typedef struct RTBatchTuning {
   uint32_t trace_blocks_per_sm; /* resident traversal blocks per SM (default: occupancy limit) */
-  uint32_t trace_ray_batch;     /* rays a warp takes from the global ray counter at a time (default 128, at most 4096) */
+  uint32_t trace_ray_batch;     /* rays a warp takes from the global ray counter at a time (0: the library's default, 32; at most 4096) */
   uint32_t cluster_min_prims;   /* meshes with more primitives get a thread-block cluster (default 4096) */
   float pipeline_ms;            /* tune: measured build + trace time with the chosen values */
   uint32_t trace_stack;         /* stack entries per ray of the closest-hit walk: 32, 48 or 64

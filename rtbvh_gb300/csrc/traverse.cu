@@ -179,7 +179,12 @@ __device__ __forceinline__ int sel4(const int4& v, uint32_t i) {
 // has finished takes the next ray from a warp-local pool (refilled `batch`
 // rays at a time from the global counter), so the warp's lanes stay busy
 // instead of idling until the warp's slowest ray ends.
-constexpr uint32_t kPoolBatch = 128;  // default rays per pool refill (TraceArgs::ray_batch)
+// Default rays per pool refill (TraceArgs::ray_batch). Small batches keep the
+// end of a launch short (the last warps hold few rays); measured on one GB300
+// against 128: the 1M incoherent scene +0.9 %, the 6,400-triangle sphere's
+// camera +20 %, the 200k-triangle camera -4 % time (64, 16: less on one or
+// the other; 256, 512: slower everywhere).
+constexpr uint32_t kPoolBatch = 32;
 
 struct WarpPool {
   uint32_t next = 0, end = 0;  // warp-uniform (ray counts < 2^32 - 2^25)
