@@ -1076,6 +1076,10 @@ cudaError_t launch_any(const TraceArgs& a0, cudaStream_t s) {
   if (a0.stack_limit != 0 && a0.stack_limit != 32 && a0.stack_limit != 48 && a0.stack_limit != 64)
     return cudaErrorInvalidValue;
   TraceArgs a = a0;
+  // any hit: most walks end after a few nodes, so refills are frequent and
+  // larger pools cost fewer counter atomics (128: 34.0 against 28.7 Grays/s
+  // with 32 on the 1M incoherent scene's occlusion rays)
+  if (a.any_hit && a.ray_batch == 0) a.ray_batch = 128u;
   Scratch<unsigned int> work;
   Scratch<uint32_t> keys, order, acc, deferred;
   Scratch<char> sort_temp;
