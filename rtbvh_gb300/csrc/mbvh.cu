@@ -1250,7 +1250,7 @@ ResultCode build_wide(const DAabb* nodes, uint32_t node_count, const uint32_t* i
   const unsigned node_blocks = (node_count + kBlock - 1) / kBlock;
   // status[1]: not nested, or leaves that are not whole primitives once
   // each -> no traversal tree (closest hit uses the exact nodes); the
-  // collapse reads the verdict on the device and does nothing then
+  // collapse reads the result on the device and does nothing then
   const bool checked = !nested || indices;
   Scratch<uint32_t> seen;
   if (checked) {
